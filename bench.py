@@ -1,0 +1,345 @@
+"""Benchmark: suffix-array construction throughput (Msuffixes/s) on GB300.
+
+Workload (default): the DNA-like text with planted repeats — n = 2^28 u8
+symbols over {0,1,2,3}, 30% of positions covered by copies of log-uniform
+length 100..10,000 taken from earlier offsets with 1% substitutions — built
+with build_in_memory (PlainText, u32 index).  Synthetic and seeded (no public
+dataset backs this workload).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours:       one JSON line; `value` = suffixes/s with the text resident in HBM
+            (device pointers through the C ABI), `e2e` = the same call with
+            pinned host text and host output (copies inside the timed region).
+reference:  the reference's CPU algorithm (the C restatement in oracle/, the
+            Rust crate cannot be built here) on the host cores, each step a
+            bounded prefix of the same text.
+N > 1:      independent replicas, one per GPU (the path has no exchange step);
+            value = all ranks' suffixes / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "caps-sa_gb300"))
+
+import numpy as np  # noqa: E402
+
+CPU_SAMPLE_LOG2 = 24  # bounded CPU sample: the first 2^24 symbols of the text
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--log2n", type=int, default=28)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload(log2n, seed=2):
+    from capssa import workloads
+    return workloads.dna_with_repeats(1 << log2n, seed=seed)
+
+
+def config(log2n, n):
+    return {"workload": "dna-repeats: n=2^%d u8 over {0,1,2,3}, 30%% planted repeats "
+                        "(log-uniform 100..10000, 1%% substitutions), build_in_memory "
+                        "PlainText, u32 index" % log2n,
+            "n": n, "symbol": "u8", "index": "u32", "limits": "PlainText",
+            "l2": "no flush: inputs (256 MiB text, ~4 GiB working set) exceed the 129 MB L2",
+            "parallelism": "replicas (one independent text per GPU)"}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0, None
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    return rank, ws, local, dist
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------------ peaks / profile
+
+def hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(n):
+    """DRAM bytes per radix-pass launch from the committed ncu summary,
+    scaled by pairs per launch (traffic grows linearly with pairs)."""
+    p = os.path.join(ROOT, "profiles", "radix_onesweep_pass.txt")
+    try:
+        vals = {}
+        for ln in open(p):
+            if ":" in ln:
+                k, v = ln.split(":", 1)
+                vals[k.strip()] = v.strip().split()[0]
+        per_pair = float(vals["dram_bytes_per_pair"])
+        return per_pair * n
+    except Exception:
+        return None
+
+
+# ------------------------------------------------------------------ CPU baseline
+
+def cpu_baseline(text, repeats=3):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    sample = np.ascontiguousarray(text[: 1 << CPU_SAMPLE_LOG2])
+    cores = oracle.max_threads()
+    oracle.build_in_memory(sample[: 1 << 20])  # warm-up
+    times = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        oracle.build_in_memory(sample)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    return {"value": len(sample) / t / 1e6, "unit": "Msuffixes/s", "cores": cores,
+            "kind": "port",
+            "sample": "build_in_memory restated in C (merge sort + LCP merge, OpenMP tasks) on "
+                      "the first 2^%d symbols of the workload text; median of %d"
+                      % (CPU_SAMPLE_LOG2, repeats)}
+
+
+def run_reference(args):
+    rank, ws, local, dist = dist_init()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    log2n = args.log2n
+    text = workload(log2n)
+    sample = np.ascontiguousarray(text[: 1 << min(CPU_SAMPLE_LOG2, log2n)])
+    cores = oracle.max_threads()
+    for _ in range(args.warmup):
+        oracle.build_in_memory(sample[: 1 << 20])
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.build_in_memory(sample)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = len(sample) * args.steps / total / 1e6
+    line = {"impl": "reference", "metric": "Msuffixes/s", "value": value, "unit": "Msuffixes/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": config(log2n, 1 << log2n),
+            "cpu_baseline": {"value": value, "unit": "Msuffixes/s", "cores": cores,
+                             "kind": "port",
+                             "sample": "first 2^%d symbols of the workload text per step; the "
+                                       "Rust crate cannot be built here, so its algorithm "
+                                       "restated in C (oracle/) runs instead"
+                                       % (CPU_SAMPLE_LOG2)},
+            "e2e": {"value": value, "unit": "Msuffixes/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ our arm
+
+def run_ours(args):
+    import torch
+
+    import capssa
+
+    rank, ws, local, dist = dist_init()
+    torch.cuda.set_device(local)
+    if dist is not None:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    log2n = args.log2n
+    n = 1 << log2n
+    text = workload(log2n, seed=2 + rank)
+    ctx = capssa.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+
+    t_dev = torch.from_numpy(text).to("cuda")
+    sa_dev = torch.empty(n, dtype=torch.int32, device="cuda")
+    for _ in range(args.warmup):
+        ctx.build_in_memory(t_dev, out=sa_dev)
+    torch.cuda.synchronize()
+
+    # correctness guard on the timed configuration: a permutation check on
+    # the device (every position appears once)
+    seen = torch.zeros(n, dtype=torch.int32, device="cuda")
+    seen.index_add_(0, sa_dev.long(), torch.ones(n, dtype=torch.int32, device="cuda"))
+    if not bool((seen == 1).all()):
+        raise SystemExit("suffix array is not a permutation")
+    del seen
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    launches = 0
+    pass_ms, passes, phase = [], [], {"keys_ms": 0, "sort_ms": 0, "refine_ms": 0, "finish_ms": 0}
+    rounds = 0
+    ev0.record(stream)
+    for _ in range(args.steps):
+        ctx.build_in_memory(t_dev, out=sa_dev)
+        st = ctx.stats()
+        launches += st["kernel_launches"]
+        pass_ms.append(st["sort_pass_ms"])
+        passes.append(st["sort_passes"])
+        rounds = st["refine_rounds"]
+        for k in phase:
+            phase[k] += st[k] / args.steps
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    if dist is not None:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    ms_per_step = elapsed_ms / args.steps
+    value = n * ws * args.steps / (elapsed_ms / 1e3) / 1e6
+
+    # roofline of the dominant kernel: one onesweep radix pass over n
+    # (key u64, value u32) pairs reads and writes 12 B per pair
+    peak, peak_kind = hbm_peak()
+    avg_pass_ms = sum(pass_ms) / max(1, sum(passes))
+    alg_bytes = 24.0 * n
+    achieved = alg_bytes / (avg_pass_ms / 1e3) / 1e9
+    traffic = profiled_traffic(n)
+    roofline = {"kernel": "radix onesweep pass (initial 64-bit key sort)", "bound": "hbm",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_kind": peak_kind, "traffic": traffic,
+                "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_pass_ms,
+                "launches_per_step": sum(passes) / len(passes),
+                "phase_ms": phase, "refine_rounds": rounds}
+
+    e2e = None
+    if not args.no_e2e:
+        h_text = torch.from_numpy(text).pin_memory()
+        h_out = torch.empty(n, dtype=torch.int32).pin_memory()
+        ctx.build_in_memory(h_text.numpy(), out=h_out.numpy().view(np.uint32))  # warm
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ctx.build_in_memory(h_text.numpy(), out=h_out.numpy().view(np.uint32))
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        if dist is not None:
+            t = torch.tensor([el], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el = float(t.item())
+        e2e = {"value": n * ws * args.steps / el / 1e6, "unit": "Msuffixes/s",
+               "h2d_bytes_per_step": int(n), "d2h_bytes_per_step": int(4 * n),
+               "ms_per_step": el / args.steps * 1e3}
+        if not np.array_equal(h_out.numpy().view(np.uint32), sa_dev.cpu().numpy().view(np.uint32)):
+            raise SystemExit("host-path suffix array differs from the device-path one")
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(text)
+
+    if rank == 0:
+        line = {"metric": "Msuffixes/s", "value": value, "unit": "Msuffixes/s", "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+                "data": "synthetic (seeded generator, caps-sa_gb300/capssa/workloads.py)",
+                "config": config(log2n, n), "roofline": roofline, "cpu_baseline": cpu,
+                "e2e": e2e, "clocks": clk, "gpu_launches": launches}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

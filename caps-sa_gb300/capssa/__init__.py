@@ -1,0 +1,572 @@
+"""Python mirror of caps-sa's in-memory suffix-array API over the GB300 C ABI.
+
+Names and argument meanings follow the reference crate (caps-sa 0.7.0):
+
+    build_in_memory(text)                               src/sample_sort.rs:97
+    build_in_memory_with_opts(text, opts)               src/sample_sort.rs:106
+    build_in_memory_with(text, lp, opts)                src/sample_sort.rs:118
+    build_in_memory_for_positions(text, positions)      src/sample_sort.rs:143
+    build_in_memory_for_positions_with_opts(...)        src/sample_sort.rs:152
+    build_in_memory_for_positions_with(...)             src/sample_sort.rs:168
+    build_in_memory_sample_sort(text, opts, emit)       src/ext_mem.rs:717
+    try_build_in_memory_sample_sort(...)                src/ext_mem.rs:726
+    build_in_memory_sample_sort_with(...)               src/ext_mem.rs:740
+    build_in_memory_sample_sort_for_positions[_with]    src/ext_mem.rs:787, 824
+    lcp / suffix_cmp / LcpDispatch                      src/lcp.rs:125-216
+    PlainText / SegmentedText / BoundaryRank            src/limits.rs:107-336
+    Opts / ExtMemOpts                                   src/sample_sort.rs:70-85,
+                                                        src/ext_mem.rs:60-118
+
+Texts are numpy arrays of uint8/uint16/uint32 (or CUDA tensors exposing
+``data_ptr()``); the index type is chosen like the reference's generic
+``I: Index`` (``index=np.uint32`` or ``np.uint64``).  Contract violations the
+reference panics on raise ``ValueError``; emit aborts raise ``BuildError``.
+
+Every call runs the CUDA library; there is no CPU fallback, and importing
+this module fails loudly when the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import os
+import threading
+from dataclasses import dataclass, field
+from typing import Callable, Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "_build", "libcapssa_gb300.so")
+
+UNBOUNDED = (1 << 64) - 1
+
+
+class Status(enum.IntEnum):
+    OK = 0
+    EINVAL = 1
+    ENOMEM = 2
+    ECUDA = 3
+    ETIMEOUT = 4
+    EEMIT = 5
+    EUNSUPPORTED = 6
+
+
+class CapsSaError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (Status(status).name, message))
+        self.status = Status(status)
+
+
+class BuildError(CapsSaError):
+    """BuildError::Emit (src/ext_mem.rs:258-264): the emit callback aborted."""
+
+    def __init__(self, status, message, inner=None):
+        super().__init__(status, message)
+        self.inner = inner
+
+
+class BoundaryRank(enum.IntEnum):
+    """src/limits.rs:113-123."""
+    SHORTER_FIRST = 0
+    LONGER_FIRST = 1
+
+
+class Partition(enum.IntEnum):
+    AUTO = 0
+    SPLITTERS = 1
+    LEARNED = 2
+
+
+class _Limits(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("boundary", C.c_int32),
+                ("ends", C.c_void_p), ("n_ends", C.c_uint64)]
+
+
+class _Opts(C.Structure):
+    _fields_ = [("max_context", C.c_uint64), ("subproblem_count", C.c_uint64),
+                ("partition", C.c_int32), ("host_threads", C.c_int32),
+                ("reserved", C.c_uint64 * 6)]
+
+
+class _Stats(C.Structure):
+    _fields_ = [("n_suffixes", C.c_uint64), ("key_symbols", C.c_uint32),
+                ("key_bits_per_symbol", C.c_uint32), ("refine_rounds", C.c_uint32),
+                ("partitions", C.c_uint32), ("refined_suffixes", C.c_uint64),
+                ("max_partition", C.c_uint64), ("mispredicted", C.c_uint64),
+                ("kernel_launches", C.c_uint64), ("device_ms", C.c_double),
+                ("h2d_ms", C.c_double), ("d2h_ms", C.c_double), ("h2d_bytes", C.c_uint64),
+                ("d2h_bytes", C.c_uint64), ("keys_ms", C.c_double), ("sort_ms", C.c_double),
+                ("refine_ms", C.c_double), ("finish_ms", C.c_double),
+                ("sort_passes", C.c_uint32), ("reserved0", C.c_uint32),
+                ("sort_pass_ms", C.c_double)]
+
+
+class _Packer(C.Structure):
+    _fields_ = [("bits", C.c_uint32), ("k", C.c_uint32), ("alphabet", C.c_uint32),
+                ("identity", C.c_uint32), ("code", C.c_uint8 * 256)]
+
+
+EMIT_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_uint64), C.c_uint64)
+
+_SYM = {np.dtype(np.uint8): "u8", np.dtype(np.uint16): "u16", np.dtype(np.uint32): "u32"}
+_IDX = {np.dtype(np.uint32): "u32", np.dtype(np.uint64): "u64"}
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libcapssa_gb300.so is not built (run caps-sa_gb300/build.py "
+                          "or __graft_entry__.build()); there is no CPU fallback")
+    L = C.CDLL(LIB_PATH)
+    vp, u64, i32 = C.c_void_p, C.c_uint64, C.c_int32
+    L.capssa_ctx_create.argtypes = [C.POINTER(vp), C.c_int]
+    L.capssa_ctx_destroy.argtypes = [vp]
+    L.capssa_ctx_last_error.argtypes = [vp]
+    L.capssa_ctx_last_error.restype = C.c_char_p
+    L.capssa_ctx_stats.argtypes = [vp, C.POINTER(_Stats)]
+    L.capssa_ctx_workspace_bytes.argtypes = [vp]
+    L.capssa_ctx_workspace_bytes.restype = u64
+    L.capssa_ctx_trim.argtypes = [vp]
+    L.capssa_ctx_set_stream.argtypes = [vp, vp]
+    L.capssa_opts_default.argtypes = [C.POINTER(_Opts)]
+    for s in ("u8", "u16", "u32"):
+        for i in ("u32", "u64"):
+            getattr(L, "capssa_build_in_memory_%s_%s" % (s, i)).argtypes = [
+                vp, vp, u64, C.POINTER(_Limits), C.POINTER(_Opts), vp]
+            getattr(L, "capssa_build_in_memory_for_positions_%s_%s" % (s, i)).argtypes = [
+                vp, vp, u64, vp, u64, C.POINTER(_Limits), C.POINTER(_Opts), vp]
+            getattr(L, "capssa_build_in_memory_lcp_%s_%s" % (s, i)).argtypes = [
+                vp, vp, u64, vp, u64, C.POINTER(_Limits), C.POINTER(_Opts), vp, vp]
+            getattr(L, "capssa_merge_%s_%s" % (s, i)).argtypes = [
+                vp, vp, u64, C.POINTER(_Limits), vp, vp, u64, vp, vp, u64, u64, vp, vp]
+            getattr(L, "capssa_build_batched_%s_%s" % (s, i)).argtypes = [
+                vp, vp, vp, u64, C.POINTER(_Opts), vp]
+        getattr(L, "capssa_build_in_memory_sample_sort_%s" % s).argtypes = [
+            vp, vp, u64, C.POINTER(_Limits), C.POINTER(_Opts), EMIT_FN, vp]
+        getattr(L, "capssa_build_in_memory_sample_sort_for_positions_%s" % s).argtypes = [
+            vp, vp, u64, vp, u64, C.POINTER(_Limits), C.POINTER(_Opts), EMIT_FN, vp]
+        getattr(L, "capssa_lcp_%s" % s).argtypes = [vp, vp, u64, vp, vp, u64, u64, vp]
+        getattr(L, "capssa_suffix_cmp_%s" % s).argtypes = [
+            vp, vp, u64, C.POINTER(_Limits), vp, vp, u64, u64, vp]
+    L.capssa_pack_params_u8.argtypes = [vp, vp, u64, i32, u64, C.POINTER(_Packer),
+                                        C.POINTER(i32)]
+    L.capssa_pack_keys_u8.argtypes = [vp, vp, u64, C.POINTER(_Packer), C.POINTER(_Limits), vp,
+                                      u64, vp]
+    for i in ("u32", "u64"):
+        getattr(L, "capssa_seed_subarray_u8_%s" % i).argtypes = [
+            vp, vp, u64, C.POINTER(_Packer), C.POINTER(_Limits), vp, vp, u64]
+    return L
+
+
+lib = _load()
+
+
+# ------------------------------------------------------------------ providers
+
+class PlainText:
+    """lim_at(p) = n - p (src/limits.rs:125-156)."""
+
+    def __init__(self, n: int, boundary: BoundaryRank = BoundaryRank.SHORTER_FIRST):
+        self.n = int(n)
+        self.boundary = BoundaryRank(boundary)
+
+    def _c(self):
+        return _Limits(0, int(self.boundary), None, 0)
+
+
+class SegmentedText:
+    """Segments at cumulative ends (src/limits.rs:158-336).  The STAR order of
+    the reference's tests (lim_b.cmp(lim_a).then(p_a.cmp(p_b))) is
+    ``boundary=BoundaryRank.LONGER_FIRST``."""
+
+    def __init__(self, text_len: int, ends, boundary: BoundaryRank = BoundaryRank.SHORTER_FIRST):
+        self.n = int(text_len)
+        self.ends = np.ascontiguousarray(ends, dtype=np.uint64)
+        self.boundary = BoundaryRank(boundary)
+        if len(self.ends):
+            if np.any(self.ends[1:] <= self.ends[:-1]):
+                raise ValueError("SegmentedText::from_ends: ends must be strictly increasing")
+            if int(self.ends[-1]) != self.n:
+                raise ValueError("SegmentedText::from_ends: last end (%d) != text_len (%d)"
+                                 % (int(self.ends[-1]), self.n))
+        elif self.n != 0:
+            raise ValueError("SegmentedText::from_ends: empty ends but text_len != 0")
+
+    @classmethod
+    def from_lengths(cls, text_len, lengths, boundary=BoundaryRank.SHORTER_FIRST):
+        ends = np.cumsum(np.asarray(lengths, dtype=np.uint64), dtype=np.uint64)
+        total = int(ends[-1]) if len(ends) else 0
+        if total != int(text_len):
+            raise ValueError("SegmentedText::from_lengths: per-segment lengths sum to %d but "
+                             "text_len is %d" % (total, int(text_len)))
+        return cls(text_len, ends, boundary)
+
+    @classmethod
+    def from_ends(cls, text_len, ends, boundary=BoundaryRank.SHORTER_FIRST):
+        return cls(text_len, ends, boundary)
+
+    def n_segments(self):
+        return len(self.ends)
+
+    def _c(self):
+        return _Limits(1, int(self.boundary), self.ends.ctypes.data, len(self.ends))
+
+
+@dataclass
+class Opts:
+    """src/sample_sort.rs:70-85."""
+    max_context: int = UNBOUNDED
+
+
+@dataclass
+class ExtMemOpts:
+    """The in-memory subset of src/ext_mem.rs:60-118."""
+    max_context: int = UNBOUNDED
+    subproblem_count: int = 0
+    partition: Partition = Partition.AUTO
+    host_threads: int = 0
+
+
+def _copts(o) -> _Opts:
+    c = _Opts()
+    lib.capssa_opts_default(C.byref(c))
+    if o is not None:
+        c.max_context = int(getattr(o, "max_context", UNBOUNDED))
+        c.subproblem_count = int(getattr(o, "subproblem_count", 0))
+        c.partition = int(getattr(o, "partition", 0))
+        c.host_threads = int(getattr(o, "host_threads", 0))
+    return c
+
+
+# ------------------------------------------------------------------ buffers
+
+def _is_cuda_tensor(a):
+    return hasattr(a, "data_ptr") and getattr(getattr(a, "device", None), "type", "") == "cuda"
+
+
+def _ptr_len_dtype(a):
+    """(address, length, numpy dtype) of a numpy array or CUDA tensor."""
+    if _is_cuda_tensor(a):
+        import torch
+        m = {torch.uint8: np.uint8, torch.int32: np.uint32, torch.int64: np.uint64}
+        if hasattr(torch, "uint16"):
+            m[torch.uint16] = np.uint16
+        if hasattr(torch, "uint32"):
+            m[torch.uint32] = np.uint32
+        if hasattr(torch, "uint64"):
+            m[torch.uint64] = np.uint64
+        if not a.is_contiguous():
+            raise ValueError("CUDA tensors must be contiguous")
+        return a.data_ptr(), a.numel(), np.dtype(m[a.dtype])
+    a = np.ascontiguousarray(a)
+    return a.ctypes.data, len(a), a.dtype
+
+
+def _text(text):
+    if isinstance(text, (bytes, bytearray)):
+        text = np.frombuffer(bytes(text), dtype=np.uint8)
+    if not _is_cuda_tensor(text):
+        text = np.ascontiguousarray(text)
+    ptr, n, dt = _ptr_len_dtype(text)
+    if dt not in _SYM:
+        raise TypeError("symbols must be uint8, uint16 or uint32, got %s" % dt)
+    return text, ptr, n, _SYM[dt]
+
+
+# ------------------------------------------------------------------ context
+
+class Context:
+    """One GPU context (device memory cache + CUDA stream).  Not thread-safe."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        st = lib.capssa_ctx_create(C.byref(h), int(device))
+        if st != 0:
+            raise CapsSaError(st, "cannot create a context on CUDA device %d" % device)
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib.capssa_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st, inner=None):
+        if st == 0:
+            return
+        msg = lib.capssa_ctx_last_error(self._h).decode()
+        if st == Status.EINVAL:
+            raise ValueError(msg)
+        if st == Status.EEMIT:
+            raise BuildError(st, msg, inner)
+        raise CapsSaError(st, msg)
+
+    def stats(self) -> dict:
+        s = _Stats()
+        lib.capssa_ctx_stats(self._h, C.byref(s))
+        return {k: getattr(s, k) for k, _ in _Stats._fields_}
+
+    def workspace_bytes(self) -> int:
+        return int(lib.capssa_ctx_workspace_bytes(self._h))
+
+    def trim(self):
+        lib.capssa_ctx_trim(self._h)
+
+    def set_stream(self, stream_ptr: int):
+        self._check(lib.capssa_ctx_set_stream(self._h, C.c_void_p(stream_ptr)))
+
+    # ---- builders
+
+    def build_in_memory(self, text, lp=None, opts=None, index=np.uint32, out=None):
+        """build_in_memory / _with_opts / _with (src/sample_sort.rs:97-127)."""
+        text, tp, n, s = _text(text)
+        idx = np.dtype(index)
+        if lp is not None and lp.n != n:
+            raise ValueError("limit provider length %d != text length %d" % (lp.n, n))
+        if out is None:
+            out = np.empty(n, dtype=idx)
+        op, _, odt = _ptr_len_dtype(out)
+        fn = getattr(lib, "capssa_build_in_memory_%s_%s" % (s, _IDX[odt]))
+        lim = (lp or PlainText(n))._c()
+        o = _copts(opts)
+        self._check(fn(self._h, tp, n, C.byref(lim), C.byref(o), op))
+        return out
+
+    def build_in_memory_for_positions(self, text, positions, lp=None, opts=None, out=None):
+        """build_in_memory_for_positions[_with[_opts]] (src/sample_sort.rs:143-206)."""
+        text, tp, n, s = _text(text)
+        if not _is_cuda_tensor(positions):
+            positions = np.ascontiguousarray(positions)
+            if positions.dtype not in (np.uint32, np.uint64):
+                positions = positions.astype(np.uint64)
+        pp, m, pdt = _ptr_len_dtype(positions)
+        if out is None:
+            out = np.empty(m, dtype=pdt)
+        op, _, _ = _ptr_len_dtype(out)
+        fn = getattr(lib, "capssa_build_in_memory_for_positions_%s_%s" % (s, _IDX[pdt]))
+        lim = (lp or PlainText(n))._c()
+        o = _copts(opts)
+        self._check(fn(self._h, tp, n, pp, m, C.byref(lim), C.byref(o), op))
+        return out
+
+    def build_in_memory_lcp(self, text, positions=None, lp=None, opts=None, index=np.uint32):
+        """Suffix array plus merge_sort's LCP postcondition
+        (src/sample_sort.rs:208-216)."""
+        text, tp, n, s = _text(text)
+        if positions is not None:
+            positions = np.ascontiguousarray(positions, dtype=index)
+            m = len(positions)
+            pp = positions.ctypes.data
+        else:
+            m, pp = n, None
+        sa = np.empty(m, dtype=index)
+        lcp = np.empty(m, dtype=index)
+        fn = getattr(lib, "capssa_build_in_memory_lcp_%s_%s" % (s, _IDX[np.dtype(index)]))
+        lim = (lp or PlainText(n))._c()
+        o = _copts(opts)
+        self._check(fn(self._h, tp, n, pp, m if positions is not None else 0, C.byref(lim),
+                       C.byref(o), sa.ctypes.data, lcp.ctypes.data))
+        return sa, lcp
+
+    def try_build_in_memory_sample_sort(self, text, opts=None, emit=None, lp=None,
+                                        positions=None):
+        """try_build_in_memory_sample_sort[_for_positions]_with
+        (src/ext_mem.rs:726-871).  `emit(batch: np.ndarray[u64])` is called in
+        suffix order; raising from it aborts with BuildError."""
+        text, tp, n, s = _text(text)
+        err = {}
+
+        def cb(user, ptr, length):
+            try:
+                arr = np.ctypeslib.as_array(ptr, shape=(length,))
+                r = emit(arr)
+                return 0 if r is None or r == 0 or r is True else 1
+            except BaseException as e:  # the callback must not unwind through C
+                err["e"] = e
+                return 1
+
+        cfn = EMIT_FN(cb)
+        lim = (lp or PlainText(n))._c()
+        o = _copts(opts)
+        if positions is None:
+            st = getattr(lib, "capssa_build_in_memory_sample_sort_%s" % s)(
+                self._h, tp, n, C.byref(lim), C.byref(o), cfn, None)
+        else:
+            pos = np.ascontiguousarray(positions, dtype=np.uint64)
+            st = getattr(lib, "capssa_build_in_memory_sample_sort_for_positions_%s" % s)(
+                self._h, tp, n, pos.ctypes.data, len(pos), C.byref(lim), C.byref(o), cfn, None)
+        self._check(st, err.get("e"))
+
+    def build_in_memory_sample_sort(self, text, opts=None, emit=None, lp=None, positions=None):
+        """build_in_memory_sample_sort[_with|_for_positions[_with]]
+        (src/ext_mem.rs:717, 740, 787, 824); without `emit` the emitted
+        positions are collected and returned."""
+        if emit is None:
+            chunks = []
+            self.try_build_in_memory_sample_sort(text, opts, lambda b: chunks.append(b.copy()),
+                                                 lp, positions)
+            return np.concatenate(chunks) if chunks else np.zeros(0, dtype=np.uint64)
+        self.try_build_in_memory_sample_sort(text, opts, emit, lp, positions)
+        return None
+
+    def build_batched(self, texts, offsets, index=np.uint32, opts=None):
+        """Many independent texts: out[offsets[t]:offsets[t+1]] is the SA of
+        texts[offsets[t]:offsets[t+1]] in local positions."""
+        text, tp, n, s = _text(texts)
+        offs = np.ascontiguousarray(offsets, dtype=np.uint64)
+        out = np.empty(n, dtype=index)
+        fn = getattr(lib, "capssa_build_batched_%s_%s" % (s, _IDX[np.dtype(index)]))
+        o = _copts(opts)
+        self._check(fn(self._h, tp, offs.ctypes.data, len(offs) - 1, C.byref(o),
+                       out.ctypes.data))
+        return out
+
+    # ---- primitives
+
+    def lcp(self, text, p, q, max_ctx=UNBOUNDED):
+        """LcpDispatch::lcp over arrays of pairs (src/lcp.rs:125-153)."""
+        text, tp, n, s = _text(text)
+        p = np.ascontiguousarray(np.atleast_1d(p), dtype=np.uint64)
+        q = np.ascontiguousarray(np.atleast_1d(q), dtype=np.uint64)
+        out = np.empty(len(p), dtype=np.uint64)
+        self._check(getattr(lib, "capssa_lcp_%s" % s)(self._h, tp, n, p.ctypes.data,
+                                                       q.ctypes.data, len(p), int(max_ctx),
+                                                       out.ctypes.data))
+        return out
+
+    def suffix_cmp(self, text, p, q, lp=None, max_ctx=UNBOUNDED):
+        """LcpDispatch::suffix_cmp_with over arrays of pairs (src/lcp.rs:184-201)."""
+        text, tp, n, s = _text(text)
+        p = np.ascontiguousarray(np.atleast_1d(p), dtype=np.uint64)
+        q = np.ascontiguousarray(np.atleast_1d(q), dtype=np.uint64)
+        out = np.empty(len(p), dtype=np.int8)
+        lim = (lp or PlainText(n))._c()
+        self._check(getattr(lib, "capssa_suffix_cmp_%s" % s)(
+            self._h, tp, n, C.byref(lim), p.ctypes.data, q.ctypes.data, len(p), int(max_ctx),
+            out.ctypes.data))
+        return out
+
+    def merge(self, text, x, lcp_x, y, lcp_y, lp=None, max_ctx=UNBOUNDED):
+        """sample_sort::merge (src/sample_sort.rs:397-522)."""
+        text, tp, n, s = _text(text)
+        x = np.ascontiguousarray(x)
+        dt = x.dtype
+        y = np.ascontiguousarray(y, dtype=dt)
+        lx = np.ascontiguousarray(lcp_x, dtype=dt)
+        ly = np.ascontiguousarray(lcp_y, dtype=dt)
+        z = np.empty(len(x) + len(y), dtype=dt)
+        lz = np.empty_like(z)
+        lim = (lp or PlainText(n))._c()
+        self._check(getattr(lib, "capssa_merge_%s_%s" % (s, _IDX[dt]))(
+            self._h, tp, n, C.byref(lim), x.ctypes.data, lx.ctypes.data, len(x), y.ctypes.data,
+            ly.ctypes.data, len(y), int(max_ctx), z.ctypes.data, lz.ctypes.data))
+        return z, lz
+
+    def pack_params(self, text, policy=1, max_extra_bytes=0):
+        """seed_params / Packer::new (src/pack.rs:103-176, 217-234)."""
+        t = np.ascontiguousarray(text, dtype=np.uint8)
+        pk = _Packer()
+        avail = C.c_int32()
+        self._check(lib.capssa_pack_params_u8(self._h, t.ctypes.data, len(t), int(policy),
+                                              int(max_extra_bytes), C.byref(pk), C.byref(avail)))
+        if not avail.value:
+            return None
+        return {"bits": pk.bits, "k": pk.k, "alphabet": pk.alphabet,
+                "identity": pk.identity, "code": np.array(pk.code, dtype=np.uint8), "_c": pk}
+
+    def pack_keys(self, text, params, positions, lp=None):
+        """Packer::key_at_bounded per position (src/pack.rs:187-203)."""
+        t = np.ascontiguousarray(text, dtype=np.uint8)
+        pos = np.ascontiguousarray(positions, dtype=np.uint64)
+        keys = np.empty(len(pos), dtype=np.uint64)
+        lim = (lp or PlainText(len(t)))._c()
+        self._check(lib.capssa_pack_keys_u8(self._h, t.ctypes.data, len(t), C.byref(params["_c"]),
+                                            C.byref(lim), pos.ctypes.data, len(pos),
+                                            keys.ctypes.data))
+        return keys
+
+    def seed_subarray(self, text, params, positions, lp=None, index=np.uint32):
+        """seed_subarray (src/pack.rs:241-321) -> (sa, lcp)."""
+        t = np.ascontiguousarray(text, dtype=np.uint8)
+        sa = np.ascontiguousarray(positions, dtype=index).copy()
+        lcp = np.zeros_like(sa)
+        lim = (lp or PlainText(len(t)))._c()
+        fn = getattr(lib, "capssa_seed_subarray_u8_%s" % _IDX[np.dtype(index)])
+        self._check(fn(self._h, t.ctypes.data, len(t), C.byref(params["_c"]), C.byref(lim),
+                       sa.ctypes.data, lcp.ctypes.data, len(sa)))
+        return sa, lcp
+
+
+# ------------------------------------------------------------------ free functions
+
+_default = threading.local()
+
+
+def default_context() -> Context:
+    if getattr(_default, "ctx", None) is None:
+        _default.ctx = Context(0)
+    return _default.ctx
+
+
+def build_in_memory(text, index=np.uint32):
+    return default_context().build_in_memory(text, index=index)
+
+
+def build_in_memory_with_opts(text, opts, index=np.uint32):
+    return default_context().build_in_memory(text, None, opts, index)
+
+
+def build_in_memory_with(text, lp, opts=None, index=np.uint32):
+    return default_context().build_in_memory(text, lp, opts, index)
+
+
+def build_in_memory_for_positions(text, positions):
+    return default_context().build_in_memory_for_positions(text, positions)
+
+
+def build_in_memory_for_positions_with_opts(text, positions, opts):
+    return default_context().build_in_memory_for_positions(text, positions, None, opts)
+
+
+def build_in_memory_for_positions_with(text, positions, lp, opts=None):
+    return default_context().build_in_memory_for_positions(text, positions, lp, opts)
+
+
+def build_in_memory_sample_sort(text, opts=None, emit=None):
+    return default_context().build_in_memory_sample_sort(text, opts, emit)
+
+
+def try_build_in_memory_sample_sort(text, opts, emit):
+    return default_context().try_build_in_memory_sample_sort(text, opts, emit)
+
+
+def build_in_memory_sample_sort_with(text, lp, opts=None, emit=None):
+    return default_context().build_in_memory_sample_sort(text, opts, emit, lp)
+
+
+def build_in_memory_sample_sort_for_positions(text, positions, opts=None, emit=None):
+    return default_context().build_in_memory_sample_sort(text, opts, emit, None, positions)
+
+
+def build_in_memory_sample_sort_for_positions_with(text, positions, lp, opts=None, emit=None):
+    return default_context().build_in_memory_sample_sort(text, opts, emit, lp, positions)
+
+
+def lcp(text, p, q, max_ctx=UNBOUNDED):
+    return int(default_context().lcp(text, p, q, max_ctx)[0])
+
+
+def suffix_cmp(text, p, q, max_ctx=UNBOUNDED):
+    return int(default_context().suffix_cmp(text, p, q, None, max_ctx)[0])

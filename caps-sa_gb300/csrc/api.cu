@@ -1,0 +1,887 @@
+// api.cu — the C ABI (include/capssa.h): contexts, workspace, staging of
+// host/device buffers, and the exported entry points.
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "common.cuh"
+#include "engine.cuh"
+#include "lcp.cuh"
+#include "radix.cuh"
+
+namespace capssa {
+
+capssa_status widen_u32_u64(Ctx &c, const uint32_t *in, uint64_t *out, uint64_t n);
+capssa_status presence_u8(Ctx &c, const uint8_t *text, uint64_t n, uint32_t *present);
+
+void *ws_get(Ctx &c, int slot, size_t bytes) {
+    if (bytes == 0) bytes = 64;
+    if (c.sizes[slot] >= bytes) return c.bufs[slot];
+    if (c.bufs[slot]) {
+        cudaStreamSynchronize(c.stream);
+        cudaFree(c.bufs[slot]);
+        c.bufs[slot] = nullptr;
+        c.sizes[slot] = 0;
+    }
+    // grow with headroom so repeated calls of similar size do not realloc
+    size_t want = bytes + bytes / 8 + 256;
+    void *p = nullptr;
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+        cudaGetLastError();
+        want = bytes;
+        if (cudaMalloc(&p, want) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+    }
+    c.bufs[slot] = p;
+    c.sizes[slot] = want;
+    return p;
+}
+
+capssa_status set_err(Ctx &c, capssa_status s, const std::string &msg) {
+    if (c.err.empty()) c.err = msg;
+    return s;
+}
+
+capssa_status cuda_err(Ctx &c, cudaError_t e, const char *where) {
+    std::string m = std::string("CUDA error in ") + where + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return set_err(c, CAPSSA_ENOMEM, m);
+    return set_err(c, CAPSSA_ECUDA, m);
+}
+
+capssa_status check_dev_flags(Ctx &c) {
+    int h[2] = {0, 0};
+    CAPSSA_CUDA(c, cudaMemcpyAsync(h, c.d_flags, 4, cudaMemcpyDeviceToHost, c.stream));
+    CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+    if (h[0] == DEV_LOOKBACK_TIMEOUT)
+        return set_err(c, CAPSSA_ETIMEOUT, "a device-side wait exceeded its limit");
+    if (h[0] != DEV_OK) return set_err(c, CAPSSA_ECUDA, "device error flag set");
+    return CAPSSA_OK;
+}
+
+KeyGeom key_geom(int b) {
+    KeyGeom g{};
+    g.b = b < 1 ? 1 : b;
+    int best = 1;
+    for (int k = 1; k * g.b <= 63; k++) {
+        int lb = 0;
+        while ((1 << lb) <= k) lb++;  // bits of 0..k
+        if (k * g.b + lb <= 64) best = k;
+    }
+    g.k = best;
+    int lb = 0;
+    while ((1 << lb) <= best) lb++;
+    g.lbits = lb;
+    g.total = g.k * g.b + g.lbits;
+    return g;
+}
+
+namespace {
+
+bool is_device_ptr(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// Copy `bytes` from a host or device buffer into workspace slot `slot`
+// (plus `pad` zero bytes); returns the device pointer.
+capssa_status stage_in(Ctx &c, int slot, const void *src, size_t bytes, size_t pad, void **out) {
+    void *d = ws_get(c, slot, bytes + pad);
+    if (!d) return set_err(c, CAPSSA_ENOMEM, "staging buffer");
+    if (bytes) {
+        bool dev = is_device_ptr(src);
+        auto t0 = std::chrono::steady_clock::now();
+        CAPSSA_CUDA(c, cudaMemcpyAsync(d, src, bytes,
+                                       dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                       c.stream));
+        if (!dev) {
+            CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+            c.stats.h2d_ms += ms_since(t0);
+            c.stats.h2d_bytes += bytes;
+        }
+    }
+    if (pad) CAPSSA_CUDA(c, cudaMemsetAsync((char *)d + bytes, 0, pad, c.stream));
+    *out = d;
+    return CAPSSA_OK;
+}
+
+// Device-resident limits: ends validated like SegmentedText::from_ends
+// (src/limits.rs:261-282) and the coarse directory of
+// BoundaryDirectory::build (src/limits.rs:210-235).
+capssa_status stage_limits(Ctx &c, const capssa_limits *lp, uint64_t n, DevLimits *out) {
+    DevLimits L{};
+    L.n = n;
+    if (lp && (lp->boundary != CAPSSA_SHORTER_FIRST && lp->boundary != CAPSSA_LONGER_FIRST))
+        return set_err(c, CAPSSA_EINVAL, "unknown boundary order");
+    if (lp && lp->kind != CAPSSA_LIMITS_PLAIN && lp->kind != CAPSSA_LIMITS_SEGMENTED)
+        return set_err(c, CAPSSA_EINVAL, "unknown limits kind");
+    L.longer_first = lp ? (lp->boundary == CAPSSA_LONGER_FIRST) : 0;
+    if (!lp || lp->kind == CAPSSA_LIMITS_PLAIN) {
+        *out = L;
+        return CAPSSA_OK;
+    }
+    L.segmented = 1;
+    const uint64_t ne = lp->n_ends;
+    std::vector<uint64_t> h(ne);
+    if (ne) {
+        if (!lp->ends) return set_err(c, CAPSSA_EINVAL, "segmented limits without ends");
+        if (is_device_ptr(lp->ends)) {
+            CAPSSA_CUDA(c, cudaMemcpyAsync(h.data(), lp->ends, ne * 8, cudaMemcpyDeviceToHost,
+                                           c.stream));
+            CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+        } else {
+            std::memcpy(h.data(), lp->ends, ne * 8);
+        }
+    }
+    for (uint64_t i = 1; i < ne; i++)
+        if (!(h[i - 1] < h[i]))
+            return set_err(c, CAPSSA_EINVAL, "SegmentedText::from_ends: ends must be strictly increasing");
+    if (ne == 0 ? n != 0 : h[ne - 1] != n)
+        return set_err(c, CAPSSA_EINVAL, "SegmentedText::from_ends: last end != text length");
+    std::vector<uint32_t> dir;
+    uint32_t shift = 0;
+    if (ne >= 256 && ne <= 0xFFFFFFFFull && n > 0) {
+        uint64_t target = std::min<uint64_t>(std::max<uint64_t>(ne * 2, 1), 2000000);
+        uint64_t min_block = (n + target - 1) / target;
+        uint64_t bs = 1;
+        while (bs < min_block) bs <<= 1;
+        while ((1ull << shift) < bs) shift++;
+        uint64_t nb = (n + bs - 1) / bs;
+        dir.resize(nb + 1);
+        uint64_t e = 0;
+        for (uint64_t b = 0; b <= nb; b++) {
+            uint64_t bstart = std::min(b * bs, n);
+            while (e < ne && h[e] <= bstart) e++;
+            dir[b] = (uint32_t)e;
+        }
+    }
+    void *d_ends = nullptr;
+    capssa_status s = stage_in(c, WS_ENDS, h.data(), ne * 8, 64, &d_ends);
+    if (s != CAPSSA_OK) return s;
+    L.ends = (const uint64_t *)d_ends;
+    L.n_ends = ne;
+    if (!dir.empty()) {
+        void *d_dir = nullptr;
+        s = stage_in(c, WS_DIR, dir.data(), dir.size() * 4, 64, &d_dir);
+        if (s != CAPSSA_OK) return s;
+        L.dir = (const uint32_t *)d_dir;
+        L.n_dir = dir.size();
+        L.block_shift = shift;
+    }
+    CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));  // host vectors go out of scope
+    *out = L;
+    return CAPSSA_OK;
+}
+
+struct CallScope {
+    Ctx &c;
+    explicit CallScope(Ctx &cc) : c(cc) {
+        c.err.clear();
+        c.stats = capssa_stats{};
+        c.launches = 0;
+        cudaSetDevice(c.device);
+        cudaMemsetAsync(c.d_flags, 0, 16, c.stream);
+        cudaEventRecord(c.ev0, c.stream);
+    }
+    capssa_status finish(capssa_status s) {
+        if (s == CAPSSA_OK) s = check_dev_flags(c);
+        cudaEventRecord(c.ev1, c.stream);
+        cudaEventSynchronize(c.ev1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+        c.stats.device_ms = ms;
+        c.stats.kernel_launches = c.launches;
+        cudaError_t e = cudaGetLastError();
+        if (s == CAPSSA_OK && e != cudaSuccess) s = cuda_err(c, e, "call");
+        return s;
+    }
+};
+
+// Deliver a device result to a host or device destination.
+capssa_status stage_out(Ctx &c, void *dst, const void *dsrc, size_t bytes) {
+    if (!bytes || dst == dsrc) return CAPSSA_OK;
+    bool dev = is_device_ptr(dst);
+    auto t0 = std::chrono::steady_clock::now();
+    CAPSSA_CUDA(c, cudaMemcpyAsync(dst, dsrc, bytes,
+                                   dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                   c.stream));
+    if (!dev) {
+        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+        c.stats.d2h_ms += ms_since(t0);
+        c.stats.d2h_bytes += bytes;
+    }
+    return CAPSSA_OK;
+}
+
+template <typename ST>
+capssa_status stage_text(Ctx &c, const ST *text, uint64_t n, void **d_text) {
+    return stage_in(c, WS_TEXT, text, n * sizeof(ST), 64 + sizeof(ST) * 8, d_text);
+}
+
+// Every builder funnels through here.
+template <typename ST>
+capssa_status build_common(Ctx &c, const ST *text, uint64_t n, const void *positions,
+                           int pos_bytes, uint64_t m, const capssa_limits *lp,
+                           const capssa_opts *opts, void *out_sa, int out_bytes, void *out_lcp) {
+    if (!text && n) return set_err(c, CAPSSA_EINVAL, "null text");
+    if (!out_sa && (positions ? m : n)) return set_err(c, CAPSSA_EINVAL, "null output");
+    if (out_bytes == 4 && n > 0xFFFFFFFFull)
+        return set_err(c, CAPSSA_EINVAL, "u32 index cannot address this text");
+    uint64_t max_ctx = opts ? opts->max_context : CAPSSA_UNBOUNDED;
+    DevLimits L{};
+    capssa_status s = stage_limits(c, lp, n, &L);
+    if (s != CAPSSA_OK) return s;
+    void *d_text = nullptr;
+    s = stage_text(c, text, n, &d_text);
+    if (s != CAPSSA_OK) return s;
+    const uint64_t count = positions ? m : n;
+    void *d_pos = nullptr;
+    if (positions && m) {
+        s = stage_in(c, WS_POS_IN, positions, m * (size_t)pos_bytes, 64, &d_pos);
+        if (s != CAPSSA_OK) return s;
+    }
+    bool out_dev = is_device_ptr(out_sa);
+    void *d_out = out_sa;
+    if (!out_dev && count) {
+        d_out = ws_get(c, WS_OUT, count * (size_t)out_bytes + 64);
+        if (!d_out) return set_err(c, CAPSSA_ENOMEM, "output buffer");
+    }
+    void *d_lcp = nullptr;
+    bool lcp_dev = out_lcp && is_device_ptr(out_lcp);
+    if (out_lcp) {
+        d_lcp = lcp_dev ? out_lcp : ws_get(c, WS_OUT2, count * (size_t)out_bytes + 64);
+        if (!d_lcp) return set_err(c, CAPSSA_ENOMEM, "lcp buffer");
+    }
+    EngineArgs a{};
+    a.text = d_text;
+    a.sym_bytes = (int)sizeof(ST);
+    a.n = n;
+    a.lim = L;
+    a.max_ctx = max_ctx;
+    a.positions = positions ? d_pos : nullptr;
+    a.pos_bytes = pos_bytes;
+    a.m = m;
+    a.out_sa = d_out;
+    a.out_bytes = out_bytes;
+    a.out_lcp = d_lcp;
+    if (positions && m == 0) return CAPSSA_OK;
+    s = engine_build(c, a);
+    if (s != CAPSSA_OK) return s;
+    s = check_dev_flags(c);
+    if (s != CAPSSA_OK) return s;
+    if (!out_dev) {
+        s = stage_out(c, out_sa, d_out, count * (size_t)out_bytes);
+        if (s != CAPSSA_OK) return s;
+    }
+    if (out_lcp && !lcp_dev) {
+        s = stage_out(c, out_lcp, d_lcp, count * (size_t)out_bytes);
+        if (s != CAPSSA_OK) return s;
+    }
+    return CAPSSA_OK;
+}
+
+// effective_subproblem_count (src/ext_mem.rs:1159-1178)
+uint64_t effective_p(uint64_t n, uint64_t requested, int threads) {
+    if (n == 0) return 0;
+    uint64_t raw;
+    if (requested == 0) {
+        uint64_t nt = threads > 0 ? (uint64_t)threads
+                                  : std::max<uint64_t>(1, std::thread::hardware_concurrency());
+        uint64_t from_size = (n + 65535) / 65536;
+        raw = std::min<uint64_t>(std::max<uint64_t>(from_size, nt), 8192);
+    } else {
+        raw = requested;
+    }
+    return std::min<uint64_t>(std::max<uint64_t>(raw, 1), n);
+}
+
+// Sample-sort builders: the suffix order on the device, delivered to the
+// caller's emit callback in batches, each batch copied while the previous
+// one is being consumed.
+template <typename ST>
+capssa_status sample_sort_common(Ctx &c, const ST *text, uint64_t n, const uint64_t *positions,
+                                 uint64_t m, const capssa_limits *lp, const capssa_opts *opts,
+                                 capssa_emit_fn emit, void *user) {
+    if (!emit) return set_err(c, CAPSSA_EINVAL, "null emit callback");
+    const uint64_t count = positions ? m : n;
+    if (count == 0) return CAPSSA_OK;
+    uint64_t *d_sa = (uint64_t *)ws_get(c, WS_OUT, count * 8 + 64);
+    if (!d_sa) return set_err(c, CAPSSA_ENOMEM, "output buffer");
+    c.stats.partitions = (uint32_t)effective_p(count, opts ? opts->subproblem_count : 0,
+                                               opts ? opts->host_threads : 0);
+    capssa_status s = build_common<ST>(c, text, n, positions, 8, m, lp, opts, d_sa, 8, nullptr);
+    if (s != CAPSSA_OK) return s;
+    const uint64_t batch = 1u << 22;  // 4 Mi positions (32 MiB) per emit
+    uint64_t *h = nullptr;
+    CAPSSA_CUDA(c, cudaMallocHost(&h, 2 * batch * 8));
+    cudaEvent_t done[2];
+    cudaEventCreateWithFlags(&done[0], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&done[1], cudaEventDisableTiming);
+    auto t0 = std::chrono::steady_clock::now();
+    uint64_t nb = (count + batch - 1) / batch;
+    auto issue = [&](uint64_t b) {
+        uint64_t off = b * batch, len = std::min(batch, count - off);
+        cudaMemcpyAsync(h + (b & 1) * batch, d_sa + off, len * 8, cudaMemcpyDeviceToHost, c.stream);
+        cudaEventRecord(done[b & 1], c.stream);
+    };
+    issue(0);
+    for (uint64_t b = 0; b < nb && s == CAPSSA_OK; b++) {
+        if (b + 1 < nb) issue(b + 1);
+        cudaEventSynchronize(done[b & 1]);
+        uint64_t off = b * batch, len = std::min(batch, count - off);
+        c.stats.d2h_bytes += len * 8;
+        if (emit(user, h + (b & 1) * batch, len) != 0)
+            s = set_err(c, CAPSSA_EEMIT, "emit callback aborted the build");
+    }
+    cudaStreamSynchronize(c.stream);
+    c.stats.d2h_ms += ms_since(t0);
+    cudaEventDestroy(done[0]);
+    cudaEventDestroy(done[1]);
+    cudaFreeHost(h);
+    return s;
+}
+
+__global__ void text_id_kernel(const uint32_t *__restrict__ sa, uint32_t n,
+                               const uint64_t *__restrict__ offs, uint64_t n_texts,
+                               uint64_t *__restrict__ keys, uint32_t *__restrict__ local) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint64_t p = sa[i];
+        uint64_t lo = 0, hi = n_texts;  // last t with offs[t] <= p
+        while (hi - lo > 1) {
+            uint64_t mid = (lo + hi) >> 1;
+            if (offs[mid] <= p)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        keys[i] = lo;
+        local[i] = (uint32_t)(p - offs[lo]);
+    }
+}
+
+// Many texts: one segmented sort of the concatenation, then a stable split
+// of the global order by text (within one text the segmented comparator is
+// exactly PlainText's).
+template <typename ST>
+capssa_status batched_common(Ctx &c, const ST *texts, const uint64_t *offsets, uint64_t n_texts,
+                             const capssa_opts *opts, void *out_sa, int out_bytes) {
+    if (n_texts == 0) return CAPSSA_OK;
+    if (!offsets) return set_err(c, CAPSSA_EINVAL, "null offsets");
+    std::vector<uint64_t> off(n_texts + 1);
+    if (is_device_ptr(offsets)) {
+        CAPSSA_CUDA(c, cudaMemcpy(off.data(), offsets, (n_texts + 1) * 8, cudaMemcpyDeviceToHost));
+    } else {
+        std::memcpy(off.data(), offsets, (n_texts + 1) * 8);
+    }
+    if (off[0] != 0) return set_err(c, CAPSSA_EINVAL, "offsets[0] must be 0");
+    for (uint64_t t = 0; t < n_texts; t++)
+        if (off[t + 1] < off[t]) return set_err(c, CAPSSA_EINVAL, "offsets must not decrease");
+    const uint64_t n = off[n_texts];
+    if (n == 0) return CAPSSA_OK;
+    if (n > 0xFFFFFFFEull) return set_err(c, CAPSSA_EUNSUPPORTED, "texts of 2^32-1 or more symbols");
+    std::vector<uint64_t> ends;
+    ends.reserve(n_texts);
+    for (uint64_t t = 1; t <= n_texts; t++)
+        if (off[t] != off[t - 1]) ends.push_back(off[t]);
+    capssa_limits lp{CAPSSA_LIMITS_SEGMENTED, CAPSSA_SHORTER_FIRST, ends.data(), ends.size()};
+    uint32_t *d_sa = (uint32_t *)ws_get(c, WS_OUT2, n * 4 + 64);
+    if (!d_sa) return set_err(c, CAPSSA_ENOMEM, "batched output");
+    capssa_opts o;
+    capssa_opts_default(&o);
+    if (opts) o = *opts;
+    o.max_context = CAPSSA_UNBOUNDED;
+    capssa_status s = build_common<ST>(c, texts, n, nullptr, 4, 0, &lp, &o, d_sa, 4, nullptr);
+    if (s != CAPSSA_OK) return s;
+    void *d_off = nullptr;
+    s = stage_in(c, WS_MISC3, off.data(), off.size() * 8, 64, &d_off);
+    if (s != CAPSSA_OK) return s;
+    uint64_t *ka = (uint64_t *)ws_get(c, WS_KEYS_A, n * 8);
+    uint64_t *kb = (uint64_t *)ws_get(c, WS_KEYS_B, n * 8);
+    uint32_t *va = (uint32_t *)ws_get(c, WS_VALS_A, n * 4);
+    uint32_t *vb = (uint32_t *)ws_get(c, WS_VALS_B, n * 4);
+    if (!ka || !kb || !va || !vb) return set_err(c, CAPSSA_ENOMEM, "batched split");
+    text_id_kernel<<<std::min<unsigned>(grid_for(n, 256), c.sm_count * 16), 256, 0, c.stream>>>(
+        d_sa, (uint32_t)n, (const uint64_t *)d_off, n_texts, ka, va);
+    CAPSSA_LAUNCHED(c);
+    int tb = 1;
+    while ((1ull << tb) < n_texts) tb++;
+    bool in_b = false;
+    s = radix::sort_pairs(c, ka, va, kb, vb, (uint32_t)n, 0, tb, false, 0, &in_b);
+    if (s != CAPSSA_OK) return s;
+    const uint32_t *res = in_b ? vb : va;
+    bool out_dev = is_device_ptr(out_sa);
+    if (out_bytes == 4) {
+        return stage_out(c, out_sa, res, n * 4);
+    }
+    uint64_t *w = (uint64_t *)ws_get(c, WS_OUT, n * 8 + 64);
+    if (!w) return set_err(c, CAPSSA_ENOMEM, "batched widen");
+    uint64_t *dst = out_dev ? (uint64_t *)out_sa : w;
+    s = widen_u32_u64(c, res, dst, n);
+    if (s != CAPSSA_OK) return s;
+    if (!out_dev) return stage_out(c, out_sa, w, n * 8);
+    return CAPSSA_OK;
+}
+
+}  // namespace
+
+__global__ void widen_u32_u64_kernel(const uint32_t *in, uint64_t *out, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = in[i];
+}
+
+capssa_status widen_u32_u64(Ctx &c, const uint32_t *in, uint64_t *out, uint64_t n) {
+    widen_u32_u64_kernel<<<std::min<unsigned>(grid_for(n, 256), c.sm_count * 16), 256, 0,
+                           c.stream>>>(in, out, n);
+    CAPSSA_LAUNCHED(c);
+    return CAPSSA_OK;
+}
+
+__global__ void pack_keys_kernel(const uint8_t *__restrict__ text, uint64_t n,
+                                 const uint8_t *__restrict__ code, uint32_t bits, uint32_t k,
+                                 uint32_t alphabet, DevLimits L, const uint64_t *__restrict__ pos,
+                                 uint64_t m, uint64_t *__restrict__ keys) {
+    // Packer::key_at_bounded (src/pack.rs:187-203)
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t p = pos[i];
+        uint64_t lim = dev_lim_at(L, p);
+        uint64_t take = k;
+        if (lim < take) take = lim;
+        if (n - p < take) take = n - p;
+        uint64_t bias = L.longer_first ? 0 : 1, pad = L.longer_first ? alphabet : 0;
+        uint64_t key = 0;
+        for (uint64_t j = 0; j < take; j++) key = (key << bits) | ((uint64_t)code[text[p + j]] + bias);
+        for (uint64_t j = take; j < k; j++) key = (key << bits) | pad;
+        keys[i] = key;
+    }
+}
+
+}  // namespace capssa
+
+using namespace capssa;
+
+// ===================================================================== C ABI
+
+extern "C" {
+
+void capssa_opts_default(capssa_opts *o) {
+    std::memset(o, 0, sizeof(*o));
+    o->max_context = CAPSSA_UNBOUNDED;
+}
+
+int capssa_abi_version(void) { return CAPSSA_ABI_VERSION; }
+
+capssa_status capssa_ctx_create(capssa_ctx **out, int device) {
+    if (!out) return CAPSSA_EINVAL;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return CAPSSA_ECUDA;
+    }
+    if (device < 0 || device >= count) return CAPSSA_EINVAL;
+    Ctx *c = new (std::nothrow) Ctx();
+    if (!c) return CAPSSA_ENOMEM;
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&c->d_flags, 64) != cudaSuccess ||
+        cudaMallocHost(&c->h_scratch, 1 << 16) != cudaSuccess ||
+        cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+        [&] {
+            for (auto &e : c->pev)
+                if (cudaEventCreate(&e) != cudaSuccess) return true;
+            for (auto &e : c->kev)
+                if (cudaEventCreate(&e) != cudaSuccess) return true;
+            return false;
+        }()) {
+        cudaGetLastError();
+        delete c;
+        return CAPSSA_ECUDA;
+    }
+    c->own_stream = true;
+    cudaMemset(c->d_flags, 0, 64);
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    *out = reinterpret_cast<capssa_ctx *>(c);
+    return CAPSSA_OK;
+}
+
+void capssa_ctx_trim(capssa_ctx *ctx) {
+    if (!ctx) return;
+    Ctx *c = reinterpret_cast<Ctx *>(ctx);
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (int i = 0; i < WS_NSLOTS; i++) {
+        if (c->bufs[i]) cudaFree(c->bufs[i]);
+        c->bufs[i] = nullptr;
+        c->sizes[i] = 0;
+    }
+}
+
+void capssa_ctx_destroy(capssa_ctx *ctx) {
+    if (!ctx) return;
+    Ctx *c = reinterpret_cast<Ctx *>(ctx);
+    capssa_ctx_trim(ctx);
+    if (c->d_flags) cudaFree(c->d_flags);
+    if (c->h_scratch) cudaFreeHost(c->h_scratch);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    for (auto &e : c->pev)
+        if (e) cudaEventDestroy(e);
+    for (auto &e : c->kev)
+        if (e) cudaEventDestroy(e);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+capssa_status capssa_ctx_set_stream(capssa_ctx *ctx, void *stream) {
+    if (!ctx) return CAPSSA_EINVAL;
+    Ctx *c = reinterpret_cast<Ctx *>(ctx);
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    if (stream) {
+        c->stream = (cudaStream_t)stream;
+        c->own_stream = false;
+    } else {
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+            return CAPSSA_ECUDA;
+        c->own_stream = true;
+    }
+    return CAPSSA_OK;
+}
+
+const char *capssa_ctx_last_error(const capssa_ctx *ctx) {
+    if (!ctx) return "null context";
+    return reinterpret_cast<const Ctx *>(ctx)->err.c_str();
+}
+
+capssa_status capssa_ctx_stats(const capssa_ctx *ctx, capssa_stats *out) {
+    if (!ctx || !out) return CAPSSA_EINVAL;
+    *out = reinterpret_cast<const Ctx *>(ctx)->stats;
+    return CAPSSA_OK;
+}
+
+uint64_t capssa_ctx_workspace_bytes(const capssa_ctx *ctx) {
+    if (!ctx) return 0;
+    const Ctx *c = reinterpret_cast<const Ctx *>(ctx);
+    uint64_t t = 0;
+    for (int i = 0; i < WS_NSLOTS; i++) t += c->sizes[i];
+    return t;
+}
+
+#define CTX_OR_EINVAL(ctx)                                                     \
+    if (!ctx) return CAPSSA_EINVAL;                                            \
+    Ctx &c = *reinterpret_cast<Ctx *>(ctx);                                    \
+    CallScope scope(c);
+
+#define DEFINE_FOR_I(S, ST, I, IT, IB)                                                        \
+    capssa_status capssa_build_in_memory_##S##_##I(capssa_ctx *ctx, const ST *text,           \
+                                                   uint64_t n, const capssa_limits *lp,       \
+                                                   const capssa_opts *opts, IT *out_sa) {     \
+        CTX_OR_EINVAL(ctx);                                                                   \
+        return scope.finish(                                                                  \
+            build_common<ST>(c, text, n, nullptr, IB, 0, lp, opts, out_sa, IB, nullptr));    \
+    }                                                                                         \
+    capssa_status capssa_build_in_memory_for_positions_##S##_##I(                             \
+        capssa_ctx *ctx, const ST *text, uint64_t n, const IT *positions, uint64_t m,         \
+        const capssa_limits *lp, const capssa_opts *opts, IT *out_sa) {                       \
+        CTX_OR_EINVAL(ctx);                                                                   \
+        if (!positions && m) return scope.finish(set_err(c, CAPSSA_EINVAL, "null positions")); \
+        return scope.finish(build_common<ST>(c, text, n, positions ? (const void *)positions   \
+                                                                   : (const void *)out_sa,    \
+                                             IB, m, lp, opts, out_sa, IB, nullptr));          \
+    }                                                                                         \
+    capssa_status capssa_build_in_memory_lcp_##S##_##I(                                       \
+        capssa_ctx *ctx, const ST *text, uint64_t n, const IT *positions, uint64_t m,         \
+        const capssa_limits *lp, const capssa_opts *opts, IT *out_sa, IT *out_lcp) {          \
+        CTX_OR_EINVAL(ctx);                                                                   \
+        if (!out_lcp) return scope.finish(set_err(c, CAPSSA_EINVAL, "null lcp output"));     \
+        return scope.finish(build_common<ST>(c, text, n, positions, IB, positions ? m : 0, lp, \
+                                             opts, out_sa, IB, out_lcp));                     \
+    }                                                                                         \
+    capssa_status capssa_merge_##S##_##I(                                                     \
+        capssa_ctx *ctx, const ST *text, uint64_t n, const capssa_limits *lp, const IT *x,    \
+        const IT *lcp_x, uint64_t len_x, const IT *y, const IT *lcp_y, uint64_t len_y,        \
+        uint64_t max_context, IT *z, IT *lcp_z) {                                             \
+        CTX_OR_EINVAL(ctx);                                                                   \
+        return scope.finish(merge_common<ST>(c, text, n, lp, x, lcp_x, len_x, y, lcp_y, len_y, \
+                                             max_context, z, lcp_z, IB));                     \
+    }                                                                                         \
+    capssa_status capssa_build_batched_##S##_##I(capssa_ctx *ctx, const ST *texts,            \
+                                                 const uint64_t *offsets, uint64_t n_texts,   \
+                                                 const capssa_opts *opts, IT *out_sa) {       \
+        CTX_OR_EINVAL(ctx);                                                                   \
+        return scope.finish(batched_common<ST>(c, texts, offsets, n_texts, opts, out_sa, IB)); \
+    }
+
+#define DEFINE_FOR_S(S, ST)                                                                   \
+    DEFINE_FOR_I(S, ST, u32, uint32_t, 4)                                                     \
+    DEFINE_FOR_I(S, ST, u64, uint64_t, 8)                                                     \
+    capssa_status capssa_build_in_memory_sample_sort_##S(                                     \
+        capssa_ctx *ctx, const ST *text, uint64_t n, const capssa_limits *lp,                 \
+        const capssa_opts *opts, capssa_emit_fn emit, void *user) {                           \
+        CTX_OR_EINVAL(ctx);                                                                   \
+        return scope.finish(sample_sort_common<ST>(c, text, n, nullptr, 0, lp, opts, emit, user)); \
+    }                                                                                         \
+    capssa_status capssa_build_in_memory_sample_sort_for_positions_##S(                       \
+        capssa_ctx *ctx, const ST *text, uint64_t n, const uint64_t *positions, uint64_t m,   \
+        const capssa_limits *lp, const capssa_opts *opts, capssa_emit_fn emit, void *user) {  \
+        CTX_OR_EINVAL(ctx);                                                                   \
+        if (!positions && m) return scope.finish(set_err(c, CAPSSA_EINVAL, "null positions")); \
+        if (m == 0) return scope.finish(CAPSSA_OK);                                           \
+        return scope.finish(                                                                  \
+            sample_sort_common<ST>(c, text, n, positions, m, lp, opts, emit, user));          \
+    }                                                                                         \
+    capssa_status capssa_lcp_##S(capssa_ctx *ctx, const ST *text, uint64_t n,                 \
+                                 const uint64_t *p, const uint64_t *q, uint64_t count,        \
+                                 uint64_t max_context, uint64_t *out) {                       \
+        CTX_OR_EINVAL(ctx);                                                                   \
+        return scope.finish(pairs_common<ST>(c, text, n, nullptr, p, q, count, max_context,   \
+                                             out, nullptr));                                  \
+    }                                                                                         \
+    capssa_status capssa_suffix_cmp_##S(capssa_ctx *ctx, const ST *text, uint64_t n,          \
+                                        const capssa_limits *lp, const uint64_t *p,           \
+                                        const uint64_t *q, uint64_t count,                    \
+                                        uint64_t max_context, int8_t *out) {                  \
+        CTX_OR_EINVAL(ctx);                                                                   \
+        return scope.finish(                                                                  \
+            pairs_common<ST>(c, text, n, lp, p, q, count, max_context, nullptr, out));        \
+    }
+
+}  // extern "C"
+
+namespace capssa {
+namespace {
+
+// True when every position (idx_bytes wide, host or device) is <= n.
+bool positions_within(Ctx &c, const void *pos, uint64_t count, int idx_bytes, uint64_t n) {
+    if (!count) return true;
+    std::vector<uint8_t> h(count * idx_bytes);
+    const void *src = pos;
+    if (is_device_ptr(pos)) {
+        if (cudaMemcpyAsync(h.data(), pos, h.size(), cudaMemcpyDeviceToHost, c.stream) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(c.stream) != cudaSuccess)
+            return false;
+        src = h.data();
+    }
+    for (uint64_t i = 0; i < count; i++) {
+        uint64_t v = idx_bytes == 4 ? ((const uint32_t *)src)[i] : ((const uint64_t *)src)[i];
+        if (v > n) return false;
+    }
+    return true;
+}
+
+template <typename ST>
+capssa_status merge_common(Ctx &c, const ST *text, uint64_t n, const capssa_limits *lp,
+                           const void *x, const void *lcp_x, uint64_t len_x, const void *y,
+                           const void *lcp_y, uint64_t len_y, uint64_t max_ctx, void *z,
+                           void *lcp_z, int ib) {
+    const uint64_t total = len_x + len_y;
+    if (total == 0) return CAPSSA_OK;
+    if ((len_x && (!x || !lcp_x)) || (len_y && (!y || !lcp_y)) || !z || !lcp_z)
+        return set_err(c, CAPSSA_EINVAL, "null merge buffer");
+    if (!positions_within(c, x, len_x, ib, n) || !positions_within(c, y, len_y, ib, n))
+        return set_err(c, CAPSSA_EINVAL, "a run position lies beyond the end of the text");
+    DevLimits L{};
+    capssa_status s = stage_limits(c, lp, n, &L);
+    if (s != CAPSSA_OK) return s;
+    void *d_text = nullptr;
+    s = stage_text(c, text, n, &d_text);
+    if (s != CAPSSA_OK) return s;
+    void *dx = nullptr, *dlx = nullptr, *dy = nullptr, *dly = nullptr;
+    if ((s = stage_in(c, WS_KEYS_A, x, len_x * ib, 64, &dx)) != CAPSSA_OK) return s;
+    if ((s = stage_in(c, WS_KEYS_B, lcp_x, len_x * ib, 64, &dlx)) != CAPSSA_OK) return s;
+    if ((s = stage_in(c, WS_VALS_A, y, len_y * ib, 64, &dy)) != CAPSSA_OK) return s;
+    if ((s = stage_in(c, WS_VALS_B, lcp_y, len_y * ib, 64, &dly)) != CAPSSA_OK) return s;
+    void *dz = ws_get(c, WS_OUT, total * ib + 64), *dlz = ws_get(c, WS_OUT2, total * ib + 64);
+    if (!dz || !dlz) return set_err(c, CAPSSA_ENOMEM, "merge output");
+    s = merge_runs(c, d_text, (int)sizeof(ST), L, dx, dlx, len_x, dy, dly, len_y, max_ctx, dz,
+                   dlz, ib);
+    if (s != CAPSSA_OK) return s;
+    if ((s = stage_out(c, z, dz, total * ib)) != CAPSSA_OK) return s;
+    return stage_out(c, lcp_z, dlz, total * ib);
+}
+
+template <typename ST>
+capssa_status pairs_common(Ctx &c, const ST *text, uint64_t n, const capssa_limits *lp,
+                           const uint64_t *p, const uint64_t *q, uint64_t count, uint64_t max_ctx,
+                           uint64_t *out_lcp, int8_t *out_cmp) {
+    if (count == 0) return CAPSSA_OK;
+    if (!p || !q || (!out_lcp && !out_cmp)) return set_err(c, CAPSSA_EINVAL, "null pair buffer");
+    std::vector<uint64_t> hp(count), hq(count);
+    const uint64_t *pp = p, *qq = q;
+    if (is_device_ptr(p)) {
+        CAPSSA_CUDA(c, cudaMemcpy(hp.data(), p, count * 8, cudaMemcpyDeviceToHost));
+        pp = hp.data();
+    }
+    if (is_device_ptr(q)) {
+        CAPSSA_CUDA(c, cudaMemcpy(hq.data(), q, count * 8, cudaMemcpyDeviceToHost));
+        qq = hq.data();
+    }
+    for (uint64_t i = 0; i < count; i++)
+        if (pp[i] > n || qq[i] > n) return set_err(c, CAPSSA_EINVAL, "position beyond the text");
+    DevLimits L{};
+    capssa_status s = stage_limits(c, lp, n, &L);
+    if (s != CAPSSA_OK) return s;
+    void *d_text = nullptr;
+    if ((s = stage_text(c, text, n, &d_text)) != CAPSSA_OK) return s;
+    void *dp = nullptr, *dq = nullptr;
+    if ((s = stage_in(c, WS_KEYS_A, pp, count * 8, 64, &dp)) != CAPSSA_OK) return s;
+    if ((s = stage_in(c, WS_KEYS_B, qq, count * 8, 64, &dq)) != CAPSSA_OK) return s;
+    if (out_lcp) {
+        uint64_t *d = (uint64_t *)ws_get(c, WS_OUT, count * 8 + 64);
+        if (!d) return set_err(c, CAPSSA_ENOMEM, "lcp output");
+        s = lcp_pairs(c, d_text, (int)sizeof(ST), n, (const uint64_t *)dp, (const uint64_t *)dq,
+                      count, max_ctx, d);
+        if (s != CAPSSA_OK) return s;
+        return stage_out(c, out_lcp, d, count * 8);
+    }
+    int8_t *d = (int8_t *)ws_get(c, WS_OUT, count + 64);
+    if (!d) return set_err(c, CAPSSA_ENOMEM, "cmp output");
+    s = suffix_cmp_pairs(c, d_text, (int)sizeof(ST), L, (const uint64_t *)dp, (const uint64_t *)dq,
+                         count, max_ctx, d);
+    if (s != CAPSSA_OK) return s;
+    return stage_out(c, out_cmp, d, count);
+}
+
+}  // namespace
+}  // namespace capssa
+
+extern "C" {
+DEFINE_FOR_S(u8, uint8_t)
+DEFINE_FOR_S(u16, uint16_t)
+DEFINE_FOR_S(u32, uint32_t)
+
+// Packer::new + seed_params (src/pack.rs:103-176, 217-234): the byte
+// presence scan runs on the device, the 256-entry map on the host.
+capssa_status capssa_pack_params_u8(capssa_ctx *ctx, const uint8_t *text, uint64_t n,
+                                    int32_t policy, uint64_t max_extra_bytes, capssa_packer *out,
+                                    int32_t *available) {
+    CTX_OR_EINVAL(ctx);
+    if (!out || !available || (!text && n)) return scope.finish(set_err(c, CAPSSA_EINVAL, "null argument"));
+    *available = 0;
+    std::memset(out, 0, sizeof(*out));
+    if (policy == CAPSSA_SEED_DISABLED) return scope.finish(CAPSSA_OK);
+    bool present[256] = {};
+    if (n) {
+        void *d_text = nullptr;
+        capssa_status s = stage_text(c, text, n, &d_text);
+        if (s != CAPSSA_OK) return scope.finish(s);
+        uint32_t *d_present = (uint32_t *)ws_get(c, WS_CODES, 256 * 4 + 64);
+        if (!d_present) return scope.finish(set_err(c, CAPSSA_ENOMEM, "presence table"));
+        cudaMemsetAsync(d_present, 0, 256 * 4, c.stream);
+        s = presence_u8(c, (const uint8_t *)d_text, n, d_present);
+        if (s != CAPSSA_OK) return scope.finish(s);
+        uint32_t h[256];
+        cudaMemcpyAsync(h, d_present, 1024, cudaMemcpyDeviceToHost, c.stream);
+        cudaStreamSynchronize(c.stream);
+        for (int i = 0; i < 256; i++) present[i] = h[i] != 0;
+    }
+    uint32_t next = 0;
+    bool identity = true;
+    for (int b = 0; b < 256; b++) {
+        out->code[b] = (uint8_t)next;
+        if (present[b]) {
+            if ((int)next != b) identity = false;
+            next++;
+        }
+    }
+    uint32_t bits = next <= 1 ? 1 : next <= 3 ? 2 : next <= 15 ? 4 : 8;
+    if (!identity) {
+        if (policy != CAPSSA_SEED_REMAP || n > max_extra_bytes) return scope.finish(CAPSSA_OK);
+    } else {
+        for (int b = 0; b < 256; b++) out->code[b] = (uint8_t)b;
+    }
+    if (!((uint64_t)next < (1ull << bits))) return scope.finish(CAPSSA_OK);  // has_sentinel
+    out->bits = bits;
+    out->k = 64 / bits;
+    out->alphabet = next;
+    out->identity = identity ? 1 : 0;
+    *available = 1;
+    return scope.finish(CAPSSA_OK);
+}
+
+capssa_status capssa_pack_keys_u8(capssa_ctx *ctx, const uint8_t *text, uint64_t n,
+                                  const capssa_packer *pk, const capssa_limits *lp,
+                                  const uint64_t *positions, uint64_t m, uint64_t *keys) {
+    CTX_OR_EINVAL(ctx);
+    if (!pk || (!positions && m) || (!keys && m)) return scope.finish(set_err(c, CAPSSA_EINVAL, "null argument"));
+    if (m == 0) return scope.finish(CAPSSA_OK);
+    if (pk->bits == 0 || pk->k == 0) return scope.finish(set_err(c, CAPSSA_EINVAL, "invalid packer"));
+    if (!positions_within(c, positions, m, 8, n))
+        return scope.finish(set_err(c, CAPSSA_EINVAL, "a position lies beyond the end of the text"));
+    DevLimits L{};
+    capssa_status s = stage_limits(c, lp, n, &L);
+    if (s != CAPSSA_OK) return scope.finish(s);
+    void *d_text = nullptr, *d_pos = nullptr, *d_code = nullptr;
+    if ((s = stage_text(c, text, n, &d_text)) != CAPSSA_OK) return scope.finish(s);
+    if ((s = stage_in(c, WS_POS_IN, positions, m * 8, 64, &d_pos)) != CAPSSA_OK) return scope.finish(s);
+    if ((s = stage_in(c, WS_CODES, pk->code, 256, 64, &d_code)) != CAPSSA_OK) return scope.finish(s);
+    uint64_t *d_keys = (uint64_t *)ws_get(c, WS_OUT, m * 8 + 64);
+    if (!d_keys) return scope.finish(set_err(c, CAPSSA_ENOMEM, "key output"));
+    pack_keys_kernel<<<std::min<unsigned>(grid_for(m, 256), c.sm_count * 16), 256, 0, c.stream>>>(
+        (const uint8_t *)d_text, n, (const uint8_t *)d_code, pk->bits, pk->k, pk->alphabet, L,
+        (const uint64_t *)d_pos, m, d_keys);
+    c.launches++;
+    if (cudaGetLastError() != cudaSuccess) return scope.finish(set_err(c, CAPSSA_ECUDA, "pack launch"));
+    return scope.finish(stage_out(c, keys, d_keys, m * 8));
+}
+
+// seed_subarray (src/pack.rs:241-321): the positions in suffix order and
+// the exact adjacent LCP array under the provider's limits.
+capssa_status capssa_seed_subarray_u8_u32(capssa_ctx *ctx, const uint8_t *text, uint64_t n,
+                                          const capssa_packer *pk, const capssa_limits *lp,
+                                          uint32_t *sa, uint32_t *lcp, uint64_t m) {
+    CTX_OR_EINVAL(ctx);
+    if (!pk) return scope.finish(set_err(c, CAPSSA_EINVAL, "null packer"));
+    capssa_opts o;
+    capssa_opts_default(&o);
+    return scope.finish(build_common<uint8_t>(c, text, n, sa, 4, m, lp, &o, sa, 4, lcp));
+}
+
+capssa_status capssa_seed_subarray_u8_u64(capssa_ctx *ctx, const uint8_t *text, uint64_t n,
+                                          const capssa_packer *pk, const capssa_limits *lp,
+                                          uint64_t *sa, uint64_t *lcp, uint64_t m) {
+    CTX_OR_EINVAL(ctx);
+    if (!pk) return scope.finish(set_err(c, CAPSSA_EINVAL, "null packer"));
+    capssa_opts o;
+    capssa_opts_default(&o);
+    return scope.finish(build_common<uint8_t>(c, text, n, sa, 8, m, lp, &o, sa, 8, lcp));
+}
+
+}  // extern "C"
+
+namespace capssa {
+__global__ void presence_u8_kernel(const uint8_t *__restrict__ text, uint64_t n,
+                                   uint32_t *__restrict__ present) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t s = text[i];
+        if (__ldcg(present + s) == 0) present[s] = 1;
+    }
+}
+capssa_status presence_u8(Ctx &c, const uint8_t *text, uint64_t n, uint32_t *present) {
+    presence_u8_kernel<<<std::min<unsigned>(grid_for(n, 256), c.sm_count * 8), 256, 0, c.stream>>>(
+        text, n, present);
+    CAPSSA_LAUNCHED(c);
+    return CAPSSA_OK;
+}
+}  // namespace capssa

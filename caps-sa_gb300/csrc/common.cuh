@@ -1,0 +1,130 @@
+// common.cuh — shared types of the GB300 suffix-array library.
+//
+// The library keeps every per-suffix array in 32-bit positions internally
+// (texts up to 2^32-2 symbols), 64-bit packed prefix keys, and converts to
+// the caller's index width only at the boundary.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/capssa.h"
+
+namespace capssa {
+
+// Device-side error codes written to Ctx::d_flags[0] (first error wins).
+enum DevError : int {
+    DEV_OK = 0,
+    DEV_LOOKBACK_TIMEOUT = 1,  // a decoupled look-back spin hit its limit
+    DEV_OVERFLOW = 2,          // a work list outgrew its capacity
+};
+
+// Spin limit for look-back waits: ~2^22 polls with a 64 ns backoff is far
+// longer than any predecessor tile takes, and bounded.
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+constexpr uint32_t kNoPos = 0xFFFFFFFFu;
+
+// LimitProvider on the device: PlainText (lim = n - p) or SegmentedText
+// with the reference's coarse boundary directory (src/limits.rs:194-236,
+// 305-328).
+struct DevLimits {
+    uint64_t n;
+    const uint64_t *ends;  // device, n_ends entries
+    uint64_t n_ends;
+    const uint32_t *dir;   // device, n_dir entries or nullptr
+    uint64_t n_dir;
+    uint32_t block_shift;
+    int segmented;
+    int longer_first;
+};
+
+__device__ __forceinline__ uint64_t first_end_after(const uint64_t *ends, uint64_t lo,
+                                                    uint64_t hi, uint64_t p) {
+    while (lo < hi) {
+        uint64_t mid = lo + ((hi - lo) >> 1);
+        if (__ldg(ends + mid) <= p)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// SegmentedText::lim_at / PlainText::lim_at (src/limits.rs:144-148, 305-328).
+__device__ __forceinline__ uint64_t dev_lim_at(const DevLimits &L, uint64_t p) {
+    if (!L.segmented) return L.n - p;
+    if (L.dir && p < L.n) {
+        uint64_t block = p >> L.block_shift;
+        uint64_t lo = __ldg(L.dir + block);
+        uint64_t hi = __ldg(L.dir + block + 1);
+        if (hi < lo + 1) hi = lo + 1;
+        if (hi > L.n_ends) hi = L.n_ends;
+        uint64_t i = first_end_after(L.ends, lo, hi, p);
+        return __ldg(L.ends + i) - p;
+    }
+    uint64_t i = first_end_after(L.ends, 0, L.n_ends, p);
+    if (i < L.n_ends) return __ldg(L.ends + i) - p;
+    return L.n - p;
+}
+
+// Grow-only device buffers owned by a context, addressed by slot.
+enum Slot : int {
+    WS_TEXT = 0, WS_ENDS, WS_DIR, WS_POS_IN, WS_OUT, WS_OUT2,
+    WS_KEYS_A, WS_KEYS_B, WS_VALS_A, WS_VALS_B,
+    WS_RANK, WS_KEY2, WS_GROUPS_A, WS_GROUPS_B, WS_COUNTERS,
+    WS_RADIX_STATUS, WS_RADIX_HIST, WS_SCAN, WS_CODES, WS_MISC, WS_MISC2, WS_MISC3,
+    WS_PINNED_DUMMY, WS_NSLOTS
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    void *bufs[WS_NSLOTS] = {};
+    size_t sizes[WS_NSLOTS] = {};
+    int *d_flags = nullptr;         // device error flag(s)
+    uint64_t *h_scratch = nullptr;  // pinned host scratch (small readbacks)
+    std::string err;
+    capssa_stats stats{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t pev[8] = {};        // phase boundaries of one suffix sort
+    cudaEvent_t kev[2 * 16] = {};   // around each radix pass of the initial sort
+    int sm_count = 0;
+    uint64_t launches = 0;
+};
+
+// Returns a device buffer of at least `bytes` for `slot` (nullptr on OOM).
+void *ws_get(Ctx &c, int slot, size_t bytes);
+
+// Error helpers.
+capssa_status set_err(Ctx &c, capssa_status s, const std::string &msg);
+capssa_status cuda_err(Ctx &c, cudaError_t e, const char *where);
+
+#define CAPSSA_CUDA(c, expr)                                        \
+    do {                                                            \
+        cudaError_t _e = (expr);                                    \
+        if (_e != cudaSuccess) return ::capssa::cuda_err((c), _e, #expr); \
+    } while (0)
+
+#define CAPSSA_LAUNCHED(c)                                          \
+    do {                                                            \
+        (c).launches++;                                             \
+        cudaError_t _e = cudaGetLastError();                        \
+        if (_e != cudaSuccess) return ::capssa::cuda_err((c), _e, "kernel launch"); \
+    } while (0)
+
+// Device flag check: returns CAPSSA_ETIMEOUT / CAPSSA_ENOMEM after a sync.
+capssa_status check_dev_flags(Ctx &c);
+
+inline unsigned grid_for(uint64_t n, unsigned block, unsigned cap = 1u << 30) {
+    uint64_t g = (n + block - 1) / block;
+    if (g == 0) g = 1;
+    if (g > cap) g = cap;
+    return (unsigned)g;
+}
+
+}  // namespace capssa

@@ -1,0 +1,68 @@
+// engine.cuh — the suffix sort behind every builder.
+//
+// Replaces the reference's merge_sort + LCP-merge recursion
+// (src/sample_sort.rs:168-348) and the packed-prefix seed
+// (src/pack.rs:241-321) with a GPU pipeline that produces the same order:
+//
+//  1. alphabet scan -> order-preserving dense codes (Packer::new,
+//     src/pack.rs:103-167), b bits per symbol;
+//  2. one 64-bit composite key per text position: the first k symbols of
+//     the suffix, truncated at its limit (min(k, lim_at(p)), as
+//     key_at_bounded does, src/pack.rs:187-203), padded, followed by the
+//     number of symbols taken.  Key order never contradicts
+//     suffix_cmp_with (src/lcp.rs:184-201); equal keys mean "equal through
+//     k symbols" or, when fewer than k were taken, a finished comparison;
+//  3. stable LSD radix sort of (key, position);
+//  4. rank doubling on the groups that are still tied: a suffix p of an
+//     unresolved group of depth h is re-keyed by the rank of p + h (or by
+//     "ended" when lim_at(p) == h); each round doubles h.  Ranks are
+//     group-head SA indices, so equal rank == equal comparison so far.
+//
+// Boundary orders: ShorterFirst (the default boundary_order) leaves suffixes
+// that end together with equal content tied; their output order is
+// ascending position.  LongerFirst (STAR) orders them by position, which the
+// stable sorts produce directly.
+#pragma once
+
+#include "common.cuh"
+
+namespace capssa {
+
+struct EngineArgs {
+    const void *text;      // device, padded with >= 64 zero bytes
+    int sym_bytes;         // 1, 2, 4
+    uint64_t n;
+    DevLimits lim;
+    uint64_t max_ctx;      // CAPSSA_UNBOUNDED or finite
+    const void *positions; // device or nullptr (= every position)
+    int pos_bytes;         // 4 or 8
+    uint64_t m;
+    void *out_sa;          // device, m (or n) entries of out_bytes
+    int out_bytes;         // 4 or 8
+    void *out_lcp;         // device or nullptr
+};
+
+// Runs the whole sort; all buffers are device buffers.
+capssa_status engine_build_u8(Ctx &c, const EngineArgs &a);
+capssa_status engine_build_u16(Ctx &c, const EngineArgs &a);
+capssa_status engine_build_u32(Ctx &c, const EngineArgs &a);
+
+inline capssa_status engine_build(Ctx &c, const EngineArgs &a) {
+    switch (a.sym_bytes) {
+    case 1: return engine_build_u8(c, a);
+    case 2: return engine_build_u16(c, a);
+    default: return engine_build_u32(c, a);
+    }
+}
+
+// Key geometry for b bits per symbol: the largest k with k*b plus the bits
+// of a 0..k length field fitting in 64.
+struct KeyGeom {
+    int b;       // bits per symbol
+    int k;       // symbols per key
+    int lbits;   // bits of the length field
+    int total;   // k*b + lbits
+};
+KeyGeom key_geom(int b);
+
+}  // namespace capssa

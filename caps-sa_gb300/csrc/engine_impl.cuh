@@ -1,0 +1,740 @@
+// engine_impl.cuh — kernels and host orchestration of the suffix sort
+// (see engine.cuh for the algorithm and its correspondence to the
+// reference).  Instantiated once per symbol type by engine_u8.cu,
+// engine_u16.cu and engine_u32.cu.
+#pragma once
+
+#include <algorithm>
+#include <vector>
+
+#include "engine.cuh"
+#include "lcp.cuh"
+#include "radix.cuh"
+#include "scan.cuh"
+
+namespace capssa {
+namespace {  // every kernel and helper is private to its engine_*.cu unit
+namespace eng {
+
+constexpr uint32_t kSmallMax = 16;  // tied groups up to this size: one thread each
+constexpr int kKeyThreads = 256;
+constexpr int kKeyPer = 8;          // positions per thread in the key kernel
+constexpr int kKeyTile = kKeyThreads * kKeyPer;
+
+struct BigGroup {
+    uint32_t start, len, toff, pad;
+};
+
+// Device counters of the refinement rounds, double-buffered by round parity.
+struct Counters {
+    uint32_t n_small[2];
+    uint32_t pad0[2];
+    unsigned long long big_packed[2];  // (ordinal << 40) | element total
+    unsigned long long refined;        // suffixes re-keyed (statistics)
+    unsigned long long pad1;
+};
+constexpr unsigned long long kBigOrdUnit = 1ull << 40;
+constexpr unsigned long long kBigTotMask = kBigOrdUnit - 1;
+
+// ---------------------------------------------------------------- alphabet
+
+template <typename S>
+__global__ void presence_kernel(const S *__restrict__ text, uint64_t n,
+                                uint32_t *__restrict__ present) {
+    // u8/u16: presence flags per symbol value; idempotent stores, read first
+    // so repeated symbols cost no write traffic.
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t s = (uint32_t)text[i];
+        if (__ldcg(present + s) == 0) present[s] = 1;
+    }
+}
+
+__global__ void minmax_kernel(const uint32_t *__restrict__ text, uint64_t n,
+                              uint32_t *__restrict__ mm) {
+    uint32_t lo = 0xFFFFFFFFu, hi = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t s = text[i];
+        lo = min(lo, s);
+        hi = max(hi, s);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(mm, lo);
+        atomicMax(mm + 1, hi);
+    }
+}
+
+// ---------------------------------------------------------------- keys
+
+// Code of one symbol: a u8/u16 table (order-preserving dense ranks) or an
+// offset from the smallest symbol (u32 texts).
+template <typename S>
+struct Coder {
+    const uint16_t *table;  // device, 256 or 65536 entries (nullptr: offset)
+    uint32_t minv;
+    __device__ __forceinline__ uint32_t operator()(S s) const {
+        return table ? (uint32_t)__ldg(table + (uint32_t)s) : (uint32_t)s - minv;
+    }
+};
+
+// Composite key of every text position (engine.cuh step 2).
+template <typename S>
+__global__ void __launch_bounds__(kKeyThreads)
+    key_kernel(const S *__restrict__ text, uint64_t n, DevLimits L, Coder<S> coder, int b,
+               int k, int lbits, uint64_t max_ctx, int lf, uint64_t *__restrict__ keys) {
+    __shared__ uint32_t codes[kKeyTile + 64];
+    const uint64_t t0 = (uint64_t)blockIdx.x * kKeyTile;
+    for (int i = threadIdx.x; i < kKeyTile + k; i += kKeyThreads) {
+        uint64_t p = t0 + i;
+        codes[i] = p < n ? coder(text[p]) : 0u;
+    }
+    __syncthreads();
+    const uint64_t pad = lf ? ((1ull << b) - 1) : 0ull;
+#pragma unroll 1
+    for (int e = 0; e < kKeyPer; e++) {
+        int i = threadIdx.x + e * kKeyThreads;
+        uint64_t p = t0 + i;
+        if (p >= n) break;
+        uint64_t lim = dev_lim_at(L, p);
+        uint64_t eff = lim < max_ctx ? lim : max_ctx;
+        int take = eff < (uint64_t)k ? (int)eff : k;
+        uint64_t content = 0;
+        for (int j = 0; j < k; j++) content = (content << b) | (j < take ? (uint64_t)codes[i + j] : pad);
+        keys[p] = (content << lbits) | (uint64_t)(lf ? k - take : take);
+    }
+}
+
+// ---------------------------------------------------------------- groups
+
+// First index of the run of `key` that contains sorted index i.
+__device__ __forceinline__ uint32_t run_head(const uint64_t *__restrict__ keys, uint32_t lo,
+                                             uint32_t i, uint64_t key) {
+    uint32_t j = i;
+    uint32_t stop = (i - lo > 32) ? i - 32 : lo;
+    while (j > stop && keys[j - 1] == key) j--;
+    if (j > stop || j == lo) return j;
+    // long run: binary search for the first index in [lo, j) equal to key
+    uint32_t a = lo, z = j;
+    while (a < z) {
+        uint32_t mid = a + ((z - a) >> 1);
+        if (keys[mid] < key)
+            a = mid + 1;
+        else
+            z = mid;
+    }
+    return a;
+}
+
+struct GroupLists {
+    uint2 *small[2];
+    BigGroup *big[2];
+    Counters *ctr;
+};
+
+__device__ __forceinline__ void append_group(const GroupLists &G, int nxt, uint32_t start,
+                                             uint32_t len) {
+    if (len <= kSmallMax) {
+        uint32_t idx = atomicAdd(&G.ctr->n_small[nxt], 1u);
+        G.small[nxt][idx] = make_uint2(start, len);
+    } else {
+        unsigned long long old = atomicAdd(&G.ctr->big_packed[nxt], kBigOrdUnit | len);
+        uint32_t ord = (uint32_t)(old >> 40);
+        BigGroup g;
+        g.start = start;
+        g.len = len;
+        g.toff = (uint32_t)(old & kBigTotMask);
+        g.pad = 0;
+        G.big[nxt][ord] = g;
+    }
+}
+
+// Ranks after the key sort; tied groups that need more symbols become the
+// first round's work (engine.cuh step 3 -> 4).
+__global__ void init_groups_kernel(const uint64_t *__restrict__ keys,
+                                   const uint32_t *__restrict__ sa, uint32_t n, int k,
+                                   uint64_t lmask, int lf, uint32_t *__restrict__ rank,
+                                   GroupLists G) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint64_t key = keys[i];
+        bool head = (i == 0) || keys[i - 1] != key;
+        uint32_t g = head ? i : run_head(keys, 0, i, key);
+        bool last = (i == n - 1) || keys[i + 1] != key;
+        uint32_t lenf = (uint32_t)(key & lmask);
+        int take = lf ? k - (int)lenf : (int)lenf;
+        bool complete = take < k;
+        rank[sa[i]] = (complete && lf) ? i : g;
+        if (!complete && last && i > g) append_group(G, 0, g, i - g + 1);
+    }
+}
+
+// Sort key of suffix p for a round at depth h: the rank of p + h, or the
+// "ended" value when the suffix's limit is exactly reached.
+__device__ __forceinline__ uint64_t doubling_key(const DevLimits &L,
+                                                 const uint32_t *__restrict__ rank, uint32_t p,
+                                                 uint64_t h, int lf, uint64_t empty_lf) {
+    uint64_t lim = dev_lim_at(L, p);
+    if (lim > h) {
+        uint32_t r = __ldcg(rank + p + h);
+        return lf ? (uint64_t)r : (uint64_t)r + 1;
+    }
+    return lf ? empty_lf : 0ull;
+}
+
+__global__ void gather_small_kernel(const uint2 *__restrict__ groups, uint32_t count,
+                                    const uint32_t *__restrict__ sa,
+                                    const uint32_t *__restrict__ rank, DevLimits L, uint64_t h,
+                                    int lf, uint64_t empty_lf, uint64_t *__restrict__ key2) {
+    for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < count;
+         gi += gridDim.x * blockDim.x) {
+        uint2 g = groups[gi];
+        for (uint32_t t = 0; t < g.y; t++) {
+            uint32_t i = g.x + t;
+            key2[i] = doubling_key(L, rank, sa[i], h, lf, empty_lf);
+        }
+    }
+}
+
+__global__ void gather_big_kernel(const BigGroup *__restrict__ groups,
+                                  const uint32_t *__restrict__ sa,
+                                  const uint32_t *__restrict__ rank, DevLimits L, uint64_t h,
+                                  int lf, uint64_t empty_lf, int k2bits,
+                                  uint64_t *__restrict__ tkeys, uint32_t *__restrict__ tvals) {
+    const uint32_t ord = blockIdx.x;
+    BigGroup g = groups[ord];
+    for (uint32_t t = threadIdx.x; t < g.len; t += blockDim.x) {
+        uint32_t p = sa[g.start + t];
+        uint64_t k2 = doubling_key(L, rank, p, h, lf, empty_lf);
+        tkeys[g.toff + t] = ((uint64_t)ord << k2bits) | k2;
+        tvals[g.toff + t] = p;
+    }
+}
+
+// One thread sorts one small tied group by (key, position), writes the new
+// SA slice, the new ranks and the still-tied subgroups.
+__global__ void sort_small_kernel(const uint2 *__restrict__ groups, uint32_t count,
+                                  uint32_t *__restrict__ sa, const uint64_t *__restrict__ key2,
+                                  uint32_t *__restrict__ rank, int lf, uint64_t empty,
+                                  GroupLists G, int nxt) {
+    for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < count;
+         gi += gridDim.x * blockDim.x) {
+        uint2 g = groups[gi];
+        uint64_t kk[kSmallMax];
+        uint32_t pp[kSmallMax];
+        for (uint32_t t = 0; t < g.y; t++) {
+            uint64_t k2 = key2[g.x + t];
+            uint32_t p = sa[g.x + t];
+            int j = (int)t - 1;
+            while (j >= 0 && (kk[j] > k2 || (kk[j] == k2 && pp[j] > p))) {
+                kk[j + 1] = kk[j];
+                pp[j + 1] = pp[j];
+                j--;
+            }
+            kk[j + 1] = k2;
+            pp[j + 1] = p;
+        }
+        uint32_t t = 0;
+        while (t < g.y) {
+            uint32_t e = t + 1;
+            while (e < g.y && kk[e] == kk[t]) e++;
+            bool ended = kk[t] == empty;
+            for (uint32_t u = t; u < e; u++) {
+                sa[g.x + u] = pp[u];
+                rank[pp[u]] = (ended && lf) ? g.x + u : g.x + t;
+            }
+            if (!ended && e - t >= 2) append_group(G, nxt, g.x + t, e - t);
+            t = e;
+        }
+    }
+}
+
+// After the big groups' (ordinal, key) pairs are sorted: scatter back into
+// the SA, re-rank, and emit the still-tied subgroups.
+__global__ void split_big_kernel(const uint64_t *__restrict__ tkeys,
+                                 const uint32_t *__restrict__ tvals, uint32_t total,
+                                 const BigGroup *__restrict__ groups, uint32_t n_groups,
+                                 int k2bits,
+                                 uint32_t *__restrict__ sa, uint32_t *__restrict__ rank, int lf,
+                                 uint64_t empty, GroupLists G, int nxt) {
+    const uint64_t k2mask = (k2bits >= 64) ? ~0ull : ((1ull << k2bits) - 1);
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += gridDim.x * blockDim.x) {
+        uint64_t key = tkeys[t];
+        uint32_t ord = (uint32_t)(key >> k2bits);
+        if (ord >= n_groups) continue;  // unreachable unless a sort step failed (flagged)
+        BigGroup g = groups[ord];
+        uint32_t local = t - g.toff;
+        if (t < g.toff || local >= g.len) continue;
+        uint32_t p = tvals[t];
+        sa[g.start + local] = p;
+        bool head = (t == g.toff) || tkeys[t - 1] != key;
+        uint32_t hd = head ? t : run_head(tkeys, g.toff, t, key);
+        bool ended = (key & k2mask) == empty;
+        rank[p] = (ended && lf) ? g.start + local : g.start + (hd - g.toff);
+        bool last = (t == g.toff + g.len - 1) || tkeys[t + 1] != key;
+        if (!ended && last && t > hd) append_group(G, nxt, g.start + (hd - g.toff), t - hd + 1);
+    }
+}
+
+// ---------------------------------------------------------------- output
+
+template <typename IT>
+__global__ void widen_kernel(const uint32_t *__restrict__ in, IT *__restrict__ out, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = (IT)in[i];
+}
+
+// Subset output: key = (rank of the suffix, position).  Position n is the
+// empty suffix: first under ShorterFirst, last under LongerFirst.
+template <typename PT>
+__global__ void subset_key_kernel(const PT *__restrict__ pos, uint64_t m, uint64_t n,
+                                  const uint32_t *__restrict__ rank, int lf,
+                                  uint64_t *__restrict__ keys, uint32_t *__restrict__ vals,
+                                  int *__restrict__ bad) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t p = (uint64_t)pos[i];
+        uint64_t rk;
+        if (p > n) {
+            atomicExch(bad, 1);
+            p = n;
+        }
+        if (p == n)
+            rk = lf ? 0xFFFFFFFFull : 0ull;
+        else
+            rk = (uint64_t)__ldg(rank + p) + 1;
+        keys[i] = (rk << 32) | p;
+        vals[i] = (uint32_t)p;
+    }
+}
+
+}  // namespace eng
+
+
+namespace eng {
+
+// ---------------------------------------------------------------- bounded context
+
+// Bounded max_context: the sort above uses the unbounded comparator; the
+// two comparators differ only for suffixes that agree through max_context
+// symbols with both limits >= max_context, and those form contiguous runs
+// of the unbounded SA.  suffix_cmp_with orders such suffixes by
+// boundary_order on their full limits (src/lcp.rs:192-200), i.e. by limit
+// (ShorterFirst) or by descending limit then position (LongerFirst).
+__global__ void run_head_value_kernel(const uint8_t *__restrict__ flags, uint32_t n,
+                                      uint32_t *__restrict__ hv, uint32_t *__restrict__ in_run) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        bool f = flags[i];
+        hv[i] = f ? 0u : i;
+        in_run[i] = (f || (i + 1 < n && flags[i + 1])) ? 1u : 0u;
+    }
+}
+
+__global__ void run_compact_kernel(const uint8_t *__restrict__ flags, uint32_t n,
+                                   const uint32_t *__restrict__ sa,
+                                   const uint32_t *__restrict__ run_id,
+                                   const uint32_t *__restrict__ dst, DevLimits L, int lf,
+                                   uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        bool in = flags[i] || (i + 1 < n && flags[i + 1]);
+        if (!in) continue;
+        uint32_t p = sa[i];
+        uint64_t lim = dev_lim_at(L, p);
+        uint64_t lk = lf ? (uint64_t)L.n - lim : lim;
+        keys[dst[i]] = (lk << 32) | p;
+        vals[dst[i]] = run_id[i];
+    }
+}
+
+__global__ void run_swap_kernel(const uint64_t *__restrict__ k1, const uint32_t *__restrict__ v1,
+                                uint32_t total, uint64_t *__restrict__ k2,
+                                uint32_t *__restrict__ v2) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += gridDim.x * blockDim.x) {
+        k2[t] = v1[t];
+        v2[t] = (uint32_t)(k1[t] & 0xFFFFFFFFull);
+    }
+}
+
+__global__ void run_writeback_kernel(const uint64_t *__restrict__ runk,
+                                     const uint32_t *__restrict__ pos, uint32_t total,
+                                     uint32_t *__restrict__ sa, uint32_t n) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += gridDim.x * blockDim.x) {
+        uint64_t r = runk[t];
+        uint32_t hd = (t == 0 || runk[t - 1] != r) ? t : run_head(runk, 0, t, r);
+        uint64_t at = r + (t - hd);
+        if (at < n) sa[at] = pos[t];
+    }
+}
+
+__global__ void isa_kernel(const uint32_t *__restrict__ sa, uint32_t n, uint32_t *__restrict__ isa) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        isa[sa[i]] = i;
+}
+
+// Subset output key: the suffix's index in the full SA (whose tie classes
+// are in ascending position), with the empty suffix at n first under
+// ShorterFirst and last under LongerFirst.
+template <typename PT>
+__global__ void subset_isa_key_kernel(const PT *__restrict__ pos, uint64_t m, uint64_t n,
+                                      const uint32_t *__restrict__ isa, int lf,
+                                      uint64_t *__restrict__ keys, uint32_t *__restrict__ vals,
+                                      int *__restrict__ bad) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t p = (uint64_t)pos[i];
+        if (p > n) {
+            atomicExch(bad, 1);
+            p = n;
+        }
+        uint64_t rk;
+        if (p == n)
+            rk = lf ? n + 1 : 0ull;
+        else
+            rk = (uint64_t)__ldg(isa + p) + 1;
+        keys[i] = rk;
+        vals[i] = (uint32_t)p;
+    }
+}
+
+}  // namespace eng
+
+// ---------------------------------------------------------------- host
+
+inline int bits_for(uint64_t v) {  // bits to represent 0..v
+    int b = 0;
+    while (b < 64 && (v >> b) != 0) b++;
+    return b == 0 ? 1 : b;
+}
+
+// Steps 1-4 of engine.cuh over every text position under the unbounded
+// comparator; *sa_out receives the device SA (n entries).
+template <typename S>
+capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
+    using namespace eng;
+    const uint64_t n = a.n;
+    const int lf = a.lim.longer_first;
+    const S *text = (const S *)a.text;
+    cudaEventRecord(c.pev[0], c.stream);
+
+    // ---- 1. alphabet -> codes
+    const uint16_t *table = nullptr;
+    uint32_t minv = 0;
+    uint64_t sigma_span = 1;
+    if (sizeof(S) <= 2) {
+        const uint32_t nvals = sizeof(S) == 1 ? 256u : 65536u;
+        uint32_t *present = (uint32_t *)ws_get(c, WS_CODES, nvals * 4 + nvals * 2 + 64);
+        if (!present) return set_err(c, CAPSSA_ENOMEM, "alphabet table");
+        CAPSSA_CUDA(c, cudaMemsetAsync(present, 0, nvals * 4, c.stream));
+        presence_kernel<S><<<std::min<unsigned>(grid_for(n, 256), c.sm_count * 8), 256, 0,
+                             c.stream>>>(text, n, present);
+        CAPSSA_LAUNCHED(c);
+        std::vector<uint32_t> h_present(nvals);
+        CAPSSA_CUDA(c, cudaMemcpyAsync(h_present.data(), present, nvals * 4,
+                                       cudaMemcpyDeviceToHost, c.stream));
+        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+        std::vector<uint16_t> h_code(nvals);
+        uint32_t next = 0;
+        for (uint32_t v = 0; v < nvals; v++) {
+            h_code[v] = (uint16_t)next;
+            if (h_present[v]) next++;
+        }
+        sigma_span = next ? next : 1;
+        uint16_t *d_code = (uint16_t *)(present + nvals);
+        CAPSSA_CUDA(c, cudaMemcpyAsync(d_code, h_code.data(), nvals * 2, cudaMemcpyHostToDevice,
+                                       c.stream));
+        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));  // h_code goes out of scope
+        table = d_code;
+    } else {
+        uint32_t *mm = (uint32_t *)ws_get(c, WS_CODES, 64);
+        if (!mm) return set_err(c, CAPSSA_ENOMEM, "alphabet table");
+        uint32_t init[2] = {0xFFFFFFFFu, 0u};
+        CAPSSA_CUDA(c, cudaMemcpyAsync(mm, init, 8, cudaMemcpyHostToDevice, c.stream));
+        minmax_kernel<<<std::min<unsigned>(grid_for(n, 256), c.sm_count * 8), 256, 0, c.stream>>>(
+            (const uint32_t *)text, n, mm);
+        CAPSSA_LAUNCHED(c);
+        uint32_t h_mm[2];
+        CAPSSA_CUDA(c, cudaMemcpyAsync(h_mm, mm, 8, cudaMemcpyDeviceToHost, c.stream));
+        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+        minv = h_mm[0];
+        sigma_span = (uint64_t)h_mm[1] - h_mm[0] + 1;
+    }
+    const int b = bits_for(sigma_span > 1 ? sigma_span - 1 : 1);
+    const KeyGeom geo = key_geom(b);
+    c.stats.key_symbols = geo.k;
+    c.stats.key_bits_per_symbol = geo.b;
+
+    // ---- 2+3. composite keys of every position, stable radix sort
+    const uint32_t nn = (uint32_t)n;
+    uint64_t *keys_a = (uint64_t *)ws_get(c, WS_KEYS_A, (size_t)n * 8);
+    uint64_t *keys_b = (uint64_t *)ws_get(c, WS_KEYS_B, (size_t)n * 8);
+    uint32_t *vals_a = (uint32_t *)ws_get(c, WS_VALS_A, (size_t)n * 4);
+    uint32_t *vals_b = (uint32_t *)ws_get(c, WS_VALS_B, (size_t)n * 4);
+    uint32_t *rank = (uint32_t *)ws_get(c, WS_RANK, (size_t)n * 4 + 64);
+    uint64_t *key2 = (uint64_t *)ws_get(c, WS_KEY2, (size_t)n * 8);
+    if (!keys_a || !keys_b || !vals_a || !vals_b || !rank || !key2)
+        return set_err(c, CAPSSA_ENOMEM, "suffix-sort workspace");
+    Coder<S> coder{table, minv};
+    key_kernel<S><<<grid_for(n, kKeyTile), kKeyThreads, 0, c.stream>>>(
+        text, n, a.lim, coder, geo.b, geo.k, geo.lbits, CAPSSA_UNBOUNDED, lf, keys_a);
+    CAPSSA_LAUNCHED(c);
+    cudaEventRecord(c.pev[1], c.stream);
+    bool in_b = false;
+    int passes = 0;
+    capssa_status s = radix::sort_pairs(c, keys_a, vals_a, keys_b, vals_b, nn, 0, geo.total, true,
+                                        0, &in_b, &passes);
+    if (s != CAPSSA_OK) return s;
+    c.stats.sort_passes = (uint32_t)passes;
+    cudaEventRecord(c.pev[2], c.stream);
+    const uint64_t *skeys = in_b ? keys_b : keys_a;
+    uint32_t *sa = in_b ? vals_b : vals_a;
+    uint32_t *spare_vals = in_b ? vals_a : vals_b;
+
+    // ---- 4. tied groups + rank doubling
+    size_t small_cap = (size_t)n / 2 + 2, big_cap = (size_t)n / (kSmallMax + 1) + 2;
+    GroupLists G;
+    char *gl = (char *)ws_get(c, WS_GROUPS_A, small_cap * 8 * 2 + big_cap * 16 * 2 + 256);
+    if (!gl) return set_err(c, CAPSSA_ENOMEM, "group lists");
+    G.ctr = (Counters *)gl;
+    G.small[0] = (uint2 *)(gl + 256);
+    G.small[1] = G.small[0] + small_cap;
+    G.big[0] = (BigGroup *)(G.small[1] + small_cap);
+    G.big[1] = G.big[0] + big_cap;
+    CAPSSA_CUDA(c, cudaMemsetAsync(G.ctr, 0, sizeof(Counters), c.stream));
+    init_groups_kernel<<<std::min<unsigned>(grid_for(n, 256), c.sm_count * 16), 256, 0,
+                         c.stream>>>(skeys, sa, nn, geo.k, (1ull << geo.lbits) - 1, lf, rank, G);
+    CAPSSA_LAUNCHED(c);
+
+    const int k2bits = bits_for(n + 1);
+    const uint64_t empty_lf = (1ull << k2bits) - 1;  // above every rank
+    const uint64_t empty = lf ? empty_lf : 0ull;
+    uint64_t h = (uint64_t)geo.k;
+    int cur = 0;
+    Counters *hc = (Counters *)c.h_scratch;
+    for (;;) {
+        CAPSSA_CUDA(c, cudaMemcpyAsync(hc, G.ctr, sizeof(Counters), cudaMemcpyDeviceToHost,
+                                       c.stream));
+        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+        const uint32_t ns = hc->n_small[cur];
+        const uint32_t nb = (uint32_t)(hc->big_packed[cur] >> 40);
+        const uint32_t big_total = (uint32_t)(hc->big_packed[cur] & kBigTotMask);
+        if (ns == 0 && nb == 0) break;
+        if (c.stats.refine_rounds >= 70)
+            return set_err(c, CAPSSA_EINVAL, "rank doubling did not converge");
+        c.stats.refine_rounds++;
+        const int nxt = cur ^ 1;
+        CAPSSA_CUDA(c, cudaMemsetAsync(&G.ctr->n_small[nxt], 0, 4, c.stream));
+        CAPSSA_CUDA(c, cudaMemsetAsync(&G.ctr->big_packed[nxt], 0, 8, c.stream));
+        // gathers read ranks of the previous depth; all of them finish
+        // before any rank of this round is rewritten (stream order)
+        if (ns) {
+            gather_small_kernel<<<grid_for(ns, 128), 128, 0, c.stream>>>(
+                G.small[cur], ns, sa, rank, a.lim, h, lf, empty_lf, key2);
+            CAPSSA_LAUNCHED(c);
+        }
+        const int ord_bits = nb > 1 ? bits_for(nb - 1) : 1;
+        if (nb) {
+            gather_big_kernel<<<nb, 256, 0, c.stream>>>(G.big[cur], sa, rank, a.lim, h, lf,
+                                                        empty_lf, k2bits, keys_a, spare_vals);
+            CAPSSA_LAUNCHED(c);
+        }
+        if (ns) {
+            sort_small_kernel<<<grid_for(ns, 128), 128, 0, c.stream>>>(
+                G.small[cur], ns, sa, key2, rank, lf, empty, G, nxt);
+            CAPSSA_LAUNCHED(c);
+        }
+        if (nb) {
+            bool tb = false;
+            uint32_t *tv_b = (uint32_t *)key2;  // free once sort_small has run
+            s = radix::sort_pairs(c, keys_a, spare_vals, keys_b, tv_b, big_total, 0,
+                                  k2bits + ord_bits, false, 0, &tb);
+            if (s != CAPSSA_OK) return s;
+            const uint64_t *tk = tb ? keys_b : keys_a;
+            const uint32_t *tv = tb ? tv_b : spare_vals;
+            split_big_kernel<<<std::min<unsigned>(grid_for(big_total, 256), c.sm_count * 16), 256,
+                               0, c.stream>>>(tk, tv, big_total, G.big[cur], nb, k2bits, sa, rank, lf,
+                                              empty, G, nxt);
+            CAPSSA_LAUNCHED(c);
+        }
+        c.stats.refined_suffixes += big_total;
+        h *= 2;
+        cur = nxt;
+    }
+    cudaEventRecord(c.pev[3], c.stream);
+    CAPSSA_CUDA(c, cudaEventSynchronize(c.pev[3]));
+    float t01 = 0, t12 = 0, t23 = 0;
+    cudaEventElapsedTime(&t01, c.pev[0], c.pev[1]);
+    cudaEventElapsedTime(&t12, c.pev[1], c.pev[2]);
+    cudaEventElapsedTime(&t23, c.pev[2], c.pev[3]);
+    c.stats.keys_ms = t01;
+    c.stats.sort_ms = t12;
+    c.stats.refine_ms = t23;
+    double pass_ms = 0;
+    for (int i = 0; i < passes && i < 16; i++) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c.kev[2 * i], c.kev[2 * i + 1]);
+        pass_ms += ms;
+    }
+    c.stats.sort_pass_ms = pass_ms;
+    *sa_out = sa;
+    return CAPSSA_OK;
+}
+
+template <typename S>
+capssa_status bounded_pass(Ctx &c, const EngineArgs &a, uint32_t *sa) {
+    using namespace eng;
+    const uint64_t n = a.n;
+    const uint32_t nn = (uint32_t)n;
+    uint8_t *flags = (uint8_t *)ws_get(c, WS_OUT2, (size_t)n + 64);
+    uint32_t *hv = (uint32_t *)ws_get(c, WS_MISC, (size_t)n * 8 + 64);
+    uint32_t *inr = (uint32_t *)ws_get(c, WS_MISC2, (size_t)n * 8 + 64);
+    uint64_t *k1 = (uint64_t *)ws_get(c, WS_KEYS_A, (size_t)n * 8);
+    uint64_t *k2 = (uint64_t *)ws_get(c, WS_KEYS_B, (size_t)n * 8);
+    uint32_t *v1 = (uint32_t *)ws_get(c, WS_MISC3, (size_t)n * 8 + 64);
+    if (!flags || !hv || !inr || !k1 || !k2 || !v1) return set_err(c, CAPSSA_ENOMEM, "bounded pass");
+    uint32_t *v2 = v1 + n;
+    capssa_status s = ctx_run_flags(c, a.text, a.sym_bytes, a.lim, a.max_ctx, sa, n, flags);
+    if (s != CAPSSA_OK) return s;
+    unsigned g = std::min<unsigned>(grid_for(n, 256), c.sm_count * 16);
+    run_head_value_kernel<<<g, 256, 0, c.stream>>>(flags, nn, hv, inr);
+    CAPSSA_LAUNCHED(c);
+    uint32_t last_in = 0;
+    CAPSSA_CUDA(c, cudaMemcpyAsync(c.h_scratch, inr + (n - 1), 4, cudaMemcpyDeviceToHost, c.stream));
+    s = scan_u32(c, hv, hv, n, true, true);  // run id = max head index so far
+    if (s != CAPSSA_OK) return s;
+    CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+    last_in = *(uint32_t *)c.h_scratch;
+    s = scan_u32(c, inr, inr, n, false, false);  // compacted index
+    if (s != CAPSSA_OK) return s;
+    CAPSSA_CUDA(c, cudaMemcpyAsync(c.h_scratch, inr + (n - 1), 4, cudaMemcpyDeviceToHost, c.stream));
+    CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+    const uint32_t total = *(uint32_t *)c.h_scratch + last_in;
+    if (total == 0) return CAPSSA_OK;
+    run_compact_kernel<<<g, 256, 0, c.stream>>>(flags, nn, sa, hv, inr, a.lim, a.lim.longer_first,
+                                                k1, v1);
+    CAPSSA_LAUNCHED(c);
+    bool tb = false;
+    s = radix::sort_pairs(c, k1, v1, k2, v2, total, 0, 32 + bits_for(n), false, 0, &tb);
+    if (s != CAPSSA_OK) return s;
+    const uint64_t *sk = tb ? k2 : k1;
+    const uint32_t *sv = tb ? v2 : v1;
+    uint64_t *rk = tb ? k1 : k2;
+    uint32_t *rv = (uint32_t *)hv;  // run ids were consumed by the compaction
+    unsigned gt = std::min<unsigned>(grid_for(total, 256), c.sm_count * 16);
+    run_swap_kernel<<<gt, 256, 0, c.stream>>>(sk, sv, total, rk, rv);
+    CAPSSA_LAUNCHED(c);
+    uint64_t *rk2 = tb ? k2 : k1;
+    uint32_t *rv2 = (uint32_t *)inr;
+    s = radix::sort_pairs(c, rk, rv, rk2, rv2, total, 0, bits_for(n), false, 0, &tb);
+    if (s != CAPSSA_OK) return s;
+    run_writeback_kernel<<<gt, 256, 0, c.stream>>>(tb ? rk2 : rk, tb ? rv2 : rv, total, sa, nn);
+    CAPSSA_LAUNCHED(c);
+    return CAPSSA_OK;
+}
+
+// Records the device time from its construction to its destruction as
+// stats.finish_ms (the output ordering and copies of a build).
+struct FinishTimer {
+    Ctx &c;
+    explicit FinishTimer(Ctx &cc) : c(cc) { cudaEventRecord(c.pev[4], c.stream); }
+    ~FinishTimer() {
+        cudaEventRecord(c.pev[5], c.stream);
+        if (cudaEventSynchronize(c.pev[5]) == cudaSuccess) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, c.pev[4], c.pev[5]);
+            c.stats.finish_ms = ms;
+        }
+    }
+};
+
+template <typename S>
+capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
+    using namespace eng;
+    const uint64_t n = a.n;
+    const int lf = a.lim.longer_first;
+    const bool subset = a.positions != nullptr;
+    const uint64_t m = subset ? a.m : n;
+    c.stats.n_suffixes = m;
+    if (n > 0xFFFFFFFEull) return set_err(c, CAPSSA_EUNSUPPORTED, "texts of 2^32-1 or more symbols");
+    if (m > 0xFFFFFFFFull) return set_err(c, CAPSSA_EUNSUPPORTED, "more than 2^32-1 positions");
+    if (m == 0) return CAPSSA_OK;
+    const bool bounded = a.max_ctx != CAPSSA_UNBOUNDED && a.max_ctx < n;
+
+    uint32_t *sa = nullptr;
+    if (n > 0) {
+        capssa_status s = core_sort<S>(c, a, &sa);
+        if (s != CAPSSA_OK) return s;
+        if (bounded) {
+            s = bounded_pass<S>(c, a, sa);
+            if (s != CAPSSA_OK) return s;
+        }
+    }
+    FinishTimer ft(c);
+    if (!subset) {
+        if (a.out_bytes == 4) {
+            CAPSSA_CUDA(c, cudaMemcpyAsync(a.out_sa, sa, n * 4, cudaMemcpyDeviceToDevice, c.stream));
+        } else {
+            widen_kernel<uint64_t><<<std::min<unsigned>(grid_for(n, 256), c.sm_count * 16), 256, 0,
+                                     c.stream>>>(sa, (uint64_t *)a.out_sa, n);
+            CAPSSA_LAUNCHED(c);
+        }
+        if (a.out_lcp) {
+            capssa_status s = lcp_array_sa(c, a.text, a.sym_bytes, n, a.lim, a.max_ctx, sa, n,
+                                           a.out_lcp, a.out_bytes);
+            if (s != CAPSSA_OK) return s;
+        }
+        return CAPSSA_OK;
+    }
+    // subset: order the requested positions by their index in the full SA
+    uint32_t *isa = (uint32_t *)ws_get(c, WS_RANK, (size_t)n * 4 + 64);
+    uint64_t *sk_a = (uint64_t *)ws_get(c, WS_MISC, (size_t)m * 8 + 64);
+    uint64_t *sk_b = (uint64_t *)ws_get(c, WS_MISC2, (size_t)m * 8 + 64);
+    uint32_t *sv = (uint32_t *)ws_get(c, WS_MISC3, (size_t)m * 8 + 64);
+    if (!isa || !sk_a || !sk_b || !sv) return set_err(c, CAPSSA_ENOMEM, "subset workspace");
+    uint32_t *sv_b = sv + m;
+    if (n > 0) {
+        isa_kernel<<<std::min<unsigned>(grid_for(n, 256), c.sm_count * 16), 256, 0, c.stream>>>(
+            sa, (uint32_t)n, isa);
+        CAPSSA_LAUNCHED(c);
+    }
+    int *bad = c.d_flags + 1;
+    CAPSSA_CUDA(c, cudaMemsetAsync(bad, 0, 4, c.stream));
+    unsigned gm = std::min<unsigned>(grid_for(m, 256), c.sm_count * 16);
+    if (a.pos_bytes == 4)
+        subset_isa_key_kernel<uint32_t><<<gm, 256, 0, c.stream>>>(
+            (const uint32_t *)a.positions, m, n, isa, lf, sk_a, sv, bad);
+    else
+        subset_isa_key_kernel<uint64_t><<<gm, 256, 0, c.stream>>>(
+            (const uint64_t *)a.positions, m, n, isa, lf, sk_a, sv, bad);
+    CAPSSA_LAUNCHED(c);
+    int *h_bad = (int *)c.h_scratch;
+    CAPSSA_CUDA(c, cudaMemcpyAsync(h_bad, bad, 4, cudaMemcpyDeviceToHost, c.stream));
+    CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+    if (*h_bad) return set_err(c, CAPSSA_EINVAL, "a position lies beyond the end of the text");
+    bool in_b = false;
+    capssa_status s = radix::sort_pairs(c, sk_a, sv, sk_b, sv_b, (uint32_t)m, 0, bits_for(n + 1),
+                                        false, 0, &in_b);
+    if (s != CAPSSA_OK) return s;
+    const uint32_t *res = in_b ? sv_b : sv;
+    if (a.out_bytes == 4) {
+        CAPSSA_CUDA(c, cudaMemcpyAsync(a.out_sa, res, m * 4, cudaMemcpyDeviceToDevice, c.stream));
+    } else {
+        widen_kernel<uint64_t><<<gm, 256, 0, c.stream>>>(res, (uint64_t *)a.out_sa, m);
+        CAPSSA_LAUNCHED(c);
+    }
+    if (a.out_lcp) {
+        s = lcp_array_sa(c, a.text, a.sym_bytes, n, a.lim, a.max_ctx, res, m, a.out_lcp,
+                         a.out_bytes);
+        if (s != CAPSSA_OK) return s;
+    }
+    return CAPSSA_OK;
+}
+
+}  // namespace
+}  // namespace capssa

@@ -1,0 +1,272 @@
+/*
+ * capssa.h — C ABI of the GB300 suffix-array library (libcapssa_gb300.so).
+ *
+ * Drop-in for the in-memory suffix-array path of caps-sa 0.7.0 (Rust):
+ * every entry point below names the reference item it replaces
+ * (file:line inside the caps-sa crate).  The reference is generic over
+ * `S: Symbol` and `I: Index`; a Rust FFI shim binds one monomorphized symbol
+ * per (S, I) pair, which is how the names are formed here:
+ *     S in {u8, u16, u32}    I in {u32, u64}
+ *
+ * Buffers may live in host memory (pageable or pinned) or in device memory
+ * of the context's GPU; the library inspects each pointer and copies as
+ * needed.  All work of one context runs on its CUDA stream and every call
+ * returns after its outputs are complete.  A context is not thread-safe;
+ * use one per host thread.
+ *
+ * There is no CPU fallback: without a usable CUDA device every builder
+ * returns CAPSSA_ECUDA.
+ */
+#ifndef CAPSSA_H
+#define CAPSSA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CAPSSA_ABI_VERSION 1
+
+typedef enum capssa_status {
+    CAPSSA_OK = 0,
+    /* a contract violation the reference panics on (bad segment ends,
+     * position beyond the text, index type too narrow) */
+    CAPSSA_EINVAL = 1,
+    CAPSSA_ENOMEM = 2,
+    CAPSSA_ECUDA = 3,
+    /* a bounded device-side wait ran out; the context stays usable */
+    CAPSSA_ETIMEOUT = 4,
+    /* the emit callback returned nonzero (BuildError::Emit,
+     * src/ext_mem.rs:258-264) */
+    CAPSSA_EEMIT = 5,
+    /* outside what this build supports (e.g. a text of 2^32-1 or more
+     * symbols) */
+    CAPSSA_EUNSUPPORTED = 6
+} capssa_status;
+
+/* LimitProvider (src/limits.rs:27-105) as a tagged descriptor.
+ * kind PLAIN     = PlainText (src/limits.rs:125-156), ends ignored;
+ * kind SEGMENTED = SegmentedText::from_ends (src/limits.rs:261-282):
+ *                  strictly increasing cumulative ends, last == n.
+ * boundary SHORTER_FIRST  = the default boundary_order, lim_a.cmp(lim_b)
+ *                           (src/limits.rs:66-75), BoundaryRank::ShorterFirst;
+ * boundary LONGER_FIRST   = STAR's spacer-as-largest order,
+ *                           lim_b.cmp(lim_a).then(p_a.cmp(p_b))
+ *                           (src/limits.rs:48-57), BoundaryRank::LongerFirst.
+ * Arbitrary Rust boundary_order closures cannot cross the ABI. */
+typedef enum { CAPSSA_LIMITS_PLAIN = 0, CAPSSA_LIMITS_SEGMENTED = 1 } capssa_limits_kind;
+typedef enum { CAPSSA_SHORTER_FIRST = 0, CAPSSA_LONGER_FIRST = 1 } capssa_boundary;
+
+typedef struct capssa_limits {
+    int32_t kind;     /* capssa_limits_kind */
+    int32_t boundary; /* capssa_boundary */
+    const uint64_t *ends;
+    uint64_t n_ends;
+} capssa_limits;
+
+/* How the sort's first level splits suffixes into buckets. */
+typedef enum {
+    CAPSSA_PARTITION_AUTO = 0,
+    /* splitter suffixes drawn by the reference's sampling rule, bucket
+     * found by binary search with the full comparator */
+    CAPSSA_PARTITION_SPLITTERS = 1,
+    /* as SPLITTERS, but a small MLP trained on the splitter sample
+     * predicts the bucket; every prediction is checked against its two
+     * neighbouring splitters and corrected */
+    CAPSSA_PARTITION_LEARNED = 2
+} capssa_partition;
+
+/* Opts{max_context} (src/sample_sort.rs:70-85) and the in-memory subset of
+ * ExtMemOpts (src/ext_mem.rs:60-118).  Zero-initialise, then set
+ * max_context = CAPSSA_UNBOUNDED for the reference default. */
+#define CAPSSA_UNBOUNDED UINT64_MAX
+typedef struct capssa_opts {
+    uint64_t max_context;      /* comparison cap; CAPSSA_UNBOUNDED default */
+    uint64_t subproblem_count; /* p of the sample sort; 0 = auto rule of
+                                  effective_subproblem_count, src/ext_mem.rs:1159-1178 */
+    int32_t partition;         /* capssa_partition (sample-sort builders) */
+    int32_t host_threads;      /* thread count the auto p rule assumes; 0 = all cores */
+    uint64_t reserved[6];
+} capssa_opts;
+
+void capssa_opts_default(capssa_opts *o);
+
+/* Per-call statistics of the last builder call on a context. */
+typedef struct capssa_stats {
+    uint64_t n_suffixes;        /* suffixes sorted */
+    uint32_t key_symbols;       /* symbols per packed prefix key */
+    uint32_t key_bits_per_symbol;
+    uint32_t refine_rounds;     /* rank-doubling rounds after the key sort */
+    uint32_t partitions;        /* buckets of the sample sort (0 if none) */
+    uint64_t refined_suffixes;  /* sum over rounds of suffixes still tied */
+    uint64_t max_partition;     /* largest bucket */
+    uint64_t mispredicted;      /* learned partition: predictions corrected */
+    uint64_t kernel_launches;   /* kernels launched by the call */
+    double device_ms;           /* device time of the call (CUDA events) */
+    double h2d_ms;
+    double d2h_ms;
+    uint64_t h2d_bytes;
+    uint64_t d2h_bytes;
+    /* device time per phase of the last suffix sort (CUDA events on the
+     * context's stream) */
+    double keys_ms;       /* alphabet scan + packed-key build */
+    double sort_ms;       /* initial radix sort, all passes */
+    double refine_ms;     /* rank-doubling rounds */
+    double finish_ms;     /* bounded-context pass, output ordering and copy */
+    uint32_t sort_passes; /* radix passes executed by the initial sort */
+    uint32_t reserved0;
+    double sort_pass_ms;  /* summed duration of those radix-pass kernels */
+} capssa_stats;
+
+typedef struct capssa_ctx capssa_ctx;
+
+/* Create a context on CUDA device `device`. */
+capssa_status capssa_ctx_create(capssa_ctx **out, int device);
+void capssa_ctx_destroy(capssa_ctx *ctx);
+/* Run the context's work on an existing cudaStream_t (NULL = own stream). */
+capssa_status capssa_ctx_set_stream(capssa_ctx *ctx, void *cuda_stream);
+/* Text of the last error on this context ("" if none). */
+const char *capssa_ctx_last_error(const capssa_ctx *ctx);
+capssa_status capssa_ctx_stats(const capssa_ctx *ctx, capssa_stats *out);
+/* Device bytes currently held by the context's workspace. */
+uint64_t capssa_ctx_workspace_bytes(const capssa_ctx *ctx);
+/* Release the context's cached workspace. */
+void capssa_ctx_trim(capssa_ctx *ctx);
+int capssa_abi_version(void);
+
+/* Emit callback of the sample-sort builders: called in suffix order with
+ * consecutive batches of positions (u64).  The reference calls
+ * FnMut(u64) -> Result<(), E> once per position (src/ext_mem.rs:1932-1937);
+ * a per-position FFI call would cost more than the sort, so batches cross
+ * instead.  Return 0 to continue, nonzero to abort (-> CAPSSA_EEMIT). */
+typedef int (*capssa_emit_fn)(void *user, const uint64_t *positions, uint64_t len);
+
+/* ---------------------------------------------------------------------
+ * Builders
+ * ------------------------------------------------------------------- */
+
+/* build_in_memory / _with_opts / _with (src/sample_sort.rs:97-127):
+ * the suffix array of `text` (n symbols) into out_sa[0..n).
+ * lp == NULL means PlainText, opts == NULL means Opts::default(). */
+#define CAPSSA_DECL_BUILD(S, ST, I, IT)                                                   \
+    capssa_status capssa_build_in_memory_##S##_##I(capssa_ctx *ctx, const ST *text,       \
+                                                   uint64_t n, const capssa_limits *lp,   \
+                                                   const capssa_opts *opts, IT *out_sa);
+
+/* build_in_memory_for_positions / _with_opts / _with
+ * (src/sample_sort.rs:143-206): the given positions (each <= n) reordered
+ * by suffix into out_sa[0..m). */
+#define CAPSSA_DECL_BUILD_POS(S, ST, I, IT)                                               \
+    capssa_status capssa_build_in_memory_for_positions_##S##_##I(                         \
+        capssa_ctx *ctx, const ST *text, uint64_t n, const IT *positions, uint64_t m,     \
+        const capssa_limits *lp, const capssa_opts *opts, IT *out_sa);
+
+/* merge_sort's postcondition (src/sample_sort.rs:208-216) exposed: the
+ * suffix array plus lcp[0] = 0, lcp[i] = lcp(sa[i-1], sa[i]) capped by both
+ * limits and max_context.  positions == NULL sorts every position. */
+#define CAPSSA_DECL_BUILD_LCP(S, ST, I, IT)                                               \
+    capssa_status capssa_build_in_memory_lcp_##S##_##I(                                   \
+        capssa_ctx *ctx, const ST *text, uint64_t n, const IT *positions, uint64_t m,     \
+        const capssa_limits *lp, const capssa_opts *opts, IT *out_sa, IT *out_lcp);
+
+/* sample_sort::merge (src/sample_sort.rs:397-522, drain :614-636): merge two
+ * LCP-annotated sorted runs into z / lcp_z (len_x + len_y), with the
+ * reference's tie rule (a comparator tie outputs the stream not last
+ * output from). */
+#define CAPSSA_DECL_MERGE(S, ST, I, IT)                                                   \
+    capssa_status capssa_merge_##S##_##I(                                                 \
+        capssa_ctx *ctx, const ST *text, uint64_t n, const capssa_limits *lp,             \
+        const IT *x, const IT *lcp_x, uint64_t len_x, const IT *y, const IT *lcp_y,       \
+        uint64_t len_y, uint64_t max_context, IT *z, IT *lcp_z);
+
+/* build_in_memory_sample_sort[_with] / try_* (src/ext_mem.rs:711-783):
+ * positions emitted in suffix order through `emit`. */
+#define CAPSSA_DECL_SS(S, ST)                                                             \
+    capssa_status capssa_build_in_memory_sample_sort_##S(                                 \
+        capssa_ctx *ctx, const ST *text, uint64_t n, const capssa_limits *lp,             \
+        const capssa_opts *opts, capssa_emit_fn emit, void *user);                        \
+    /* build_in_memory_sample_sort_for_positions[_with] / try_*                           \
+     * (src/ext_mem.rs:785-871) */                                                        \
+    capssa_status capssa_build_in_memory_sample_sort_for_positions_##S(                   \
+        capssa_ctx *ctx, const ST *text, uint64_t n, const uint64_t *positions,           \
+        uint64_t m, const capssa_limits *lp, const capssa_opts *opts, capssa_emit_fn emit, \
+        void *user);                                                                      \
+    /* LcpDispatch::lcp (src/lcp.rs:125-153) for `count` pairs (p[i], q[i]) */            \
+    capssa_status capssa_lcp_##S(capssa_ctx *ctx, const ST *text, uint64_t n,             \
+                                 const uint64_t *p, const uint64_t *q, uint64_t count,    \
+                                 uint64_t max_context, uint64_t *out);                    \
+    /* LcpDispatch::suffix_cmp_with (src/lcp.rs:184-201): -1, 0, 1 per pair */            \
+    capssa_status capssa_suffix_cmp_##S(capssa_ctx *ctx, const ST *text, uint64_t n,      \
+                                        const capssa_limits *lp, const uint64_t *p,       \
+                                        const uint64_t *q, uint64_t count,                \
+                                        uint64_t max_context, int8_t *out);
+
+/* Many independent texts in one launch sequence: texts[offsets[t] ..
+ * offsets[t+1]) is text t (offsets has n_texts+1 entries, offsets[0] == 0).
+ * out_sa[offsets[t] + i] receives the i-th suffix of text t as a position
+ * local to that text, exactly build_in_memory(text_t). */
+#define CAPSSA_DECL_BATCHED(S, ST, I, IT)                                                 \
+    capssa_status capssa_build_batched_##S##_##I(                                         \
+        capssa_ctx *ctx, const ST *texts, const uint64_t *offsets, uint64_t n_texts,      \
+        const capssa_opts *opts, IT *out_sa);
+
+#define CAPSSA_DECL_ALL_I(S, ST)                                                          \
+    CAPSSA_DECL_BUILD(S, ST, u32, uint32_t)                                               \
+    CAPSSA_DECL_BUILD(S, ST, u64, uint64_t)                                               \
+    CAPSSA_DECL_BUILD_POS(S, ST, u32, uint32_t)                                           \
+    CAPSSA_DECL_BUILD_POS(S, ST, u64, uint64_t)                                           \
+    CAPSSA_DECL_BUILD_LCP(S, ST, u32, uint32_t)                                           \
+    CAPSSA_DECL_BUILD_LCP(S, ST, u64, uint64_t)                                           \
+    CAPSSA_DECL_MERGE(S, ST, u32, uint32_t)                                               \
+    CAPSSA_DECL_MERGE(S, ST, u64, uint64_t)                                               \
+    CAPSSA_DECL_BATCHED(S, ST, u32, uint32_t)                                             \
+    CAPSSA_DECL_BATCHED(S, ST, u64, uint64_t)                                             \
+    CAPSSA_DECL_SS(S, ST)
+
+CAPSSA_DECL_ALL_I(u8, uint8_t)
+CAPSSA_DECL_ALL_I(u16, uint16_t)
+CAPSSA_DECL_ALL_I(u32, uint32_t)
+
+/* ---------------------------------------------------------------------
+ * Packed-prefix keys (src/pack.rs), u8 text only like the reference
+ * (seed_params requires S == u8, src/pack.rs:223-228).
+ * ------------------------------------------------------------------- */
+
+typedef enum {
+    CAPSSA_SEED_DISABLED = 0,
+    CAPSSA_SEED_DENSE_ALPHABET_ONLY = 1,
+    CAPSSA_SEED_REMAP = 2
+} capssa_seed_policy;
+
+typedef struct capssa_packer {
+    uint32_t bits;      /* bits per packed field */
+    uint32_t k;         /* symbols per u64 key */
+    uint32_t alphabet;  /* distinct symbols; `alphabet` is the sentinel */
+    uint32_t identity;  /* 1 when codes equal the bytes */
+    uint8_t code[256];  /* byte -> code (order preserving) */
+} capssa_packer;
+
+/* Packer::new + seed_params (src/pack.rs:103-176, 217-234).  Returns
+ * CAPSSA_OK and *available = 1 when a packer exists. */
+capssa_status capssa_pack_params_u8(capssa_ctx *ctx, const uint8_t *text, uint64_t n,
+                                    int32_t policy, uint64_t max_extra_bytes,
+                                    capssa_packer *out, int32_t *available);
+/* Packer::key_at_bounded for each position (src/pack.rs:187-203). */
+capssa_status capssa_pack_keys_u8(capssa_ctx *ctx, const uint8_t *text, uint64_t n,
+                                  const capssa_packer *pk, const capssa_limits *lp,
+                                  const uint64_t *positions, uint64_t m, uint64_t *keys);
+/* seed_subarray (src/pack.rs:241-321): sort `sa` in place by suffix using
+ * the packed keys first, and fill lcp. */
+capssa_status capssa_seed_subarray_u8_u32(capssa_ctx *ctx, const uint8_t *text, uint64_t n,
+                                          const capssa_packer *pk, const capssa_limits *lp,
+                                          uint32_t *sa, uint32_t *lcp, uint64_t m);
+capssa_status capssa_seed_subarray_u8_u64(capssa_ctx *ctx, const uint8_t *text, uint64_t n,
+                                          const capssa_packer *pk, const capssa_limits *lp,
+                                          uint64_t *sa, uint64_t *lcp, uint64_t m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CAPSSA_H */
