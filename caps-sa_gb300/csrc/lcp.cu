@@ -2,6 +2,7 @@
 // suffix_cmp_with, the bounded-context run flags, and the merge-path
 // version of the reference's LCP-enhanced two-way merge.
 #include <algorithm>
+#include <mutex>
 
 #include "lcp.cuh"
 
@@ -392,3 +393,139 @@ capssa_status merge_runs(Ctx &c, const void *text, int sym_bytes, const DevLimit
 }
 
 }  // namespace capssa
+
+// ====================================================================
+// Allocation-free merge entry point.
+//
+// Some callers cannot call cudaMalloc at the point where they need a merge:
+// a host application that hands all device memory to its own pool allocator
+// up front, code running between other work on a stream where an allocation
+// (and the device-wide synchronisation cudaMalloc/cudaFree may imply) is not
+// acceptable, or a caller without a library context.  For them
+// capssa_merge_noalloc_u8_u32 runs the same merge-path kernels as
+// capssa_merge_u8_u32, but with every buffer supplied by the caller and the
+// merge-path scratch (split points and safety flags) taken from a fixed
+// file-scope device array instead of the context workspace.
+// ====================================================================
+
+namespace capssa {
+namespace {
+
+// Largest merge (len_x + len_y) the static scratch serves: 2^24 records.
+constexpr uint64_t kNoAllocMaxRecords = 1ull << 24;
+constexpr uint64_t kNoAllocMaxSegs = kNoAllocMaxRecords / kMergeSeg;  // 131072
+constexpr size_t kNoAllocSplitBytes = (kNoAllocMaxSegs + 1) * 8;
+constexpr size_t kNoAllocSafeOff = (kNoAllocSplitBytes + 255) & ~size_t(255);
+constexpr size_t kNoAllocFlagOff = (kNoAllocSafeOff + kNoAllocMaxSegs + 1 + 255) & ~size_t(255);
+constexpr size_t kNoAllocScratchBytes = kNoAllocFlagOff + 256;  // about 1.2 MiB
+
+// Held by every GPU that loads the library until the process exits.  Every
+// call shares it and it keeps the last call's contents.
+static __device__ __align__(256) unsigned char g_noalloc_merge_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the host-side symbol is only a stand-in, never a device
+// address).
+cudaError_t noalloc_scratch(int dev, unsigned char **out) {
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_merge_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = (unsigned char *)g_noalloc_ptr[dev];
+    return cudaSuccess;
+}
+
+// Contract checks the reference makes by panicking: positions <= n and
+// SegmentedText ends strictly increasing with the last one equal to n.
+__global__ void noalloc_check_kernel(const uint32_t *__restrict__ x, uint64_t lx,
+                                     const uint32_t *__restrict__ y, uint64_t ly, uint64_t n,
+                                     const uint64_t *__restrict__ ends, uint64_t n_ends,
+                                     uint32_t *__restrict__ bad) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < lx + ly + n_ends;
+         i += stride) {
+        bool ok;
+        if (i < lx)
+            ok = x[i] <= n;
+        else if (i < lx + ly)
+            ok = y[i - lx] <= n;
+        else {
+            uint64_t e = i - lx - ly;
+            ok = (e == 0 || ends[e - 1] < ends[e]) && (e + 1 < n_ends || ends[e] == n);
+        }
+        if (!ok) atomicExch(bad, 1u);
+    }
+}
+
+}  // namespace
+}  // namespace capssa
+
+extern "C" capssa_status capssa_merge_noalloc_u8_u32(
+    void *cuda_stream, const uint8_t *text, uint64_t n, const uint64_t *ends, uint64_t n_ends,
+    int32_t boundary, const uint32_t *x, const uint32_t *lcp_x, uint64_t len_x,
+    const uint32_t *y, const uint32_t *lcp_y, uint64_t len_y, uint64_t max_context, uint32_t *z,
+    uint32_t *lcp_z) {
+    using namespace capssa;
+    const uint64_t total = len_x + len_y;
+    if (total == 0) return CAPSSA_OK;
+    if (total > kNoAllocMaxRecords) return CAPSSA_EINVAL;
+    if (boundary != CAPSSA_SHORTER_FIRST && boundary != CAPSSA_LONGER_FIRST) return CAPSSA_EINVAL;
+    if (!text || !z || !lcp_z || (len_x && (!x || !lcp_x)) || (len_y && (!y || !lcp_y)) ||
+        (n_ends && !ends))
+        return CAPSSA_EINVAL;
+    cudaStream_t stream = (cudaStream_t)cuda_stream;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return CAPSSA_ECUDA;
+    unsigned char *scratch = nullptr;
+    if (noalloc_scratch(dev, &scratch) != cudaSuccess) return CAPSSA_ECUDA;
+    uint64_t *split = (uint64_t *)scratch;
+    uint8_t *safe = scratch + kNoAllocSafeOff;
+    uint32_t *bad = (uint32_t *)(scratch + kNoAllocFlagOff);
+
+    // the flag keeps the previous call's value: clear it first
+    if (cudaMemsetAsync(bad, 0, 4, stream) != cudaSuccess) return CAPSSA_ECUDA;
+    noalloc_check_kernel<<<256, 256, 0, stream>>>(x, len_x, y, len_y, n, ends, n_ends, bad);
+    uint32_t h_bad = 0;
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(&h_bad, bad, 4, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+        cudaStreamSynchronize(stream) != cudaSuccess)
+        return CAPSSA_ECUDA;
+    if (h_bad) return CAPSSA_EINVAL;
+
+    if (len_x == 0 || len_y == 0) {
+        const uint32_t *src = len_x ? x : y, *ls = len_x ? lcp_x : lcp_y;
+        if (cudaMemcpyAsync(z, src, total * 4, cudaMemcpyDeviceToDevice, stream) != cudaSuccess ||
+            cudaMemcpyAsync(lcp_z, ls, total * 4, cudaMemcpyDeviceToDevice, stream) != cudaSuccess ||
+            cudaStreamSynchronize(stream) != cudaSuccess)
+            return CAPSSA_ECUDA;
+        return CAPSSA_OK;
+    }
+    DevLimits L{};
+    L.n = n;
+    L.longer_first = boundary == CAPSSA_LONGER_FIRST;
+    if (n_ends) {  // SegmentedText without the coarse directory: binary search over ends
+        L.segmented = 1;
+        L.ends = ends;
+        L.n_ends = n_ends;
+    }
+    const uint64_t nseg = (total + kMergeSeg - 1) / kMergeSeg;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    unsigned g = grid_for(nseg + 1, 128, (unsigned)(sms > 0 ? sms : 1) * 16);
+    merge_split_kernel<uint32_t><<<g, 128, 0, stream>>>(text, 1, L, x, len_x, y, len_y,
+                                                        max_context, nseg, split, safe);
+    merge_seg_kernel<uint32_t><<<g, 128, 0, stream>>>(text, 1, L, x, lcp_x, len_x, y, lcp_y,
+                                                      len_y, max_context, nseg, split, safe, z,
+                                                      lcp_z);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(stream) != cudaSuccess)
+        return CAPSSA_ECUDA;
+    return CAPSSA_OK;
+}

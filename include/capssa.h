@@ -266,6 +266,42 @@ capssa_status capssa_seed_subarray_u8_u64(capssa_ctx *ctx, const uint8_t *text, 
                                           const capssa_packer *pk, const capssa_limits *lp,
                                           uint64_t *sa, uint64_t *lcp, uint64_t m);
 
+/* ---------------------------------------------------------------------
+ * Allocation-free merge.  No counterpart in the reference: it exists for
+ * callers that cannot call cudaMalloc where they need a merge (an
+ * application whose own pool allocator owns all device memory, a stream
+ * where the synchronisation an allocation may imply is not acceptable, or a
+ * caller without a capssa_ctx).
+ *
+ * Same result as capssa_merge_u8_u32 (sample_sort::merge,
+ * src/sample_sort.rs:397-522), but it allocates nothing: every pointer is a
+ * device pointer owned by the caller, and the merge-path scratch lives in a
+ * fixed static device array of about 1.2 MiB that every GPU loading the
+ * library holds until the process exits.
+ *   - len_x + len_y must be at most 2^24 records; larger merges return
+ *     CAPSSA_EINVAL.
+ *   - text must be followed by at least 64 readable bytes (the vector LCP
+ *     reads past the last compared byte).
+ *   - ends == NULL / n_ends == 0 means PlainText; otherwise SegmentedText
+ *     ends on the device (checked like from_ends).  boundary is a
+ *     capssa_boundary.
+ *   - runs on `cuda_stream` (NULL = legacy default stream) of the current
+ *     device and returns after the merge has finished.  The first call on a
+ *     device looks up the scratch array's device address; make that first
+ *     call before any stream capture.
+ *   - every call shares the one scratch array (it keeps the last call's
+ *     contents); calls that overlap on the GPU, on any streams or host
+ *     threads, race on it and must be serialised by the caller.
+ * Returns CAPSSA_EINVAL for contract violations (position > n, bad ends,
+ * oversize merge), CAPSSA_ECUDA for CUDA errors; no error text is kept. */
+capssa_status capssa_merge_noalloc_u8_u32(void *cuda_stream, const uint8_t *text, uint64_t n,
+                                          const uint64_t *ends, uint64_t n_ends,
+                                          int32_t boundary, const uint32_t *x,
+                                          const uint32_t *lcp_x, uint64_t len_x,
+                                          const uint32_t *y, const uint32_t *lcp_y,
+                                          uint64_t len_y, uint64_t max_context, uint32_t *z,
+                                          uint32_t *lcp_z);
+
 #ifdef __cplusplus
 }
 #endif
