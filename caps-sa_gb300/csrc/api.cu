@@ -65,19 +65,33 @@ capssa_status check_dev_flags(Ctx &c) {
     return CAPSSA_OK;
 }
 
-KeyGeom key_geom(int b) {
+// Key geometry for b bits per symbol on a text of n symbols.  The widest
+// key holds kmax symbols (kmax*b + bits(kmax) <= 64).  Symbols past
+// log_{2^b}(n) + 4 rarely separate random suffixes, so the key keeps only
+// as many symbols as fit in the radix passes that this minimum needs:
+// DNA at n = 2^28 keeps 21 symbols in 6 passes instead of 29 in 8.
+KeyGeom key_geom(int b, uint64_t n) {
     KeyGeom g{};
     g.b = b < 1 ? 1 : b;
-    int best = 1;
-    for (int k = 1; k * g.b <= 63; k++) {
+    auto lbits_of = [](int k) {
         int lb = 0;
         while ((1 << lb) <= k) lb++;  // bits of 0..k
-        if (k * g.b + lb <= 64) best = k;
+        return lb;
+    };
+    int kmax = 1;
+    for (int k = 1; k * g.b <= 63; k++)
+        if (k * g.b + lbits_of(k) <= 64) kmax = k;
+    int logn = 0;
+    while (logn < 64 && (n >> logn) > 1) logn++;
+    int kmin = (logn + g.b - 1) / g.b + 4;
+    int k = kmax;
+    if (kmin < kmax) {
+        int passes = (kmin * g.b + lbits_of(kmin) + 7) / 8;
+        k = kmin;
+        while (k + 1 <= kmax && (k + 1) * g.b + lbits_of(k + 1) <= 8 * passes) k++;
     }
-    g.k = best;
-    int lb = 0;
-    while ((1 << lb) <= best) lb++;
-    g.lbits = lb;
+    g.k = k;
+    g.lbits = lbits_of(k);
     g.total = g.k * g.b + g.lbits;
     return g;
 }

@@ -55,14 +55,13 @@ inline capssa_status engine_build(Ctx &c, const EngineArgs &a) {
     }
 }
 
-// Key geometry for b bits per symbol: the largest k with k*b plus the bits
-// of a 0..k length field fitting in 64.
+// Key geometry for b bits per symbol and n symbols (api.cu).
 struct KeyGeom {
     int b;       // bits per symbol
     int k;       // symbols per key
     int lbits;   // bits of the length field
     int total;   // k*b + lbits
 };
-KeyGeom key_geom(int b);
+KeyGeom key_geom(int b, uint64_t n);
 
 }  // namespace capssa

@@ -41,8 +41,29 @@ constexpr unsigned long long kBigTotMask = kBigOrdUnit - 1;
 template <typename S>
 __global__ void presence_kernel(const S *__restrict__ text, uint64_t n,
                                 uint32_t *__restrict__ present) {
-    // u8/u16: presence flags per symbol value; idempotent stores, read first
-    // so repeated symbols cost no write traffic.
+    // u8: per-block flags in shared memory, merged once per block; u16:
+    // idempotent global flags, read first so repeats cost no write traffic.
+    if (sizeof(S) == 1) {
+        __shared__ uint32_t f[256];
+        f[threadIdx.x & 255] = 0;
+        __syncthreads();
+        const uint64_t nv = n / 16;
+        const uint4 *t4 = reinterpret_cast<const uint4 *>(text);
+        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nv;
+             i += (uint64_t)gridDim.x * blockDim.x) {
+            uint4 v = t4[i];
+            uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int j = 0; j < 16; j++) f[(w[j >> 2] >> ((j & 3) * 8)) & 255] = 1;
+        }
+        for (uint64_t i = nv * 16 + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+             i += (uint64_t)gridDim.x * blockDim.x)
+            f[(uint32_t)text[i]] = 1;
+        __syncthreads();
+        for (int i = threadIdx.x; i < 256; i += blockDim.x)
+            if (f[i] && __ldcg(present + i) == 0) present[i] = 1;
+        return;
+    }
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t s = (uint32_t)text[i];
@@ -82,31 +103,71 @@ struct Coder {
     }
 };
 
-// Composite key of every text position (engine.cuh step 2).
+// Composite key of every text position (engine.cuh step 2), with the digit
+// histograms of every radix pass accumulated on the way (so the sort needs
+// no separate histogram read of the keys).  Each thread owns kKeyPer
+// consecutive positions: the k-symbol window slides one symbol per
+// position over codes staged in shared memory, and only suffixes that end
+// inside the window (lim < k) are masked and padded.
 template <typename S>
 __global__ void __launch_bounds__(kKeyThreads)
     key_kernel(const S *__restrict__ text, uint64_t n, DevLimits L, Coder<S> coder, int b,
-               int k, int lbits, uint64_t max_ctx, int lf, uint64_t *__restrict__ keys) {
+               int k, int lbits, int lf, int n_passes, uint64_t *__restrict__ keys,
+               uint32_t *__restrict__ counts) {
     __shared__ uint32_t codes[kKeyTile + 64];
+    __shared__ uint32_t hist[8 * 256];
     const uint64_t t0 = (uint64_t)blockIdx.x * kKeyTile;
+    for (int i = threadIdx.x; i < n_passes * 256; i += kKeyThreads) hist[i] = 0;
     for (int i = threadIdx.x; i < kKeyTile + k; i += kKeyThreads) {
         uint64_t p = t0 + i;
         codes[i] = p < n ? coder(text[p]) : 0u;
     }
     __syncthreads();
-    const uint64_t pad = lf ? ((1ull << b) - 1) : 0ull;
-#pragma unroll 1
-    for (int e = 0; e < kKeyPer; e++) {
-        int i = threadIdx.x + e * kKeyThreads;
-        uint64_t p = t0 + i;
-        if (p >= n) break;
-        uint64_t lim = dev_lim_at(L, p);
-        uint64_t eff = lim < max_ctx ? lim : max_ctx;
-        int take = eff < (uint64_t)k ? (int)eff : k;
-        uint64_t content = 0;
-        for (int j = 0; j < k; j++) content = (content << b) | (j < take ? (uint64_t)codes[i + j] : pad);
-        keys[p] = (content << lbits) | (uint64_t)(lf ? k - take : take);
+    const int i0 = threadIdx.x * kKeyPer;
+    const uint64_t p0 = t0 + i0;
+    const uint64_t kbits = (uint64_t)k * b;
+    const uint64_t kmask = (1ull << kbits) - 1;
+    if (p0 < n) {
+        uint64_t w = 0;
+        for (int j = 0; j < k; j++) w = (w << b) | codes[i0 + j];
+        uint64_t end = p0 + dev_lim_at(L, p0);  // one past the last symbol of p0's suffix
+        uint64_t out[kKeyPer];
+#pragma unroll
+        for (int e = 0; e < kKeyPer; e++) {
+            const uint64_t p = p0 + e;
+            uint64_t key = 0;
+            if (p < n) {
+                if (p >= end) end = p + dev_lim_at(L, p);
+                const uint64_t lim = end - p;
+                uint64_t content = w;
+                int take = k;
+                if (lim < (uint64_t)k) {
+                    take = (int)lim;
+                    uint64_t low = (uint64_t)(k - take) * b;
+                    uint64_t lowmask = (1ull << low) - 1;
+                    content = lf ? (w | lowmask) : (w & ~lowmask);
+                }
+                key = (content << lbits) | (uint64_t)(lf ? k - take : take);
+                for (int ps = 0; ps < n_passes; ps++)
+                    atomicAdd(&hist[ps * 256 + ((key >> (8 * ps)) & 255)], 1u);
+            }
+            out[e] = key;
+            w = ((w << b) | codes[i0 + e + k]) & kmask;
+        }
+        if (p0 + kKeyPer <= n) {
+            uint4 *dst = reinterpret_cast<uint4 *>(keys + p0);
+#pragma unroll
+            for (int e = 0; e < kKeyPer; e += 2)
+                dst[e / 2] = make_uint4((uint32_t)out[e], (uint32_t)(out[e] >> 32),
+                                        (uint32_t)out[e + 1], (uint32_t)(out[e + 1] >> 32));
+        } else {
+            for (int e = 0; e < kKeyPer; e++)
+                if (p0 + e < n) keys[p0 + e] = out[e];
+        }
     }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n_passes * 256; i += kKeyThreads)
+        if (hist[i]) atomicAdd(&counts[i], hist[i]);
 }
 
 // ---------------------------------------------------------------- groups
@@ -247,6 +308,126 @@ __global__ void sort_small_kernel(const uint2 *__restrict__ groups, uint32_t cou
                 rank[pp[u]] = (ended && lf) ? g.x + u : g.x + t;
             }
             if (!ended && e - t >= 2) append_group(G, nxt, g.x + t, e - t);
+            t = e;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- direct resolution
+
+// Small tied groups are resolved by comparing the suffixes themselves, as
+// the reference's merge does with LcpDispatch::lcp (src/lcp.rs:125-153),
+// but on a bit-packed copy of the text: one 64-bit window holds 64/b
+// symbols (32 for DNA), so a suffix pair that differs within ~100 symbols
+// costs a few sector reads instead of several rank-doubling rounds.
+constexpr uint64_t kDirectCap = 256;     // symbols compared past the shared prefix (at least h)
+constexpr uint64_t kDirectMaxH = 4096;   // deeper groups fall back to rank doubling
+
+struct Packed {
+    const uint64_t *w;  // MSB-first b-bit codes, zero padded
+    int b;              // bits per symbol
+    int spw;            // whole symbols per 64-bit window
+    uint64_t mask;      // the spw*b leading bits
+};
+
+// 64-bit window of the packed text starting at symbol p.
+__device__ __forceinline__ uint64_t window_at(const Packed &P, uint64_t p) {
+    uint64_t s = p * (uint64_t)P.b;
+    uint64_t wi = s >> 6;
+    uint32_t sh = (uint32_t)(s & 63);
+    uint64_t v = __ldg(P.w + wi);
+    if (sh) v = (v << sh) | (__ldg(P.w + wi + 1) >> (64 - sh));
+    return v & P.mask;
+}
+
+// Order of suffixes a and b, known to agree on their first `o` symbols:
+// -1 / 1, 0 for a complete tie (ShorterFirst, equal limits), 2 when they
+// still agree `cap` symbols further (undecided).  Mirrors suffix_cmp_with
+// (src/lcp.rs:184-201) from offset o.
+__device__ __forceinline__ int direct_cmp(const Packed &P, uint64_t a, uint64_t la, uint64_t b,
+                                          uint64_t lb, uint64_t o, uint64_t cap, int lf) {
+    const uint64_t lim = la < lb ? la : lb;
+    const uint64_t end = lim < o + cap ? lim : o + cap;
+    for (uint64_t t = o; t < end; t += (uint64_t)P.spw) {
+        uint64_t va = window_at(P, a + t), vb = window_at(P, b + t);
+        uint64_t x = va ^ vb;
+        if (x) {
+            uint64_t d = (uint64_t)__clzll((long long)x) / (uint64_t)P.b;
+            if (t + d < end) return va < vb ? -1 : 1;
+            break;
+        }
+    }
+    if (end < lim) return 2;
+    if (!lf) return (la > lb) - (la < lb);
+    if (la != lb) return (lb > la) - (lb < la);
+    return (a > b) - (a < b);
+}
+
+template <typename S>
+__global__ void pack_text_kernel(const S *__restrict__ text, uint64_t n, Coder<S> coder, int b,
+                                 uint64_t *__restrict__ words, uint64_t nwords) {
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwords;
+         w += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t bit0 = w * 64;
+        uint64_t i0 = bit0 / (uint64_t)b, i1 = (bit0 + 63) / (uint64_t)b;
+        uint64_t v = 0;
+        for (uint64_t i = i0; i <= i1; i++) {
+            if (i >= n) break;
+            uint64_t c = coder(text[i]);
+            int64_t off = (int64_t)(i * (uint64_t)b) - (int64_t)bit0;
+            int64_t shift = 64 - off - b;
+            if (shift >= 0)
+                v |= shift < 64 ? (c << shift) : 0ull;
+            else
+                v |= c >> (-shift);
+        }
+        words[w] = v;
+    }
+}
+
+// One thread sorts one small tied group (all members agree on h symbols)
+// by direct comparison, writes the SA slice and ranks, and passes groups
+// still undecided after max(h, kDirectCap) more symbols to the next round
+// (they then agree on >= 2h symbols, the next round's depth).
+__global__ void direct_small_kernel(const uint2 *__restrict__ groups, uint32_t count,
+                                    uint32_t *__restrict__ sa, uint32_t *__restrict__ rank,
+                                    DevLimits L, Packed P, uint64_t h, uint64_t cap, int lf,
+                                    GroupLists G, int nxt) {
+    for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < count;
+         gi += gridDim.x * blockDim.x) {
+        const uint2 g = groups[gi];
+        uint32_t pp[kSmallMax];
+        uint64_t ll[kSmallMax];
+        for (uint32_t t = 0; t < g.y; t++) {
+            uint32_t p = sa[g.x + t];
+            uint64_t lp = dev_lim_at(L, p);
+            int j = (int)t - 1;
+            while (j >= 0) {
+                int r = direct_cmp(P, pp[j], ll[j], p, lp, h, cap, lf);
+                bool after = r == 1 || ((r == 0 || r == 2) && pp[j] > p);
+                if (!after) break;
+                pp[j + 1] = pp[j];
+                ll[j + 1] = ll[j];
+                j--;
+            }
+            pp[j + 1] = p;
+            ll[j + 1] = lp;
+        }
+        uint32_t t = 0;
+        while (t < g.y) {
+            uint32_t e = t + 1;
+            int rel = -1;
+            while (e < g.y) {
+                int r = direct_cmp(P, pp[e - 1], ll[e - 1], pp[e], ll[e], h, cap, lf);
+                if (r != 0 && r != 2) break;
+                rel = r;
+                e++;
+            }
+            for (uint32_t u = t; u < e; u++) {
+                sa[g.x + u] = pp[u];
+                rank[pp[u]] = g.x + t;
+            }
+            if (rel == 2 && e - t >= 2) append_group(G, nxt, g.x + t, e - t);
             t = e;
         }
     }
@@ -466,7 +647,7 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
         sigma_span = (uint64_t)h_mm[1] - h_mm[0] + 1;
     }
     const int b = bits_for(sigma_span > 1 ? sigma_span - 1 : 1);
-    const KeyGeom geo = key_geom(b);
+    const KeyGeom geo = key_geom(b, n);
     c.stats.key_symbols = geo.k;
     c.stats.key_bits_per_symbol = geo.b;
 
@@ -481,14 +662,30 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
     if (!keys_a || !keys_b || !vals_a || !vals_b || !rank || !key2)
         return set_err(c, CAPSSA_ENOMEM, "suffix-sort workspace");
     Coder<S> coder{table, minv};
+    const int key_passes = (geo.total + 7) / 8;
+    uint32_t *counts = radix::hist_buffer(c);
+    if (!counts) return set_err(c, CAPSSA_ENOMEM, "radix histograms");
+    CAPSSA_CUDA(c, cudaMemsetAsync(counts, 0, radix::kMaxPasses * 256 * 4, c.stream));
     key_kernel<S><<<grid_for(n, kKeyTile), kKeyThreads, 0, c.stream>>>(
-        text, n, a.lim, coder, geo.b, geo.k, geo.lbits, CAPSSA_UNBOUNDED, lf, keys_a);
+        text, n, a.lim, coder, geo.b, geo.k, geo.lbits, lf, key_passes, keys_a, counts);
     CAPSSA_LAUNCHED(c);
+    // bit-packed copy of the text for direct comparisons of small groups
+    const uint64_t nwords = (n * (uint64_t)geo.b + 63) / 64 + 4;
+    uint64_t *packed = (uint64_t *)ws_get(c, WS_PACKED, nwords * 8);
+    if (!packed) return set_err(c, CAPSSA_ENOMEM, "packed text");
+    pack_text_kernel<S><<<std::min<unsigned>(grid_for(nwords, 256), c.sm_count * 16), 256, 0,
+                          c.stream>>>(text, n, coder, geo.b, packed, nwords);
+    CAPSSA_LAUNCHED(c);
+    Packed P;
+    P.w = packed;
+    P.b = geo.b;
+    P.spw = 64 / geo.b;
+    P.mask = P.spw * P.b >= 64 ? ~0ull : (~0ull << (64 - P.spw * P.b));
     cudaEventRecord(c.pev[1], c.stream);
     bool in_b = false;
     int passes = 0;
     capssa_status s = radix::sort_pairs(c, keys_a, vals_a, keys_b, vals_b, nn, 0, geo.total, true,
-                                        0, &in_b, &passes);
+                                        0, &in_b, &passes, /*hist_ready=*/true);
     if (s != CAPSSA_OK) return s;
     c.stats.sort_passes = (uint32_t)passes;
     cudaEventRecord(c.pev[2], c.stream);
@@ -533,7 +730,8 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
         CAPSSA_CUDA(c, cudaMemsetAsync(&G.ctr->big_packed[nxt], 0, 8, c.stream));
         // gathers read ranks of the previous depth; all of them finish
         // before any rank of this round is rewritten (stream order)
-        if (ns) {
+        const bool direct = h <= kDirectMaxH;
+        if (ns && !direct) {
             gather_small_kernel<<<grid_for(ns, 128), 128, 0, c.stream>>>(
                 G.small[cur], ns, sa, rank, a.lim, h, lf, empty_lf, key2);
             CAPSSA_LAUNCHED(c);
@@ -544,7 +742,13 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
                                                         empty_lf, k2bits, keys_a, spare_vals);
             CAPSSA_LAUNCHED(c);
         }
-        if (ns) {
+        if (ns && direct) {
+            // after gather_big: it reads the ranks this kernel rewrites
+            direct_small_kernel<<<grid_for(ns, 128), 128, 0, c.stream>>>(
+                G.small[cur], ns, sa, rank, a.lim, P, h, std::max<uint64_t>(h, kDirectCap), lf, G,
+                nxt);
+            CAPSSA_LAUNCHED(c);
+        } else if (ns) {
             sort_small_kernel<<<grid_for(ns, 128), 128, 0, c.stream>>>(
                 G.small[cur], ns, sa, key2, rank, lf, empty, G, nxt);
             CAPSSA_LAUNCHED(c);

@@ -209,10 +209,14 @@ static size_t pass_smem() {
            (size_t)kRadix * 4 * 2 + (size_t)kWarps * 4;
 }
 
+uint32_t *hist_buffer(Ctx &c) {
+    return (uint32_t *)ws_get(c, WS_RADIX_HIST, (kMaxPasses + 1) * kRadix * 4 + 64);
+}
+
 capssa_status sort_pairs(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *keys_b,
                          uint32_t *vals_b, uint32_t n, int begin_bit, int end_bit,
                          bool gen_vals, uint32_t val_base, bool *result_in_b,
-                         int *passes_run) {
+                         int *passes_run, bool hist_ready) {
     *result_in_b = false;
     if (passes_run) *passes_run = 0;
     if (n == 0) return CAPSSA_OK;
@@ -225,7 +229,7 @@ capssa_status sort_pairs(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *k
         }
         return CAPSSA_OK;
     }
-    uint32_t *counts = (uint32_t *)ws_get(c, WS_RADIX_HIST, (kMaxPasses + 1) * kRadix * 4 + 64);
+    uint32_t *counts = hist_buffer(c);
     uint32_t n_tiles = (n + kTile - 1) / kTile;
     unsigned long long *status = (unsigned long long *)ws_get(
         c, WS_RADIX_STATUS, (size_t)n_tiles * kRadix * sizeof(unsigned long long));
@@ -233,10 +237,12 @@ capssa_status sort_pairs(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *k
     uint32_t *offsets = counts + kMaxPasses * kRadix;  // 256 entries
     uint32_t *tile_counter = offsets + kRadix;
 
-    CAPSSA_CUDA(c, cudaMemsetAsync(counts, 0, kMaxPasses * kRadix * 4, c.stream));
-    hist_kernel<<<std::min<unsigned>(grid_for(n, kThreads), (unsigned)c.sm_count * 8), kThreads, 0,
-                  c.stream>>>(keys_a, n, begin_bit, n_passes, counts);
-    CAPSSA_LAUNCHED(c);
+    if (!hist_ready) {
+        CAPSSA_CUDA(c, cudaMemsetAsync(counts, 0, kMaxPasses * kRadix * 4, c.stream));
+        hist_kernel<<<std::min<unsigned>(grid_for(n, kThreads), (unsigned)c.sm_count * 8),
+                      kThreads, 0, c.stream>>>(keys_a, n, begin_bit, n_passes, counts);
+        CAPSSA_LAUNCHED(c);
+    }
     uint32_t *h = (uint32_t *)c.h_scratch;  // pinned, >= 8 * 256 * 4 bytes
     CAPSSA_CUDA(c, cudaMemcpyAsync(h, counts, n_passes * kRadix * 4, cudaMemcpyDeviceToHost,
                                    c.stream));

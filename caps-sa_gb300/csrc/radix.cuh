@@ -16,7 +16,12 @@ constexpr int kMaxPasses = 8;
 capssa_status sort_pairs(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *keys_b,
                          uint32_t *vals_b, uint32_t n, int begin_bit, int end_bit,
                          bool gen_vals, uint32_t val_base, bool *result_in_b,
-                         int *passes_run = nullptr);
+                         int *passes_run = nullptr, bool hist_ready = false);
+
+// The histogram buffer sort_pairs reads ([pass][256] u32 counts of the
+// digits at bits begin_bit + 8*pass).  A producer that already saw every key
+// can fill it and pass hist_ready = true to skip the histogram read.
+uint32_t *hist_buffer(Ctx &c);
 
 }  // namespace radix
 }  // namespace capssa
