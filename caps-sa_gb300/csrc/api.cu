@@ -429,7 +429,7 @@ capssa_status batched_common(Ctx &c, const ST *texts, const uint64_t *offsets, u
     uint32_t *va = (uint32_t *)ws_get(c, WS_VALS_A, n * 4);
     uint32_t *vb = (uint32_t *)ws_get(c, WS_VALS_B, n * 4);
     if (!ka || !kb || !va || !vb) return set_err(c, CAPSSA_ENOMEM, "batched split");
-    text_id_kernel<<<std::min<unsigned>(grid_for(n, 256), c.sm_count * 16), 256, 0, c.stream>>>(
+    text_id_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(
         d_sa, (uint32_t)n, (const uint64_t *)d_off, n_texts, ka, va);
     CAPSSA_LAUNCHED(c);
     int tb = 1;
@@ -460,7 +460,7 @@ __global__ void widen_u32_u64_kernel(const uint32_t *in, uint64_t *out, uint64_t
 }
 
 capssa_status widen_u32_u64(Ctx &c, const uint32_t *in, uint64_t *out, uint64_t n) {
-    widen_u32_u64_kernel<<<std::min<unsigned>(grid_for(n, 256), c.sm_count * 16), 256, 0,
+    widen_u32_u64_kernel<<<grid_for(n, 256), 256, 0,
                            c.stream>>>(in, out, n);
     CAPSSA_LAUNCHED(c);
     return CAPSSA_OK;
@@ -851,7 +851,7 @@ capssa_status capssa_pack_keys_u8(capssa_ctx *ctx, const uint8_t *text, uint64_t
     if ((s = stage_in(c, WS_CODES, pk->code, 256, 64, &d_code)) != CAPSSA_OK) return scope.finish(s);
     uint64_t *d_keys = (uint64_t *)ws_get(c, WS_OUT, m * 8 + 64);
     if (!d_keys) return scope.finish(set_err(c, CAPSSA_ENOMEM, "key output"));
-    pack_keys_kernel<<<std::min<unsigned>(grid_for(m, 256), c.sm_count * 16), 256, 0, c.stream>>>(
+    pack_keys_kernel<<<grid_for(m, 256), 256, 0, c.stream>>>(
         (const uint8_t *)d_text, n, (const uint8_t *)d_code, pk->bits, pk->k, pk->alphabet, L,
         (const uint64_t *)d_pos, m, d_keys);
     c.launches++;

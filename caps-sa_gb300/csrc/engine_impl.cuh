@@ -5,6 +5,8 @@
 #pragma once
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "engine.cuh"
@@ -16,7 +18,10 @@ namespace capssa {
 namespace {  // every kernel and helper is private to its engine_*.cu unit
 namespace eng {
 
-constexpr uint32_t kSmallMax = 16;  // tied groups up to this size: one thread each
+constexpr uint32_t kSmallMax = 32;    // tied groups up to this size: one warp each (pairs: one thread)
+constexpr uint32_t kMediumMax = 2048; // up to this size: one block, direct comparisons
+constexpr uint64_t kDirectCap = 256;   // symbols compared past the shared prefix (at least it)
+constexpr uint64_t kDirectMaxH = 4096; // deeper groups fall back to rank doubling
 constexpr int kKeyThreads = 256;
 constexpr int kKeyPer = 8;          // positions per thread in the key kernel
 constexpr int kKeyTile = kKeyThreads * kKeyPer;
@@ -25,13 +30,21 @@ struct BigGroup {
     uint32_t start, len, toff, pad;
 };
 
+// Work lists of one refinement round, by group size and depth.
+enum GroupList : int {
+    L_PAIR = 0,    // 2 members: one thread
+    L_TINY = 1,    // 3..8 members: one thread
+    L_SMALL = 2,   // 9..32 members: one warp
+    L_MEDIUM = 3,  // 33..kMediumMax members: one block
+    L_DEEP = 4,    // <= 32 members deeper than kDirectMaxH: rank doubling
+    kLists = 5     // larger groups: the radix (rank doubling) path
+};
+constexpr uint32_t kTinyMax = 8;
+
 // Device counters of the refinement rounds, double-buffered by round parity.
 struct Counters {
-    uint32_t n_small[2];
-    uint32_t pad0[2];
+    uint32_t n[kLists][2];
     unsigned long long big_packed[2];  // (ordinal << 40) | element total
-    unsigned long long refined;        // suffixes re-keyed (statistics)
-    unsigned long long pad1;
 };
 constexpr unsigned long long kBigOrdUnit = 1ull << 40;
 constexpr unsigned long long kBigTotMask = kBigOrdUnit - 1;
@@ -192,35 +205,124 @@ __device__ __forceinline__ uint32_t run_head(const uint64_t *__restrict__ keys, 
 }
 
 struct GroupLists {
-    uint2 *small[2];
+    uint4 *list[kLists][2];  // (start, len, depth, 0)
     BigGroup *big[2];
     Counters *ctr;
 };
 
-__device__ __forceinline__ void append_group(const GroupLists &G, int nxt, uint32_t start,
-                                             uint32_t len) {
-    if (len <= kSmallMax) {
-        uint32_t idx = atomicAdd(&G.ctr->n_small[nxt], 1u);
-        G.small[nxt][idx] = make_uint2(start, len);
-    } else {
-        unsigned long long old = atomicAdd(&G.ctr->big_packed[nxt], kBigOrdUnit | len);
-        uint32_t ord = (uint32_t)(old >> 40);
-        BigGroup g;
-        g.start = start;
-        g.len = len;
-        g.toff = (uint32_t)(old & kBigTotMask);
-        g.pad = 0;
-        G.big[nxt][ord] = g;
-    }
+// List of a still-tied group whose members agree on `depth` symbols
+// (kLists = the radix path).
+__device__ __forceinline__ int list_of(uint32_t len, uint64_t depth) {
+    if (len <= kSmallMax && depth > kDirectMaxH) return L_DEEP;
+    if (len == 2) return L_PAIR;
+    if (len <= kTinyMax) return L_TINY;
+    if (len <= kSmallMax) return L_SMALL;
+    if (len <= kMediumMax && depth <= kDirectMaxH) return L_MEDIUM;
+    return kLists;
 }
 
-// Ranks after the key sort; tied groups that need more symbols become the
-// first round's work (engine.cuh step 3 -> 4).
-__global__ void init_groups_kernel(const uint64_t *__restrict__ keys,
-                                   const uint32_t *__restrict__ sa, uint32_t n, int k,
-                                   uint64_t lmask, int lf, uint32_t *__restrict__ rank,
-                                   GroupLists G) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+__device__ __forceinline__ uint4 group_entry(uint32_t start, uint32_t len, uint64_t depth) {
+    return make_uint4(start, len, depth > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)depth, 0u);
+}
+
+__device__ __forceinline__ void append_big(const GroupLists &G, int nxt, uint32_t start,
+                                           uint32_t len) {
+    unsigned long long old = atomicAdd(&G.ctr->big_packed[nxt], kBigOrdUnit | len);
+    uint32_t ord = (uint32_t)(old >> 40);
+    BigGroup g;
+    g.start = start;
+    g.len = len;
+    g.toff = (uint32_t)(old & kBigTotMask);
+    g.pad = 0;
+    G.big[nxt][ord] = g;
+}
+
+// Slot in a list for every thread of the warp that calls this together
+// with the same `counter`: one atomic per warp instead of one per thread.
+// Same-address atomics serialise in L2 (a few ns each), so the heavy
+// producers use block_append below instead.
+__device__ __forceinline__ uint32_t warp_append(uint32_t *counter) {
+    const unsigned mask = __activemask();
+    const unsigned peers = __match_any_sync(mask, (unsigned long long)counter);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs((int)peers) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+}
+
+// Route a still-tied group to the next round's list (any thread, any time).
+__device__ __forceinline__ void append_group(const GroupLists &G, int nxt, uint32_t start,
+                                             uint32_t len, uint64_t depth) {
+    int l = list_of(len, depth);
+    if (l == kLists) {
+        append_big(G, nxt, start, len);
+        return;
+    }
+    uint32_t idx = warp_append(&G.ctr->n[l][nxt]);
+    G.list[l][nxt][idx] = group_entry(start, len, depth);
+}
+
+// Block-wide append: every thread of the block calls this at the same
+// point with at most one group (want); one global atomic per list per
+// block.  The block's entries of a list are contiguous.
+__device__ __forceinline__ void block_append(const GroupLists &G, int nxt, bool want,
+                                             uint32_t start, uint32_t len, uint64_t depth) {
+    __shared__ uint32_t s_cnt[kLists], s_base[kLists];
+    const int l = want ? list_of(len, depth) : -1;
+    if (threadIdx.x < kLists) s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+    uint32_t local = 0;
+    if (l >= 0 && l < kLists) local = atomicAdd(&s_cnt[l], 1u);
+    __syncthreads();
+    if (threadIdx.x < kLists && s_cnt[threadIdx.x])
+        s_base[threadIdx.x] = atomicAdd(&G.ctr->n[threadIdx.x][nxt], s_cnt[threadIdx.x]);
+    __syncthreads();
+    if (l >= 0 && l < kLists) G.list[l][nxt][s_base[l] + local] = group_entry(start, len, depth);
+    if (l == kLists) append_big(G, nxt, start, len);
+}
+
+// Exclusive block-wide prefix of one u32 per thread; returns the block total.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *excl) {
+    __shared__ uint32_t s_w[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < nw; w++) {
+        uint32_t t = s_w[w];
+        if (w < warp) before += t;
+        total += t;
+    }
+    __syncthreads();
+    *excl = before + x - v;
+    return total;
+}
+
+constexpr int kInitPer = 16;  // sorted keys per thread in init_groups_kernel
+
+// Group heads after the key sort, in SA order (hd[i] = first SA index of
+// i's group; equal heads == equal comparison so far); tied groups that need
+// more symbols become the first round's work (engine.cuh step 3 -> 4).
+// A block covers 256 * kInitPer keys and appends its groups with one
+// atomic per list.
+__global__ void __launch_bounds__(256)
+    init_groups_kernel(const uint64_t *__restrict__ keys, uint32_t n, int k, uint64_t lmask,
+                       int lf, uint32_t *__restrict__ hd, GroupLists G) {
+    const uint32_t base = blockIdx.x * (256u * kInitPer);
+    uint32_t cnt[kLists] = {0, 0, 0, 0, 0};
+    // pass 1: heads, and how many groups of each list this thread ends
+#pragma unroll 4
+    for (int j = 0; j < kInitPer; j++) {
+        const uint32_t i = base + j * 256 + threadIdx.x;
+        if (i >= n) break;
         uint64_t key = keys[i];
         bool head = (i == 0) || keys[i - 1] != key;
         uint32_t g = head ? i : run_head(keys, 0, i, key);
@@ -228,9 +330,50 @@ __global__ void init_groups_kernel(const uint64_t *__restrict__ keys,
         uint32_t lenf = (uint32_t)(key & lmask);
         int take = lf ? k - (int)lenf : (int)lenf;
         bool complete = take < k;
-        rank[sa[i]] = (complete && lf) ? i : g;
-        if (!complete && last && i > g) append_group(G, 0, g, i - g + 1);
+        hd[i] = (complete && lf) ? i : g;
+        if (!complete && last && i > g) {
+            int l = list_of(i - g + 1, (uint64_t)k);
+            if (l == kLists)
+                append_big(G, 0, g, i - g + 1);
+            else
+                cnt[l]++;
+        }
     }
+    __shared__ uint32_t s_base[kLists];
+    uint32_t off[kLists];
+#pragma unroll
+    for (int l = 0; l < kLists; l++) {
+        uint32_t total = block_excl_scan(cnt[l], &off[l]);
+        if (threadIdx.x == 0 && total) s_base[l] = atomicAdd(&G.ctr->n[l][0], total);
+    }
+    __syncthreads();
+    // pass 2: write the entries (keys are in L1/L2 from pass 1)
+#pragma unroll 4
+    for (int j = 0; j < kInitPer; j++) {
+        const uint32_t i = base + j * 256 + threadIdx.x;
+        if (i >= n) break;
+        uint64_t key = keys[i];
+        bool last = (i == n - 1) || keys[i + 1] != key;
+        if (!last) continue;
+        uint32_t lenf = (uint32_t)(key & lmask);
+        int take = lf ? k - (int)lenf : (int)lenf;
+        if (take < k) continue;
+        bool head = (i == 0) || keys[i - 1] != key;
+        if (head) continue;
+        uint32_t g = run_head(keys, 0, i, key);
+        int l = list_of(i - g + 1, (uint64_t)k);
+        if (l == kLists) continue;
+        G.list[l][0][s_base[l] + off[l]++] = group_entry(g, i - g + 1, (uint64_t)k);
+    }
+}
+
+// Position-ordered ranks from the SA-ordered heads; built once, the first
+// time a round needs rank doubling (rank[p + h] lookups).
+__global__ void rank_from_heads_kernel(const uint32_t *__restrict__ sa,
+                                       const uint32_t *__restrict__ hd, uint32_t n,
+                                       uint32_t *__restrict__ rank) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        rank[sa[i]] = hd[i];
 }
 
 // Sort key of suffix p for a round at depth h: the rank of p + h, or the
@@ -246,13 +389,13 @@ __device__ __forceinline__ uint64_t doubling_key(const DevLimits &L,
     return lf ? empty_lf : 0ull;
 }
 
-__global__ void gather_small_kernel(const uint2 *__restrict__ groups, uint32_t count,
+__global__ void gather_small_kernel(const uint4 *__restrict__ groups, uint32_t count,
                                     const uint32_t *__restrict__ sa,
                                     const uint32_t *__restrict__ rank, DevLimits L, uint64_t h,
                                     int lf, uint64_t empty_lf, uint64_t *__restrict__ key2) {
     for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < count;
          gi += gridDim.x * blockDim.x) {
-        uint2 g = groups[gi];
+        uint4 g = groups[gi];
         for (uint32_t t = 0; t < g.y; t++) {
             uint32_t i = g.x + t;
             key2[i] = doubling_key(L, rank, sa[i], h, lf, empty_lf);
@@ -277,13 +420,13 @@ __global__ void gather_big_kernel(const BigGroup *__restrict__ groups,
 
 // One thread sorts one small tied group by (key, position), writes the new
 // SA slice, the new ranks and the still-tied subgroups.
-__global__ void sort_small_kernel(const uint2 *__restrict__ groups, uint32_t count,
+__global__ void sort_small_kernel(const uint4 *__restrict__ groups, uint32_t count,
                                   uint32_t *__restrict__ sa, const uint64_t *__restrict__ key2,
-                                  uint32_t *__restrict__ rank, int lf, uint64_t empty,
-                                  GroupLists G, int nxt) {
+                                  uint32_t *__restrict__ hd, uint32_t *__restrict__ rank, int lf,
+                                  uint64_t empty, uint64_t next_depth, GroupLists G, int nxt) {
     for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < count;
          gi += gridDim.x * blockDim.x) {
-        uint2 g = groups[gi];
+        uint4 g = groups[gi];
         uint64_t kk[kSmallMax];
         uint32_t pp[kSmallMax];
         for (uint32_t t = 0; t < g.y; t++) {
@@ -304,10 +447,12 @@ __global__ void sort_small_kernel(const uint2 *__restrict__ groups, uint32_t cou
             while (e < g.y && kk[e] == kk[t]) e++;
             bool ended = kk[t] == empty;
             for (uint32_t u = t; u < e; u++) {
+                uint32_t r = (ended && lf) ? g.x + u : g.x + t;
                 sa[g.x + u] = pp[u];
-                rank[pp[u]] = (ended && lf) ? g.x + u : g.x + t;
+                hd[g.x + u] = r;
+                rank[pp[u]] = r;
             }
-            if (!ended && e - t >= 2) append_group(G, nxt, g.x + t, e - t);
+            if (!ended && e - t >= 2) append_group(G, nxt, g.x + t, e - t, next_depth);
             t = e;
         }
     }
@@ -320,9 +465,6 @@ __global__ void sort_small_kernel(const uint2 *__restrict__ groups, uint32_t cou
 // but on a bit-packed copy of the text: one 64-bit window holds 64/b
 // symbols (32 for DNA), so a suffix pair that differs within ~100 symbols
 // costs a few sector reads instead of several rank-doubling rounds.
-constexpr uint64_t kDirectCap = 256;     // symbols compared past the shared prefix (at least h)
-constexpr uint64_t kDirectMaxH = 4096;   // deeper groups fall back to rank doubling
-
 struct Packed {
     const uint64_t *w;  // MSB-first b-bit codes, zero padded
     int b;              // bits per symbol
@@ -340,6 +482,45 @@ __device__ __forceinline__ uint64_t window_at(const Packed &P, uint64_t p) {
     return v & P.mask;
 }
 
+// Sequential reader of b-bit symbols from the packed text: one 64-bit
+// load per window after the first.
+struct PackedStream {
+    const uint64_t *w;
+    uint64_t wi;
+    uint32_t sh;
+    uint64_t cur, nxt;
+    __device__ __forceinline__ void init(const Packed &P, uint64_t p) {
+        uint64_t s = p * (uint64_t)P.b;
+        w = P.w;
+        wi = s >> 6;
+        sh = (uint32_t)(s & 63);
+        cur = __ldg(w + wi);
+        nxt = __ldg(w + wi + 1);
+    }
+    __device__ __forceinline__ uint64_t get(uint64_t mask) const {
+        return (sh ? (cur << sh) | (nxt >> (64 - sh)) : cur) & mask;
+    }
+    __device__ __forceinline__ void advance(uint32_t bits) {
+        sh += bits;
+        if (sh >= 64) {
+            sh -= 64;
+            wi++;
+            cur = nxt;
+            nxt = __ldg(w + wi + 1);
+        }
+    }
+};
+
+// A[q] for a runtime q < 5 without spilling the array to local memory.
+__device__ __forceinline__ uint64_t pick5(const uint64_t (&A)[5], int q) {
+    uint64_t v = A[0];
+    v = q == 1 ? A[1] : v;
+    v = q == 2 ? A[2] : v;
+    v = q == 3 ? A[3] : v;
+    v = q == 4 ? A[4] : v;
+    return v;
+}
+
 // Order of suffixes a and b, known to agree on their first `o` symbols:
 // -1 / 1, 0 for a complete tie (ShorterFirst, equal limits), 2 when they
 // still agree `cap` symbols further (undecided).  Mirrors suffix_cmp_with
@@ -348,13 +529,62 @@ __device__ __forceinline__ int direct_cmp(const Packed &P, uint64_t a, uint64_t 
                                           uint64_t lb, uint64_t o, uint64_t cap, int lf) {
     const uint64_t lim = la < lb ? la : lb;
     const uint64_t end = lim < o + cap ? lim : o + cap;
-    for (uint64_t t = o; t < end; t += (uint64_t)P.spw) {
-        uint64_t va = window_at(P, a + t), vb = window_at(P, b + t);
-        uint64_t x = va ^ vb;
-        if (x) {
-            uint64_t d = (uint64_t)__clzll((long long)x) / (uint64_t)P.b;
-            if (t + d < end) return va < vb ? -1 : 1;
-            break;
+    // the first four windows of both suffixes are fetched with independent
+    // loads (one round trip covers the common short-LCP case), later ones
+    // stream one word per window
+    constexpr int kBurst = 4;
+    uint64_t t = o;
+    if (t < end) {
+        uint64_t sa0 = (a + t) * (uint64_t)P.b, sb0 = (b + t) * (uint64_t)P.b;
+        const uint64_t *wa = P.w + (sa0 >> 6), *wb = P.w + (sb0 >> 6);
+        const uint32_t sha = (uint32_t)(sa0 & 63), shb = (uint32_t)(sb0 & 63);
+        // words spanned by four windows: at most 5 (a window is <= 64 bits)
+        uint64_t A[kBurst + 1], B[kBurst + 1];
+        const uint32_t wbits = (uint32_t)(P.spw * P.b);
+        const int nwa = (int)((sha + (kBurst - 1) * wbits) >> 6) + 2;
+        const int nwb = (int)((shb + (kBurst - 1) * wbits) >> 6) + 2;
+#pragma unroll
+        for (int q = 0; q < kBurst + 1; q++) {
+            A[q] = q < nwa ? __ldg(wa + q) : 0ull;
+            B[q] = q < nwb ? __ldg(wb + q) : 0ull;
+        }
+        uint32_t bit_a = sha, bit_b = shb;
+#pragma unroll
+        for (int s = 0; s < kBurst; s++) {
+            if (t >= end) break;
+            int qa = (int)(bit_a >> 6), qb = (int)(bit_b >> 6);
+            uint32_t ra = bit_a & 63, rb = bit_b & 63;
+            uint64_t a0 = pick5(A, qa), a1 = pick5(A, qa + 1);
+            uint64_t b0 = pick5(B, qb), b1 = pick5(B, qb + 1);
+            uint64_t va = (ra ? (a0 << ra) | (a1 >> (64 - ra)) : a0) & P.mask;
+            uint64_t vb = (rb ? (b0 << rb) | (b1 >> (64 - rb)) : b0) & P.mask;
+            uint64_t x = va ^ vb;
+            if (x) {
+                uint64_t d = (uint64_t)__clzll((long long)x) / (uint64_t)P.b;
+                if (t + d < end) return va < vb ? -1 : 1;
+                t = end;
+                break;
+            }
+            bit_a += (uint32_t)(P.spw * P.b);
+            bit_b += (uint32_t)(P.spw * P.b);
+            t += (uint64_t)P.spw;
+        }
+    }
+    if (t < end) {
+        PackedStream sa_, sb_;
+        sa_.init(P, a + t);
+        sb_.init(P, b + t);
+        const uint32_t step_bits = (uint32_t)(P.spw * P.b);
+        for (; t < end; t += (uint64_t)P.spw) {
+            uint64_t va = sa_.get(P.mask), vb = sb_.get(P.mask);
+            uint64_t x = va ^ vb;
+            if (x) {
+                uint64_t d = (uint64_t)__clzll((long long)x) / (uint64_t)P.b;
+                if (t + d < end) return va < vb ? -1 : 1;
+                break;
+            }
+            sa_.advance(step_bits);
+            sb_.advance(step_bits);
         }
     }
     if (end < lim) return 2;
@@ -385,25 +615,66 @@ __global__ void pack_text_kernel(const S *__restrict__ text, uint64_t n, Coder<S
     }
 }
 
-// One thread sorts one small tied group (all members agree on h symbols)
-// by direct comparison, writes the SA slice and ranks, and passes groups
-// still undecided after max(h, kDirectCap) more symbols to the next round
-// (they then agree on >= 2h symbols, the next round's depth).
-__global__ void direct_small_kernel(const uint2 *__restrict__ groups, uint32_t count,
-                                    uint32_t *__restrict__ sa, uint32_t *__restrict__ rank,
-                                    DevLimits L, Packed P, uint64_t h, uint64_t cap, int lf,
-                                    GroupLists G, int nxt) {
+// Two-member tied groups (the bulk of the work on repeat-rich text): one
+// thread compares the pair directly past their shared depth g.z, writes
+// the SA slice and heads (and ranks once they exist), and passes a pair
+// still undecided after max(g.z, kDirectCap) more symbols to the next
+// round with that larger depth.
+__global__ void __launch_bounds__(256)
+    direct_pair_kernel(const uint4 *__restrict__ groups, uint32_t count, uint32_t *__restrict__ sa,
+                       uint32_t *__restrict__ hd, uint32_t *__restrict__ rank, DevLimits L,
+                       Packed P, int lf, GroupLists G, int nxt) {
+    const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+    bool again = false;
+    uint4 g = make_uint4(0, 0, 0, 0);
+    uint64_t cap = 0;
+    if (gi < count) {
+        g = groups[gi];
+        const uint64_t o = g.z;
+        cap = o > kDirectCap ? o : kDirectCap;
+        uint32_t p0 = sa[g.x], p1 = sa[g.x + 1];
+        uint64_t l0 = dev_lim_at(L, p0), l1 = dev_lim_at(L, p1);
+        int r = direct_cmp(P, p0, l0, p1, l1, o, cap, lf);
+        if (r == 1 || ((r == 0 || r == 2) && p0 > p1)) {
+            uint32_t t = p0;
+            p0 = p1;
+            p1 = t;
+            if (r == 1) r = -1;
+        }
+        sa[g.x] = p0;
+        sa[g.x + 1] = p1;
+        uint32_t h1 = (r == -1) ? g.x + 1 : g.x;
+        hd[g.x] = g.x;
+        hd[g.x + 1] = h1;
+        if (rank) {
+            rank[p0] = g.x;
+            rank[p1] = h1;
+        }
+        again = r == 2;
+    }
+    block_append(G, nxt, again, g.x, 2, (uint64_t)g.z + cap);
+}
+
+// Tied groups of 3..kTinyMax members: one thread sorts one group by
+// insertion with direct comparisons.
+__global__ void direct_tiny_kernel(const uint4 *__restrict__ groups, uint32_t count,
+                                   uint32_t *__restrict__ sa, uint32_t *__restrict__ hd,
+                                   uint32_t *__restrict__ rank, DevLimits L, Packed P, int lf,
+                                   GroupLists G, int nxt) {
     for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < count;
          gi += gridDim.x * blockDim.x) {
-        const uint2 g = groups[gi];
-        uint32_t pp[kSmallMax];
-        uint64_t ll[kSmallMax];
+        const uint4 g = groups[gi];
+        const uint64_t o = g.z;
+        const uint64_t cap = o > kDirectCap ? o : kDirectCap;
+        uint32_t pp[kTinyMax];
+        uint64_t ll[kTinyMax];
+        int8_t rr[kTinyMax];  // relation of member t to member t-1 once sorted
         for (uint32_t t = 0; t < g.y; t++) {
             uint32_t p = sa[g.x + t];
             uint64_t lp = dev_lim_at(L, p);
             int j = (int)t - 1;
             while (j >= 0) {
-                int r = direct_cmp(P, pp[j], ll[j], p, lp, h, cap, lf);
+                int r = direct_cmp(P, pp[j], ll[j], p, lp, o, cap, lf);
                 bool after = r == 1 || ((r == 0 || r == 2) && pp[j] > p);
                 if (!after) break;
                 pp[j + 1] = pp[j];
@@ -413,23 +684,193 @@ __global__ void direct_small_kernel(const uint2 *__restrict__ groups, uint32_t c
             pp[j + 1] = p;
             ll[j + 1] = lp;
         }
+        rr[0] = -1;
+        for (uint32_t t = 1; t < g.y; t++) {
+            int r = direct_cmp(P, pp[t - 1], ll[t - 1], pp[t], ll[t], o, cap, lf);
+            rr[t] = (int8_t)((r == 0 || r == 2) ? r : -1);
+        }
         uint32_t t = 0;
         while (t < g.y) {
             uint32_t e = t + 1;
-            int rel = -1;
-            while (e < g.y) {
-                int r = direct_cmp(P, pp[e - 1], ll[e - 1], pp[e], ll[e], h, cap, lf);
-                if (r != 0 && r != 2) break;
-                rel = r;
-                e++;
-            }
+            while (e < g.y && rr[e] != -1) e++;
             for (uint32_t u = t; u < e; u++) {
                 sa[g.x + u] = pp[u];
-                rank[pp[u]] = g.x + t;
+                hd[g.x + u] = g.x + t;
+                if (rank) rank[pp[u]] = g.x + t;
             }
-            if (rel == 2 && e - t >= 2) append_group(G, nxt, g.x + t, e - t);
+            if (e - t >= 2 && rr[e - 1] == 2) append_group(G, nxt, g.x + t, e - t, o + cap);
             t = e;
         }
+    }
+}
+
+// Tied groups of 9..32 members: one warp per group, one lane per member.
+// Every lane compares its member with all others (direct comparisons past
+// the shared depth, ties by position), so its rank in the group is a count
+// and the relation to its sorted predecessor is already known.  Groups
+// deeper than kDirectMaxH are left to rank doubling.
+__global__ void direct_warp_kernel(const uint4 *__restrict__ groups, uint32_t count,
+                                   uint32_t *__restrict__ sa, uint32_t *__restrict__ hd,
+                                   uint32_t *__restrict__ rank, DevLimits L, Packed P, int lf,
+                                   GroupLists G, int nxt) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t gi = warp; gi < count; gi += nwarps) {
+        const uint4 g = groups[gi];
+        const uint32_t len = g.y;
+        const uint64_t o = g.z;
+        const uint64_t cap = o > kDirectCap ? o : kDirectCap;
+        const bool mine = lane < len;
+        const uint32_t my_p = mine ? sa[g.x + lane] : 0u;
+        const uint64_t my_l = mine ? dev_lim_at(L, my_p) : 0ull;
+        uint32_t before = 0;
+        uint64_t rel = 0;  // 2 bits per other member j: code of cmp(j, mine)
+        for (uint32_t j = 0; j < len; j++) {
+            uint32_t pj = __shfl_sync(0xffffffffu, my_p, j);
+            uint64_t lj = __shfl_sync(0xffffffffu, my_l, j);
+            if (mine && j != lane) {
+                int r = direct_cmp(P, pj, lj, my_p, my_l, o, cap, lf);
+                bool j_first = r == -1 || ((r == 0 || r == 2) && pj < my_p);
+                before += j_first ? 1u : 0u;
+                rel |= (uint64_t)(r == -1 ? 0 : r == 1 ? 1 : r == 0 ? 2 : 3) << (2 * j);
+            }
+        }
+        // my sorted predecessor and whether I start a subgroup
+        bool start = true;
+        int my_rel = -1;
+        for (uint32_t j = 0; j < len; j++) {
+            uint32_t bj = __shfl_sync(0xffffffffu, before, j);
+            if (mine && before > 0 && bj + 1 == before) {
+                uint32_t code = (uint32_t)(rel >> (2 * j)) & 3u;
+                if (code >= 2) {
+                    start = false;
+                    my_rel = code == 2 ? 0 : 2;
+                }
+            }
+        }
+        unsigned starts = __reduce_or_sync(0xffffffffu, (mine && start) ? (1u << before) : 0u);
+        if (mine) {
+            uint32_t head = 31u - (uint32_t)__clz((int)(starts & (before == 31 ? 0xffffffffu
+                                                                     : ((2u << before) - 1u))));
+            sa[g.x + before] = my_p;
+            hd[g.x + before] = g.x + head;
+            if (rank) rank[my_p] = g.x + head;
+            bool last = before + 1 == len || ((starts >> (before + 1)) & 1u);
+            if (last && before > head && my_rel == 2)
+                append_group(G, nxt, g.x + head, before - head + 1, o + cap);
+        }
+    }
+}
+
+// One block sorts one medium tied group (17..kMediumMax members, all
+// agreeing on h symbols) with a bitonic network over direct comparisons,
+// then splits it into subgroups like direct_warp_kernel.
+constexpr int kMedThreads = 256;
+
+__global__ void __launch_bounds__(kMedThreads)
+    direct_medium_kernel(const uint4 *__restrict__ groups, uint32_t count,
+                         uint32_t *__restrict__ sa, uint32_t *__restrict__ hd,
+                         uint32_t *__restrict__ rank, DevLimits L, Packed P, int lf,
+                         GroupLists G, int nxt) {
+    __shared__ uint32_t spos[kMediumMax];
+    __shared__ uint64_t slim[kMediumMax];
+    __shared__ int8_t rel[kMediumMax];
+    __shared__ uint32_t shead[kMediumMax];
+    __shared__ uint32_t wmax[kMedThreads / 32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (uint32_t gi = blockIdx.x; gi < count; gi += gridDim.x) {
+        const uint4 g = groups[gi];
+        const uint32_t len = g.y;
+        const uint64_t h = g.z;
+        const uint64_t cap = h > kDirectCap ? h : kDirectCap;
+        uint32_t p2 = 1;
+        while (p2 < len) p2 <<= 1;
+        for (uint32_t t = tid; t < p2; t += kMedThreads) {
+            if (t < len) {
+                uint32_t p = sa[g.x + t];
+                spos[t] = p;
+                slim[t] = dev_lim_at(L, p);
+            } else {
+                spos[t] = 0xFFFFFFFFu;  // padding sorts last
+                slim[t] = 0;
+            }
+        }
+        __syncthreads();
+        for (uint32_t kk = 2; kk <= p2; kk <<= 1) {
+            for (uint32_t j = kk >> 1; j > 0; j >>= 1) {
+                for (uint32_t i = tid; i < p2; i += kMedThreads) {
+                    uint32_t ixj = i ^ j;
+                    if (ixj <= i) continue;
+                    uint32_t pa = spos[i], pb = spos[ixj];
+                    bool a_after;
+                    if (pa == 0xFFFFFFFFu || pb == 0xFFFFFFFFu) {
+                        a_after = pa == 0xFFFFFFFFu && pb != 0xFFFFFFFFu;
+                    } else {
+                        int r = direct_cmp(P, pa, slim[i], pb, slim[ixj], h, cap, lf);
+                        a_after = r == 1 || ((r == 0 || r == 2) && pa > pb);
+                    }
+                    bool up = (i & kk) == 0;
+                    if (up == a_after) {
+                        spos[i] = pb;
+                        spos[ixj] = pa;
+                        uint64_t tl = slim[i];
+                        slim[i] = slim[ixj];
+                        slim[ixj] = tl;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        // relation of each member to its predecessor: -1 starts a subgroup
+        for (uint32_t t = tid; t < len; t += kMedThreads) {
+            int r = -1;
+            if (t > 0) {
+                r = direct_cmp(P, spos[t - 1], slim[t - 1], spos[t], slim[t], h, cap, lf);
+                if (r != 0 && r != 2) r = -1;
+            }
+            rel[t] = (int8_t)r;
+        }
+        __syncthreads();
+        // subgroup head of every member: block max-scan of (start ? t : 0)
+        constexpr uint32_t kPer = kMediumMax / kMedThreads;
+        uint32_t base = tid * kPer, run = 0;
+        uint32_t loc[kPer];
+#pragma unroll
+        for (uint32_t q = 0; q < kPer; q++) {
+            uint32_t t = base + q;
+            if (t < len && rel[t] == -1) run = t;
+            loc[q] = run;
+        }
+        uint32_t x = run;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if ((int)lane >= o) x = max(x, y);
+        }
+        if (lane == 31) wmax[warp] = x;
+        __syncthreads();
+        uint32_t carry = 0;
+        for (uint32_t w = 0; w < warp; w++) carry = max(carry, wmax[w]);
+        uint32_t prev = __shfl_up_sync(0xffffffffu, x, 1);
+        if (lane == 0) prev = 0;
+        carry = max(carry, prev);
+#pragma unroll
+        for (uint32_t q = 0; q < kPer; q++) {
+            uint32_t t = base + q;
+            if (t < len) shead[t] = max(carry, loc[q]);
+        }
+        __syncthreads();
+        for (uint32_t t = tid; t < len; t += kMedThreads) {
+            uint32_t head = shead[t];
+            sa[g.x + t] = spos[t];
+            hd[g.x + t] = g.x + head;
+            if (rank) rank[spos[t]] = g.x + head;
+            bool last = t + 1 == len || rel[t + 1] == -1;
+            if (last && t > head && rel[t] == 2)
+                append_group(G, nxt, g.x + head, t - head + 1, h + cap);
+        }
+        __syncthreads();
     }
 }
 
@@ -439,8 +880,9 @@ __global__ void split_big_kernel(const uint64_t *__restrict__ tkeys,
                                  const uint32_t *__restrict__ tvals, uint32_t total,
                                  const BigGroup *__restrict__ groups, uint32_t n_groups,
                                  int k2bits,
-                                 uint32_t *__restrict__ sa, uint32_t *__restrict__ rank, int lf,
-                                 uint64_t empty, GroupLists G, int nxt) {
+                                 uint32_t *__restrict__ sa, uint32_t *__restrict__ hd,
+                                 uint32_t *__restrict__ rank, int lf,
+                                 uint64_t empty, uint64_t next_depth, GroupLists G, int nxt) {
     const uint64_t k2mask = (k2bits >= 64) ? ~0ull : ((1ull << k2bits) - 1);
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += gridDim.x * blockDim.x) {
@@ -453,11 +895,14 @@ __global__ void split_big_kernel(const uint64_t *__restrict__ tkeys,
         uint32_t p = tvals[t];
         sa[g.start + local] = p;
         bool head = (t == g.toff) || tkeys[t - 1] != key;
-        uint32_t hd = head ? t : run_head(tkeys, g.toff, t, key);
+        uint32_t h0 = head ? t : run_head(tkeys, g.toff, t, key);
         bool ended = (key & k2mask) == empty;
-        rank[p] = (ended && lf) ? g.start + local : g.start + (hd - g.toff);
+        uint32_t r = (ended && lf) ? g.start + local : g.start + (h0 - g.toff);
+        hd[g.start + local] = r;
+        rank[p] = r;
         bool last = (t == g.toff + g.len - 1) || tkeys[t + 1] != key;
-        if (!ended && last && t > hd) append_group(G, nxt, g.start + (hd - g.toff), t - hd + 1);
+        if (!ended && last && t > h0)
+            append_group(G, nxt, g.start + (h0 - g.toff), t - h0 + 1, next_depth);
     }
 }
 
@@ -588,6 +1033,14 @@ __global__ void subset_isa_key_kernel(const PT *__restrict__ pos, uint64_t m, ui
 
 // ---------------------------------------------------------------- host
 
+// CAPSSA_PROFILE in the environment turns on per-phase / per-round lines on
+// stderr, like the reference's CAPS_SA_PROFILE profile_log
+// (src/ext_mem.rs:42-51).
+inline bool profile_on() {
+    static const bool on = std::getenv("CAPSSA_PROFILE") != nullptr;
+    return on;
+}
+
 inline int bits_for(uint64_t v) {  // bits to represent 0..v
     int b = 0;
     while (b < 64 && (v >> b) != 0) b++;
@@ -673,7 +1126,7 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
     const uint64_t nwords = (n * (uint64_t)geo.b + 63) / 64 + 4;
     uint64_t *packed = (uint64_t *)ws_get(c, WS_PACKED, nwords * 8);
     if (!packed) return set_err(c, CAPSSA_ENOMEM, "packed text");
-    pack_text_kernel<S><<<std::min<unsigned>(grid_for(nwords, 256), c.sm_count * 16), 256, 0,
+    pack_text_kernel<S><<<grid_for(nwords, 256), 256, 0,
                           c.stream>>>(text, n, coder, geo.b, packed, nwords);
     CAPSSA_LAUNCHED(c);
     Packed P;
@@ -693,47 +1146,74 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
     uint32_t *sa = in_b ? vals_b : vals_a;
     uint32_t *spare_vals = in_b ? vals_a : vals_b;
 
-    // ---- 4. tied groups + rank doubling
-    size_t small_cap = (size_t)n / 2 + 2, big_cap = (size_t)n / (kSmallMax + 1) + 2;
+    // ---- 4. tied groups: direct comparison while shallow, rank doubling when deep
+    // list capacities from the smallest group each list can hold
+    const size_t cap_of[kLists] = {(size_t)n / 2 + 2, (size_t)n / 3 + 2, (size_t)n / 9 + 2,
+                                   (size_t)n / 33 + 2, (size_t)n / 2 + 2};
+    const size_t big_cap = (size_t)n / (kSmallMax + 1) + 2;
+    size_t list_bytes = 256 + big_cap * 16 * 2;
+    for (int l = 0; l < kLists; l++) list_bytes += cap_of[l] * 16 * 2;
     GroupLists G;
-    char *gl = (char *)ws_get(c, WS_GROUPS_A, small_cap * 8 * 2 + big_cap * 16 * 2 + 256);
-    if (!gl) return set_err(c, CAPSSA_ENOMEM, "group lists");
+    char *gl = (char *)ws_get(c, WS_GROUPS_A, list_bytes);
+    uint32_t *hd = (uint32_t *)ws_get(c, WS_GROUPS_B, (size_t)n * 4 + 64);
+    if (!gl || !hd) return set_err(c, CAPSSA_ENOMEM, "group lists");
     G.ctr = (Counters *)gl;
-    G.small[0] = (uint2 *)(gl + 256);
-    G.small[1] = G.small[0] + small_cap;
-    G.big[0] = (BigGroup *)(G.small[1] + small_cap);
+    uint4 *cursor = (uint4 *)(gl + 256);
+    for (int l = 0; l < kLists; l++)
+        for (int q = 0; q < 2; q++) {
+            G.list[l][q] = cursor;
+            cursor += cap_of[l];
+        }
+    G.big[0] = (BigGroup *)cursor;
     G.big[1] = G.big[0] + big_cap;
+    uint64_t h = (uint64_t)geo.k;
     CAPSSA_CUDA(c, cudaMemsetAsync(G.ctr, 0, sizeof(Counters), c.stream));
-    init_groups_kernel<<<std::min<unsigned>(grid_for(n, 256), c.sm_count * 16), 256, 0,
-                         c.stream>>>(skeys, sa, nn, geo.k, (1ull << geo.lbits) - 1, lf, rank, G);
+    init_groups_kernel<<<grid_for(n, 256 * kInitPer), 256, 0, c.stream>>>(
+        skeys, nn, geo.k, (1ull << geo.lbits) - 1, lf, hd, G);
     CAPSSA_LAUNCHED(c);
 
     const int k2bits = bits_for(n + 1);
     const uint64_t empty_lf = (1ull << k2bits) - 1;  // above every rank
     const uint64_t empty = lf ? empty_lf : 0ull;
-    uint64_t h = (uint64_t)geo.k;
+    bool ranks_ready = false;
     int cur = 0;
     Counters *hc = (Counters *)c.h_scratch;
     for (;;) {
         CAPSSA_CUDA(c, cudaMemcpyAsync(hc, G.ctr, sizeof(Counters), cudaMemcpyDeviceToHost,
                                        c.stream));
         CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
-        const uint32_t ns = hc->n_small[cur];
+        uint32_t cnt[kLists];
+        uint32_t any = 0;
+        for (int l = 0; l < kLists; l++) any |= (cnt[l] = hc->n[l][cur]);
         const uint32_t nb = (uint32_t)(hc->big_packed[cur] >> 40);
         const uint32_t big_total = (uint32_t)(hc->big_packed[cur] & kBigTotMask);
-        if (ns == 0 && nb == 0) break;
+        if (profile_on())
+            std::fprintf(stderr,
+                         "capssa profile  round %u depth %llu: pairs %u tiny %u small %u "
+                         "medium %u deep %u big %u (%u suffixes)\n",
+                         c.stats.refine_rounds + 1, (unsigned long long)h, cnt[L_PAIR],
+                         cnt[L_TINY], cnt[L_SMALL], cnt[L_MEDIUM], cnt[L_DEEP], nb, big_total);
+        if (!any && !nb) break;
         if (c.stats.refine_rounds >= 70)
             return set_err(c, CAPSSA_EINVAL, "rank doubling did not converge");
         c.stats.refine_rounds++;
         const int nxt = cur ^ 1;
-        CAPSSA_CUDA(c, cudaMemsetAsync(&G.ctr->n_small[nxt], 0, 4, c.stream));
+        // rank doubling reads position-ordered ranks; they are built from the
+        // SA-ordered heads the first time a round needs them
+        if ((nb || cnt[L_DEEP]) && !ranks_ready) {
+            rank_from_heads_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa, hd, nn, rank);
+            CAPSSA_LAUNCHED(c);
+            ranks_ready = true;
+        }
+        uint32_t *rk = ranks_ready ? rank : nullptr;
+        for (int l = 0; l < kLists; l++)
+            CAPSSA_CUDA(c, cudaMemsetAsync(&G.ctr->n[l][nxt], 0, 4, c.stream));
         CAPSSA_CUDA(c, cudaMemsetAsync(&G.ctr->big_packed[nxt], 0, 8, c.stream));
-        // gathers read ranks of the previous depth; all of them finish
-        // before any rank of this round is rewritten (stream order)
-        const bool direct = h <= kDirectMaxH;
-        if (ns && !direct) {
-            gather_small_kernel<<<grid_for(ns, 128), 128, 0, c.stream>>>(
-                G.small[cur], ns, sa, rank, a.lim, h, lf, empty_lf, key2);
+        // gathers read ranks of the previous depth; they finish before any
+        // rank of this round is rewritten (stream order)
+        if (cnt[L_DEEP]) {
+            gather_small_kernel<<<grid_for(cnt[L_DEEP], 128), 128, 0, c.stream>>>(
+                G.list[L_DEEP][cur], cnt[L_DEEP], sa, rank, a.lim, h, lf, empty_lf, key2);
             CAPSSA_LAUNCHED(c);
         }
         const int ord_bits = nb > 1 ? bits_for(nb - 1) : 1;
@@ -742,15 +1222,30 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
                                                         empty_lf, k2bits, keys_a, spare_vals);
             CAPSSA_LAUNCHED(c);
         }
-        if (ns && direct) {
-            // after gather_big: it reads the ranks this kernel rewrites
-            direct_small_kernel<<<grid_for(ns, 128), 128, 0, c.stream>>>(
-                G.small[cur], ns, sa, rank, a.lim, P, h, std::max<uint64_t>(h, kDirectCap), lf, G,
-                nxt);
+        if (cnt[L_PAIR]) {
+            direct_pair_kernel<<<grid_for(cnt[L_PAIR], 256), 256, 0, c.stream>>>(
+                G.list[L_PAIR][cur], cnt[L_PAIR], sa, hd, rk, a.lim, P, lf, G, nxt);
             CAPSSA_LAUNCHED(c);
-        } else if (ns) {
-            sort_small_kernel<<<grid_for(ns, 128), 128, 0, c.stream>>>(
-                G.small[cur], ns, sa, key2, rank, lf, empty, G, nxt);
+        }
+        if (cnt[L_TINY]) {
+            direct_tiny_kernel<<<grid_for(cnt[L_TINY], 128), 128, 0, c.stream>>>(
+                G.list[L_TINY][cur], cnt[L_TINY], sa, hd, rk, a.lim, P, lf, G, nxt);
+            CAPSSA_LAUNCHED(c);
+        }
+        if (cnt[L_SMALL]) {
+            direct_warp_kernel<<<grid_for((uint64_t)cnt[L_SMALL] * 32, 128), 128, 0, c.stream>>>(
+                G.list[L_SMALL][cur], cnt[L_SMALL], sa, hd, rk, a.lim, P, lf, G, nxt);
+            CAPSSA_LAUNCHED(c);
+        }
+        if (cnt[L_DEEP]) {
+            sort_small_kernel<<<grid_for(cnt[L_DEEP], 128), 128, 0, c.stream>>>(
+                G.list[L_DEEP][cur], cnt[L_DEEP], sa, key2, hd, rank, lf, empty, 2 * h, G, nxt);
+            CAPSSA_LAUNCHED(c);
+        }
+        if (cnt[L_MEDIUM]) {
+            direct_medium_kernel<<<std::min<unsigned>(cnt[L_MEDIUM], c.sm_count * 8), kMedThreads,
+                                   0, c.stream>>>(G.list[L_MEDIUM][cur], cnt[L_MEDIUM], sa, hd,
+                                                  rk, a.lim, P, lf, G, nxt);
             CAPSSA_LAUNCHED(c);
         }
         if (nb) {
@@ -761,9 +1256,9 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
             if (s != CAPSSA_OK) return s;
             const uint64_t *tk = tb ? keys_b : keys_a;
             const uint32_t *tv = tb ? tv_b : spare_vals;
-            split_big_kernel<<<std::min<unsigned>(grid_for(big_total, 256), c.sm_count * 16), 256,
-                               0, c.stream>>>(tk, tv, big_total, G.big[cur], nb, k2bits, sa, rank, lf,
-                                              empty, G, nxt);
+            split_big_kernel<<<grid_for(big_total, 256), 256, 0, c.stream>>>(
+                tk, tv, big_total, G.big[cur], nb, k2bits, sa, hd, rank, lf, empty, 2 * h, G,
+                nxt);
             CAPSSA_LAUNCHED(c);
         }
         c.stats.refined_suffixes += big_total;
@@ -786,6 +1281,12 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
         pass_ms += ms;
     }
     c.stats.sort_pass_ms = pass_ms;
+    if (profile_on())
+        std::fprintf(stderr,
+                     "capssa profile  n %llu k %d b %d: keys %.3f ms, sort %.3f ms (%d passes, "
+                     "%.3f ms in pass kernels), refine %.3f ms (%u rounds)\n",
+                     (unsigned long long)n, geo.k, geo.b, t01, t12, passes, pass_ms, t23,
+                     c.stats.refine_rounds);
     *sa_out = sa;
     return CAPSSA_OK;
 }
@@ -805,7 +1306,7 @@ capssa_status bounded_pass(Ctx &c, const EngineArgs &a, uint32_t *sa) {
     uint32_t *v2 = v1 + n;
     capssa_status s = ctx_run_flags(c, a.text, a.sym_bytes, a.lim, a.max_ctx, sa, n, flags);
     if (s != CAPSSA_OK) return s;
-    unsigned g = std::min<unsigned>(grid_for(n, 256), c.sm_count * 16);
+    unsigned g = grid_for(n, 256);
     run_head_value_kernel<<<g, 256, 0, c.stream>>>(flags, nn, hv, inr);
     CAPSSA_LAUNCHED(c);
     uint32_t last_in = 0;
@@ -830,7 +1331,7 @@ capssa_status bounded_pass(Ctx &c, const EngineArgs &a, uint32_t *sa) {
     const uint32_t *sv = tb ? v2 : v1;
     uint64_t *rk = tb ? k1 : k2;
     uint32_t *rv = (uint32_t *)hv;  // run ids were consumed by the compaction
-    unsigned gt = std::min<unsigned>(grid_for(total, 256), c.sm_count * 16);
+    unsigned gt = grid_for(total, 256);
     run_swap_kernel<<<gt, 256, 0, c.stream>>>(sk, sv, total, rk, rv);
     CAPSSA_LAUNCHED(c);
     uint64_t *rk2 = tb ? k2 : k1;
@@ -884,7 +1385,7 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
         if (a.out_bytes == 4) {
             CAPSSA_CUDA(c, cudaMemcpyAsync(a.out_sa, sa, n * 4, cudaMemcpyDeviceToDevice, c.stream));
         } else {
-            widen_kernel<uint64_t><<<std::min<unsigned>(grid_for(n, 256), c.sm_count * 16), 256, 0,
+            widen_kernel<uint64_t><<<grid_for(n, 256), 256, 0,
                                      c.stream>>>(sa, (uint64_t *)a.out_sa, n);
             CAPSSA_LAUNCHED(c);
         }
@@ -903,13 +1404,13 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
     if (!isa || !sk_a || !sk_b || !sv) return set_err(c, CAPSSA_ENOMEM, "subset workspace");
     uint32_t *sv_b = sv + m;
     if (n > 0) {
-        isa_kernel<<<std::min<unsigned>(grid_for(n, 256), c.sm_count * 16), 256, 0, c.stream>>>(
+        isa_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(
             sa, (uint32_t)n, isa);
         CAPSSA_LAUNCHED(c);
     }
     int *bad = c.d_flags + 1;
     CAPSSA_CUDA(c, cudaMemsetAsync(bad, 0, 4, c.stream));
-    unsigned gm = std::min<unsigned>(grid_for(m, 256), c.sm_count * 16);
+    unsigned gm = grid_for(m, 256);
     if (a.pos_bytes == 4)
         subset_isa_key_kernel<uint32_t><<<gm, 256, 0, c.stream>>>(
             (const uint32_t *)a.positions, m, n, isa, lf, sk_a, sv, bad);

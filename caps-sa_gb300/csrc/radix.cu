@@ -23,9 +23,16 @@
 namespace capssa {
 namespace radix {
 
+#ifndef CAPSSA_RADIX_ITEMS
+#define CAPSSA_RADIX_ITEMS 16
+#endif
+#ifndef CAPSSA_RADIX_MIN_BLOCKS
+#define CAPSSA_RADIX_MIN_BLOCKS 3
+#endif
+
 constexpr int kRadix = 256;
 constexpr int kThreads = 256;
-constexpr int kItems = 16;
+constexpr int kItems = CAPSSA_RADIX_ITEMS;
 constexpr int kTile = kThreads * kItems;
 constexpr int kWarps = kThreads / 32;
 constexpr unsigned long long kFlagA = 1ull << 62;
@@ -65,7 +72,7 @@ __device__ __forceinline__ void st_volatile_u64(unsigned long long *p, unsigned 
 }
 
 template <bool GEN_VALS>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
     onesweep_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
                     uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out,
                     uint32_t n, int shift, const uint32_t *__restrict__ digit_offsets,

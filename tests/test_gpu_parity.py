@@ -131,6 +131,24 @@ def test_long_runs_and_periodic(ctx):
     check_against_oracle(ctx, np.concatenate([np.tile(unit, 500), [200]]).astype(np.uint8))
 
 
+@pytest.mark.parametrize("copies,unit", [(3, 9000), (40, 3000), (2500, 40), (5000, 3)])
+def test_repeat_structures(ctx, copies, unit):
+    """Tied groups of every kind: few members with LCPs past the direct
+    comparison depth (rank doubling), medium groups (block sort), and
+    groups of thousands (radix path)."""
+    rng = np.random.default_rng(copies)
+    u = rng.integers(0, 4, unit).astype(np.uint8)
+    parts = []
+    for _ in range(copies):
+        parts.append(u)
+        parts.append(rng.integers(0, 4, int(rng.integers(1, 50))).astype(np.uint8))
+    t = np.concatenate(parts)
+    check_against_oracle(ctx, t)
+    ends = np.cumsum([len(x) for x in parts])
+    check_against_oracle(ctx, t, ends=ends)
+    check_against_oracle(ctx, t, ends=ends, longer_first=True)
+
+
 @pytest.mark.parametrize("index", [np.uint32, np.uint64])
 def test_random_segmented_and_star(ctx, index):
     rng = np.random.default_rng(0x5E6)
