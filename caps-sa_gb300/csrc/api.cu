@@ -83,7 +83,9 @@ KeyGeom key_geom(int b, uint64_t n) {
         if (k * g.b + lbits_of(k) <= 64) kmax = k;
     int logn = 0;
     while (logn < 64 && (n >> logn) > 1) logn++;
-    int kmin = (logn + g.b - 1) / g.b + 4;
+    // log_sigma(n) + 3 symbols: random suffixes then tie in about n / (2 sigma^3)
+    // pairs, which the refinement resolves cheaply
+    int kmin = (logn + g.b - 1) / g.b + 3;
     int k = kmax;
     if (kmin < kmax) {
         int passes = (kmin * g.b + lbits_of(kmin) + 7) / 8;
@@ -293,6 +295,7 @@ capssa_status build_common(Ctx &c, const ST *text, uint64_t n, const void *posit
     a.out_sa = d_out;
     a.out_bytes = out_bytes;
     a.out_lcp = d_lcp;
+    a.bucket_front = opts && opts->partition != CAPSSA_PARTITION_AUTO ? 1 : 0;
     if (positions && m == 0) return CAPSSA_OK;
     s = engine_build(c, a);
     if (s != CAPSSA_OK) return s;

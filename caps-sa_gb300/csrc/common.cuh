@@ -71,6 +71,36 @@ __device__ __forceinline__ uint64_t dev_lim_at(const DevLimits &L, uint64_t p) {
     return L.n - p;
 }
 
+// Lanes of the (full) warp whose BITS-bit label equals this lane's: one
+// ballot per label bit, intersected.  Cheaper than the general 32-bit
+// match instruction for the 8-bit digits of the radix passes.
+template <int BITS>
+__device__ __forceinline__ unsigned warp_match_bits(uint32_t label) {
+    unsigned m = 0xffffffffu;
+#pragma unroll
+    for (int b = 0; b < BITS; b++) {
+        const bool set = (label >> b) & 1u;
+        const unsigned bal = __ballot_sync(0xffffffffu, set);
+        m &= set ? bal : ~bal;
+    }
+    return m;
+}
+
+// Stable warp multisplit of one item per lane into per-warp digit counters
+// `wh` (shared memory): returns this lane's rank among the items of its
+// digit that the warp has seen so far (earlier calls, then lower lanes).
+// The highest lane of each digit adds the digit's count with one shared
+// atomic; a warp's atomics on one address complete in issue order, so
+// successive calls need no barrier between them and pipeline.
+__device__ __forceinline__ uint32_t warp_rank_digit(uint32_t *wh, uint32_t d, unsigned peers,
+                                                    unsigned lt_mask, int lane) {
+    const int leader = 31 - __clz(peers);
+    uint32_t old = 0;
+    if (lane == leader) old = atomicAdd(&wh[d], (uint32_t)__popc(peers));
+    old = __shfl_sync(0xffffffffu, old, leader);
+    return old + __popc(peers & lt_mask);
+}
+
 // Grow-only device buffers owned by a context, addressed by slot.
 enum Slot : int {
     WS_TEXT = 0, WS_ENDS, WS_DIR, WS_POS_IN, WS_OUT, WS_OUT2,

@@ -40,6 +40,7 @@ struct EngineArgs {
     void *out_sa;          // device, m (or n) entries of out_bytes
     int out_bytes;         // 4 or 8
     void *out_lcp;         // device or nullptr
+    int bucket_front;      // 1: bucket the keys by their top 16 bits first (bucket.cuh)
 };
 
 // Runs the whole sort; all buffers are device buffers.

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "engine.cuh"
+#include "bucket.cuh"
 #include "lcp.cuh"
 #include "radix.cuh"
 #include "scan.cuh"
@@ -125,8 +126,8 @@ struct Coder {
 template <typename S>
 __global__ void __launch_bounds__(kKeyThreads)
     key_kernel(const S *__restrict__ text, uint64_t n, DevLimits L, Coder<S> coder, int b,
-               int k, int lbits, int lf, int n_passes, uint64_t *__restrict__ keys,
-               uint32_t *__restrict__ counts) {
+               int k, int lbits, int lf, int hist_shift, int n_passes,
+               uint64_t *__restrict__ keys, uint32_t *__restrict__ counts) {
     __shared__ uint32_t codes[kKeyTile + 64];
     __shared__ uint32_t hist[8 * 256];
     const uint64_t t0 = (uint64_t)blockIdx.x * kKeyTile;
@@ -162,7 +163,7 @@ __global__ void __launch_bounds__(kKeyThreads)
                 }
                 key = (content << lbits) | (uint64_t)(lf ? k - take : take);
                 for (int ps = 0; ps < n_passes; ps++)
-                    atomicAdd(&hist[ps * 256 + ((key >> (8 * ps)) & 255)], 1u);
+                    atomicAdd(&hist[ps * 256 + ((key >> (hist_shift + 8 * ps)) & 255)], 1u);
             }
             out[e] = key;
             w = ((w << b) | codes[i0 + e + k]) & kmask;
@@ -210,6 +211,18 @@ struct GroupLists {
     Counters *ctr;
 };
 
+// The lists are kernel parameters: indexing them with a runtime value would
+// copy the whole struct to local memory in every thread, so pick by select.
+__device__ __forceinline__ uint4 *list_ptr(const GroupLists &G, int l, int q) {
+    uint4 *r = nullptr;
+#pragma unroll
+    for (int i = 0; i < kLists; i++) r = l == i ? (q ? G.list[i][1] : G.list[i][0]) : r;
+    return r;
+}
+__device__ __forceinline__ BigGroup *big_ptr(const GroupLists &G, int q) {
+    return q ? G.big[1] : G.big[0];
+}
+
 // List of a still-tied group whose members agree on `depth` symbols
 // (kLists = the radix path).
 __device__ __forceinline__ int list_of(uint32_t len, uint64_t depth) {
@@ -234,7 +247,7 @@ __device__ __forceinline__ void append_big(const GroupLists &G, int nxt, uint32_
     g.len = len;
     g.toff = (uint32_t)(old & kBigTotMask);
     g.pad = 0;
-    G.big[nxt][ord] = g;
+    big_ptr(G, nxt)[ord] = g;
 }
 
 // Slot in a list for every thread of the warp that calls this together
@@ -261,7 +274,7 @@ __device__ __forceinline__ void append_group(const GroupLists &G, int nxt, uint3
         return;
     }
     uint32_t idx = warp_append(&G.ctr->n[l][nxt]);
-    G.list[l][nxt][idx] = group_entry(start, len, depth);
+    list_ptr(G, l, nxt)[idx] = group_entry(start, len, depth);
 }
 
 // Block-wide append: every thread of the block calls this at the same
@@ -279,7 +292,7 @@ __device__ __forceinline__ void block_append(const GroupLists &G, int nxt, bool 
     if (threadIdx.x < kLists && s_cnt[threadIdx.x])
         s_base[threadIdx.x] = atomicAdd(&G.ctr->n[threadIdx.x][nxt], s_cnt[threadIdx.x]);
     __syncthreads();
-    if (l >= 0 && l < kLists) G.list[l][nxt][s_base[l] + local] = group_entry(start, len, depth);
+    if (l >= 0 && l < kLists) list_ptr(G, l, nxt)[s_base[l] + local] = group_entry(start, len, depth);
     if (l == kLists) append_big(G, nxt, start, len);
 }
 
@@ -335,8 +348,8 @@ __global__ void __launch_bounds__(256)
             int l = list_of(i - g + 1, (uint64_t)k);
             if (l == kLists)
                 append_big(G, 0, g, i - g + 1);
-            else
-                cnt[l]++;
+#pragma unroll
+            for (int q = 0; q < kLists; q++) cnt[q] += l == q ? 1u : 0u;
         }
     }
     __shared__ uint32_t s_base[kLists];
@@ -363,7 +376,11 @@ __global__ void __launch_bounds__(256)
         uint32_t g = run_head(keys, 0, i, key);
         int l = list_of(i - g + 1, (uint64_t)k);
         if (l == kLists) continue;
-        G.list[l][0][s_base[l] + off[l]++] = group_entry(g, i - g + 1, (uint64_t)k);
+        uint32_t slot = 0;
+#pragma unroll
+        for (int q = 0; q < kLists; q++)
+            if (l == q) slot = s_base[q] + off[q]++;
+        list_ptr(G, l, 0)[slot] = group_entry(g, i - g + 1, (uint64_t)k);
     }
 }
 
@@ -655,51 +672,135 @@ __global__ void __launch_bounds__(256)
     block_append(G, nxt, again, g.x, 2, (uint64_t)g.z + cap);
 }
 
-// Tied groups of 3..kTinyMax members: one thread sorts one group by
-// insertion with direct comparisons.
-__global__ void direct_tiny_kernel(const uint4 *__restrict__ groups, uint32_t count,
-                                   uint32_t *__restrict__ sa, uint32_t *__restrict__ hd,
-                                   uint32_t *__restrict__ rank, DevLimits L, Packed P, int lf,
-                                   GroupLists G, int nxt) {
+// Two consecutive windows of the packed text starting at symbol p (three
+// word loads).
+__device__ __forceinline__ void windows2_at(const Packed &P, uint64_t p, uint64_t &w0,
+                                            uint64_t &w1) {
+    const uint64_t s = p * (uint64_t)P.b;
+    const uint64_t *q = P.w + (s >> 6);
+    const uint32_t sh = (uint32_t)(s & 63);
+    const uint64_t x0 = __ldg(q), x1 = __ldg(q + 1), x2 = __ldg(q + 2);
+    w0 = (sh ? (x0 << sh) | (x1 >> (64 - sh)) : x0) & P.mask;
+    const uint32_t s2 = sh + (uint32_t)(P.spw * P.b);  // < 128
+    const uint64_t y0 = s2 >= 64 ? x1 : x0, y1 = s2 >= 64 ? x2 : x1;
+    const uint32_t r2 = s2 & 63;
+    w1 = (r2 ? (y0 << r2) | (y1 >> (64 - r2)) : y0) & P.mask;
+}
+
+// Index of member pair (i, j), i < j < kTinyMax, in 0..27.
+__host__ __device__ constexpr int tiny_pair(int i, int j) {
+    return i * (2 * (int)kTinyMax - 1 - i) / 2 + (j - i - 1);
+}
+
+// Tied groups of 3..kTinyMax members: one thread per group.  The first two
+// windows of every member past the shared depth are loaded up front (all
+// independent loads, one round trip for the group) and every member pair is
+// compared on those registers; only pairs that agree on both windows go on
+// with direct_cmp.  A member's place is the count of members before it, so
+// nothing moves until the final scatter.  Counts (4 bits per member) and
+// pair relations (2 bits per pair) live in packed registers.
+__global__ void __launch_bounds__(128)
+    direct_tiny_kernel(const uint4 *__restrict__ groups, uint32_t count,
+                       uint32_t *__restrict__ sa, uint32_t *__restrict__ hd,
+                       uint32_t *__restrict__ rank, DevLimits L, Packed P, int lf, GroupLists G,
+                       int nxt) {
+    constexpr int M = (int)kTinyMax;
     for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < count;
          gi += gridDim.x * blockDim.x) {
         const uint4 g = groups[gi];
+        const int len = (int)g.y;
         const uint64_t o = g.z;
         const uint64_t cap = o > kDirectCap ? o : kDirectCap;
-        uint32_t pp[kTinyMax];
-        uint64_t ll[kTinyMax];
-        int8_t rr[kTinyMax];  // relation of member t to member t-1 once sorted
-        for (uint32_t t = 0; t < g.y; t++) {
-            uint32_t p = sa[g.x + t];
-            uint64_t lp = dev_lim_at(L, p);
-            int j = (int)t - 1;
-            while (j >= 0) {
-                int r = direct_cmp(P, pp[j], ll[j], p, lp, o, cap, lf);
-                bool after = r == 1 || ((r == 0 || r == 2) && pp[j] > p);
-                if (!after) break;
-                pp[j + 1] = pp[j];
-                ll[j + 1] = ll[j];
-                j--;
+        const uint64_t span = 2 * (uint64_t)P.spw;  // symbols held by the two windows
+        uint32_t pp[M];
+        uint64_t ll[M], w0[M], w1[M];
+        bool full[M];  // limit past both windows: the register compare is exact
+#pragma unroll
+        for (int t = 0; t < M; t++) {
+            if (t < len) {
+                pp[t] = sa[g.x + t];
+                ll[t] = dev_lim_at(L, pp[t]);
+                full[t] = ll[t] >= o + span;
+                windows2_at(P, (uint64_t)pp[t] + o, w0[t], w1[t]);
             }
-            pp[j + 1] = p;
-            ll[j + 1] = lp;
         }
-        rr[0] = -1;
-        for (uint32_t t = 1; t < g.y; t++) {
-            int r = direct_cmp(P, pp[t - 1], ll[t - 1], pp[t], ll[t], o, cap, lf);
-            rr[t] = (int8_t)((r == 0 || r == 2) ? r : -1);
-        }
-        uint32_t t = 0;
-        while (t < g.y) {
-            uint32_t e = t + 1;
-            while (e < g.y && rr[e] != -1) e++;
-            for (uint32_t u = t; u < e; u++) {
-                sa[g.x + u] = pp[u];
-                hd[g.x + u] = g.x + t;
-                if (rank) rank[pp[u]] = g.x + t;
+        uint32_t bef = 0;      // 4 bits per member: members placed before it
+        uint64_t rel = 0;      // 2 bits per pair: 0 ordered, 1 complete tie, 2 undecided
+        uint32_t slow = 0;     // pairs left for direct_cmp
+#pragma unroll
+        for (int i = 0; i < M; i++) {
+#pragma unroll
+            for (int j = i + 1; j < M; j++) {
+                if (j < len) {
+                    const int pi = tiny_pair(i, j);
+                    if (full[i] && full[j] && (w0[i] != w0[j] || w1[i] != w1[j])) {
+                        const bool i_first = w0[i] != w0[j] ? w0[i] < w0[j] : w1[i] < w1[j];
+                        bef += i_first ? (1u << (4 * j)) : (1u << (4 * i));
+                    } else {
+                        slow |= 1u << pi;
+                    }
+                }
             }
-            if (e - t >= 2 && rr[e - 1] == 2) append_group(G, nxt, g.x + t, e - t, o + cap);
-            t = e;
+        }
+        // pairs that agree on both windows (or end inside them): one
+        // direct comparison each, members re-read from the slice
+        while (slow) {
+            const int pi = __ffs((int)slow) - 1;
+            slow &= slow - 1;
+            int i = 0, rem = pi;
+            while (rem >= M - 1 - i) {
+                rem -= M - 1 - i;
+                i++;
+            }
+            const int j = i + 1 + rem;
+            const uint32_t a = sa[g.x + i], b = sa[g.x + j];
+            const uint64_t la = dev_lim_at(L, a), lb = dev_lim_at(L, b);
+            const bool past = la >= o + span && lb >= o + span;
+            const int r = past ? direct_cmp(P, a, la, b, lb, o + span, cap - span, lf)
+                               : direct_cmp(P, a, la, b, lb, o, cap, lf);
+            const bool i_first = r == -1 || ((r == 0 || r == 2) && a < b);
+            bef += i_first ? (1u << (4 * j)) : (1u << (4 * i));
+            const uint64_t code = r == 0 ? 1u : (r == 2 ? 2u : 0u);
+            rel |= code << (2 * pi);
+        }
+        // slot of each member, relation of each slot to the one before it
+        uint32_t starts = 1u;  // bit s: slot s begins a tie run
+        uint32_t undec = 0u;   // bit s: slot s is undecided against slot s-1
+#pragma unroll
+        for (int t = 0; t < M; t++) {
+            if (t < len) {
+                const uint32_t st = (bef >> (4 * t)) & 15u;
+                uint32_t code = 0;
+#pragma unroll
+                for (int u = 0; u < M; u++) {
+                    if (u < len && u != t && ((bef >> (4 * u)) & 15u) + 1u == st) {
+                        const int pi = u < t ? tiny_pair(u, t) : tiny_pair(t, u);
+                        code = (uint32_t)(rel >> (2 * pi)) & 3u;
+                    }
+                }
+                if (st > 0 && code == 0) starts |= 1u << st;
+                if (st > 0 && code == 2) undec |= 1u << st;
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < M; t++) {
+            if (t < len) {
+                const uint32_t st = (bef >> (4 * t)) & 15u;
+                const uint32_t head = 31u - (uint32_t)__clz((int)(starts & ((2u << st) - 1u)));
+                sa[g.x + st] = pp[t];
+                hd[g.x + st] = g.x + head;
+                if (rank) rank[pp[t]] = g.x + head;
+            }
+        }
+        // runs still undecided go to the next round, past this round's cap
+#pragma unroll
+        for (int s2 = 1; s2 < M; s2++) {
+            if (s2 < len) {
+                const bool run_end = s2 == len - 1 || ((starts >> (s2 + 1)) & 1u);
+                const uint32_t head = 31u - (uint32_t)__clz((int)(starts & ((2u << s2) - 1u)));
+                if (run_end && head < (uint32_t)s2 && ((undec >> s2) & 1u))
+                    append_group(G, nxt, g.x + head, (uint32_t)s2 - head + 1, o + cap);
+            }
         }
     }
 }
@@ -1115,19 +1216,25 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
     if (!keys_a || !keys_b || !vals_a || !vals_b || !rank || !key2)
         return set_err(c, CAPSSA_ENOMEM, "suffix-sort workspace");
     Coder<S> coder{table, minv};
-    const int key_passes = (geo.total + 7) / 8;
+    // large texts: two passes on the top 16 key bits make 65536 buckets
+    // contiguous, then each bucket is sorted on chip (bucket.cuh)
+    const int bb = bucket::kBucketBits;
+    const bool msd = a.bucket_front && n >= (1ull << 22) && geo.total > bb + 8;
+    const int hist_shift = msd ? geo.total - bb : 0;
+    const int key_passes = msd ? (bb + 7) / 8 : (geo.total + 7) / 8;
     uint32_t *counts = radix::hist_buffer(c);
     if (!counts) return set_err(c, CAPSSA_ENOMEM, "radix histograms");
     CAPSSA_CUDA(c, cudaMemsetAsync(counts, 0, radix::kMaxPasses * 256 * 4, c.stream));
     key_kernel<S><<<grid_for(n, kKeyTile), kKeyThreads, 0, c.stream>>>(
-        text, n, a.lim, coder, geo.b, geo.k, geo.lbits, lf, key_passes, keys_a, counts);
+        text, n, a.lim, coder, geo.b, geo.k, geo.lbits, lf, hist_shift, key_passes, keys_a,
+        counts);
     CAPSSA_LAUNCHED(c);
     // bit-packed copy of the text for direct comparisons of small groups
     const uint64_t nwords = (n * (uint64_t)geo.b + 63) / 64 + 4;
     uint64_t *packed = (uint64_t *)ws_get(c, WS_PACKED, nwords * 8);
     if (!packed) return set_err(c, CAPSSA_ENOMEM, "packed text");
-    pack_text_kernel<S><<<grid_for(nwords, 256), 256, 0,
-                          c.stream>>>(text, n, coder, geo.b, packed, nwords);
+    pack_text_kernel<S><<<grid_for(nwords, 256), 256, 0, c.stream>>>(text, n, coder, geo.b,
+                                                                     packed, nwords);
     CAPSSA_LAUNCHED(c);
     Packed P;
     P.w = packed;
@@ -1137,10 +1244,30 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
     cudaEventRecord(c.pev[1], c.stream);
     bool in_b = false;
     int passes = 0;
-    capssa_status s = radix::sort_pairs(c, keys_a, vals_a, keys_b, vals_b, nn, 0, geo.total, true,
-                                        0, &in_b, &passes, /*hist_ready=*/true);
+    capssa_status s = radix::sort_pairs(c, keys_a, vals_a, keys_b, vals_b, nn, hist_shift,
+                                        geo.total, true, 0, &in_b, &passes, /*hist_ready=*/true);
     if (s != CAPSSA_OK) return s;
     c.stats.sort_passes = (uint32_t)passes;
+    if (msd) {
+        uint64_t *xk = in_b ? keys_b : keys_a, *yk = in_b ? keys_a : keys_b;
+        uint32_t *xv = in_b ? vals_b : vals_a, *yv = in_b ? vals_a : vals_b;
+        uint32_t *d_start = (uint32_t *)ws_get(c, WS_MISC2, (bucket::kBuckets + 1) * 4 + 64);
+        if (!d_start) return set_err(c, CAPSSA_ENOMEM, "bucket starts");
+        s = bucket::bucket_starts(c, xk, nn, hist_shift, d_start);
+        if (s != CAPSSA_OK) return s;
+        std::vector<uint32_t> h_start(bucket::kBuckets + 1);
+        CAPSSA_CUDA(c, cudaMemcpyAsync(h_start.data(), d_start, h_start.size() * 4,
+                                       cudaMemcpyDeviceToHost, c.stream));
+        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+        uint32_t maxb = 0;
+        for (uint32_t b = 0; b < bucket::kBuckets; b++) maxb = std::max(maxb, h_start[b + 1] - h_start[b]);
+        c.stats.partitions = bucket::kBuckets;
+        c.stats.max_partition = maxb;
+        s = bucket::sort_buckets(c, xk, xv, yk, yv, (uint64_t *)key2, rank, nn, d_start,
+                                 h_start.data(), hist_shift);
+        if (s != CAPSSA_OK) return s;
+        in_b = xk == keys_b;
+    }
     cudaEventRecord(c.pev[2], c.stream);
     const uint64_t *skeys = in_b ? keys_b : keys_a;
     uint32_t *sa = in_b ? vals_b : vals_a;

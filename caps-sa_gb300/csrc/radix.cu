@@ -7,7 +7,7 @@
 // Per 8-bit digit pass one kernel reads each (key, value) once and writes it
 // once (24 B per pair of HBM traffic): a block claims the next tile through
 // an atomic counter, ranks its keys by digit in shared memory with a
-// warp-level multisplit (__match_any_sync), publishes its per-digit counts
+// stable warp-level multisplit (ballots + shared atomics), publishes its per-digit counts
 // and learns its global offsets by decoupled look-back over the tiles
 // before it, then writes each digit run contiguously.  One up-front kernel
 // builds the histograms of every pass from a single read of the keys;
@@ -29,6 +29,9 @@ namespace radix {
 #ifndef CAPSSA_RADIX_MIN_BLOCKS
 #define CAPSSA_RADIX_MIN_BLOCKS 3
 #endif
+#ifndef CAPSSA_RADIX_RANK
+#define CAPSSA_RADIX_RANK 2  // 0: load/store ranking, 1: match + atomics, 2: ballots + atomics
+#endif
 
 constexpr int kRadix = 256;
 constexpr int kThreads = 256;
@@ -48,15 +51,20 @@ __global__ void __launch_bounds__(kThreads) hist_kernel(const uint64_t *__restri
     __shared__ uint32_t sh[kMaxPasses * kRadix];
     for (int i = threadIdx.x; i < kMaxPasses * kRadix; i += blockDim.x) sh[i] = 0;
     __syncthreads();
+    // whole warps step together (the digit match needs all 32 lanes);
+    // lanes past the end carry label 256, which no counter has
     const uint32_t lane = threadIdx.x & 31;
-    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n;
-         idx += gridDim.x * blockDim.x) {
-        uint64_t k = keys[idx];
-        unsigned act = __activemask();
+    const uint64_t gwarp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t wstride = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t base = gwarp * 32; base < n; base += wstride * 32) {
+        const uint64_t idx = base + lane;
+        const bool valid = idx < n;
+        const uint64_t k = valid ? keys[idx] : 0;
         for (int p = 0; p < n_passes; p++) {
-            uint32_t d = (uint32_t)(k >> (begin_bit + 8 * p)) & 255u;
-            unsigned peers = __match_any_sync(act, d);
-            if (lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&sh[p * kRadix + d], __popc(peers));
+            const uint32_t d = valid ? (uint32_t)(k >> (begin_bit + 8 * p)) & 255u : 256u;
+            const unsigned peers = warp_match_bits<9>(d);
+            if (valid && lane == (uint32_t)(31 - __clz(peers)))
+                atomicAdd(&sh[p * kRadix + d], (uint32_t)__popc(peers));
         }
     }
     __syncthreads();
@@ -116,6 +124,7 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
     // warp-level multisplit: rank of each item among equal digits of this warp
     uint32_t *wh = s_whist + warp * kRadix;
     const unsigned lt_mask = (1u << lane) - 1u;
+#if CAPSSA_RADIX_RANK == 0
 #pragma unroll
     for (int j = 0; j < kItems; j++) {
         unsigned peers = __match_any_sync(0xffffffffu, d[j]);
@@ -126,6 +135,17 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
         __syncwarp();
         r[j] = cnt + pre;
     }
+#else
+#pragma unroll
+    for (int j = 0; j < kItems; j++) {
+#if CAPSSA_RADIX_RANK == 1
+        const unsigned peers = __match_any_sync(0xffffffffu, d[j]);
+#else
+        const unsigned peers = warp_match_bits<8>(d[j]);
+#endif
+        r[j] = warp_rank_digit(wh, d[j], peers, lt_mask, lane);
+    }
+#endif
     __syncthreads();
 
     // thread `tid` owns digit `tid`: warp prefixes, tile total, look-back

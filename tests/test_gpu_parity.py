@@ -53,10 +53,13 @@ def limits_pair(n, ends=None, longer_first=False):
 
 
 def check_against_oracle(ctx, text, positions=None, ends=None, longer_first=False,
-                         max_ctx=orc.UNBOUNDED, index=np.uint32):
+                         max_ctx=orc.UNBOUNDED, index=np.uint32, partition=None):
     n = len(text)
     lp, lo = limits_pair(n, ends, longer_first)
-    opts = capssa.Opts(max_context=max_ctx)
+    if partition is None:
+        opts = capssa.Opts(max_context=max_ctx)
+    else:
+        opts = capssa.ExtMemOpts(max_context=max_ctx, partition=partition)
     if positions is None:
         got = ctx.build_in_memory(text, lp, opts, index=index)
         want = orc.build_in_memory(text, None, lo, max_ctx, index=index)
@@ -390,3 +393,40 @@ def test_repeat_text_bit_exact(ctx):
     from capssa import workloads
     t = workloads.dna_with_repeats(1 << 19, seed=2)
     assert np.array_equal(ctx.build_in_memory(t), orc.build_in_memory(t))
+
+
+def _bucket_text(n, seed):
+    """Repeat DNA with one long run and one periodic stretch, so that some
+    16-bit key buckets exceed what one block sorts on chip."""
+    from capssa import workloads
+    t = workloads.dna_with_repeats(n, seed=seed).copy()
+    t[1000:61000] = 0
+    t[200000:230000] = np.tile(np.array([1, 3, 2], dtype=t.dtype), 10000)
+    return t
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.uint32])
+def test_bucket_front_end_plain(ctx, dtype):
+    """Texts of 2^22+ symbols take the bucket front end (two global passes on
+    the top 16 key bits, on-chip sort of each bucket, oversize buckets by the
+    global sort): bit-exact against the oracle."""
+    t = _bucket_text((1 << 22) + 12345, seed=11).astype(dtype)
+    opts = capssa.ExtMemOpts(partition=capssa.Partition.SPLITTERS)
+    got = ctx.build_in_memory(t, None, opts)
+    assert np.array_equal(got, orc.build_in_memory(t))
+
+
+def test_bucket_front_end_star_segments(ctx):
+    t = _bucket_text((1 << 22) + 777, seed=12).astype(np.uint8)
+    rng = np.random.default_rng(5)
+    ends = np.unique(np.concatenate([rng.integers(1, len(t), 300), [len(t)]])).tolist()
+    check_against_oracle(ctx, t, ends=ends, longer_first=True,
+                         partition=capssa.Partition.SPLITTERS)
+
+
+def test_bucket_front_end_text_alphabet(ctx):
+    """A 5-bit alphabet (key of 11 symbols + length field) through the front end."""
+    rng = np.random.default_rng(13)
+    t = rng.integers(0, 20, (1 << 22) + 99).astype(np.uint8)
+    t[5000:25000] = 7
+    check_against_oracle(ctx, t, partition=capssa.Partition.SPLITTERS)
