@@ -139,18 +139,19 @@ def hbm_peak():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(n):
-    """DRAM bytes per radix-pass launch from the committed ncu summary,
-    scaled by pairs per launch (traffic grows linearly with pairs)."""
-    p = os.path.join(ROOT, "profiles", "radix_onesweep_pass.txt")
+def profiled_traffic(n, item_bytes):
+    """DRAM bytes per radix-pass launch from the committed ncu summary for
+    this record width, scaled by records per launch (traffic grows linearly
+    with the records)."""
+    p = os.path.join(ROOT, "profiles", "radix_onesweep_pass_%dB.txt" % item_bytes)
     try:
         vals = {}
         for ln in open(p):
             if ":" in ln:
                 k, v = ln.split(":", 1)
                 vals[k.strip()] = v.strip().split()[0]
-        per_pair = float(vals["dram_bytes_per_pair"])
-        return per_pair * n
+        per_rec = float(vals["dram_bytes_per_record"])
+        return per_rec * n
     except Exception:
         return None
 
@@ -255,6 +256,7 @@ def run_ours(args):
     ev1 = torch.cuda.Event(enable_timing=True)
     launches = 0
     pass_ms, passes, phase = [], [], {"keys_ms": 0, "sort_ms": 0, "refine_ms": 0, "finish_ms": 0}
+    item_bytes = 12
     rounds = 0
     ev0.record(stream)
     for _ in range(args.steps):
@@ -263,6 +265,7 @@ def run_ours(args):
         launches += st["kernel_launches"]
         pass_ms.append(st["sort_pass_ms"])
         passes.append(st["sort_passes"])
+        item_bytes = st["sort_item_bytes"] or 12
         rounds = st["refine_rounds"]
         for k in phase:
             phase[k] += st[k] / args.steps
@@ -279,14 +282,16 @@ def run_ours(args):
     ms_per_step = elapsed_ms / args.steps
     value = n * ws * args.steps / (elapsed_ms / 1e3) / 1e6
 
-    # roofline of the dominant kernel: one onesweep radix pass over n
-    # (key u64, value u32) pairs reads and writes 12 B per pair
+    # roofline of the dominant kernel: one onesweep radix pass over the n
+    # suffix records reads and writes each record once (8 B when the
+    # position is packed below the key, else a u64 key + a u32 position)
     peak, peak_kind = hbm_peak()
     avg_pass_ms = sum(pass_ms) / max(1, sum(passes))
-    alg_bytes = 24.0 * n
+    alg_bytes = 2.0 * item_bytes * n
     achieved = alg_bytes / (avg_pass_ms / 1e3) / 1e9
-    traffic = profiled_traffic(n)
-    roofline = {"kernel": "radix onesweep pass (initial 64-bit key sort)", "bound": "hbm",
+    traffic = profiled_traffic(n, item_bytes)
+    roofline = {"kernel": "radix onesweep pass (initial sort of the %d-byte suffix records)"
+                % item_bytes, "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_kind": peak_kind, "traffic": traffic,
                 "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_pass_ms,

@@ -99,7 +99,7 @@ class _Stats(C.Structure):
                 ("h2d_ms", C.c_double), ("d2h_ms", C.c_double), ("h2d_bytes", C.c_uint64),
                 ("d2h_bytes", C.c_uint64), ("keys_ms", C.c_double), ("sort_ms", C.c_double),
                 ("refine_ms", C.c_double), ("finish_ms", C.c_double),
-                ("sort_passes", C.c_uint32), ("reserved0", C.c_uint32),
+                ("sort_passes", C.c_uint32), ("sort_item_bytes", C.c_uint32),
                 ("sort_pass_ms", C.c_double)]
 
 

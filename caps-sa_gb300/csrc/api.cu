@@ -70,9 +70,30 @@ capssa_status check_dev_flags(Ctx &c) {
 // log_{2^b}(n) + 4 rarely separate random suffixes, so the key keeps only
 // as many symbols as fit in the radix passes that this minimum needs:
 // DNA at n = 2^28 keeps 21 symbols in 6 passes instead of 29 in 8.
-KeyGeom key_geom(int b, uint64_t n) {
+KeyGeom key_geom(int b, uint64_t n, bool plain) {
     KeyGeom g{};
     g.b = b < 1 ? 1 : b;
+    int logn = 0;
+    while (logn < 64 && (n >> logn) > 1) logn++;
+    // log_sigma(n) + 3 symbols: random suffixes then tie in about n / (2 sigma^3)
+    // pairs, which the refinement resolves cheaply
+    const int kmin = (logn + g.b - 1) / g.b + 3;
+    // the position rides below the key when both fit in 64 bits; a plain
+    // text then marks its k-1 short suffixes with one flag bit instead of a
+    // length field (they are refined from depth 0)
+    int vbits = 1;
+    while (vbits < 32 && (1ull << vbits) < n) vbits++;
+    if (plain && kmin * g.b + 1 + vbits <= 64) {
+        const int passes = (kmin * g.b + 1 + 7) / 8;
+        int k = kmin;
+        while ((k + 1) * g.b + 1 <= 8 * passes && (k + 1) * g.b + 1 + vbits <= 64) k++;
+        g.k = k;
+        g.lbits = 1;
+        g.flag_len = 1;
+        g.total = k * g.b + 1;
+        g.vbits = vbits;
+        return g;
+    }
     auto lbits_of = [](int k) {
         int lb = 0;
         while ((1 << lb) <= k) lb++;  // bits of 0..k
@@ -81,11 +102,6 @@ KeyGeom key_geom(int b, uint64_t n) {
     int kmax = 1;
     for (int k = 1; k * g.b <= 63; k++)
         if (k * g.b + lbits_of(k) <= 64) kmax = k;
-    int logn = 0;
-    while (logn < 64 && (n >> logn) > 1) logn++;
-    // log_sigma(n) + 3 symbols: random suffixes then tie in about n / (2 sigma^3)
-    // pairs, which the refinement resolves cheaply
-    int kmin = (logn + g.b - 1) / g.b + 3;
     int k = kmax;
     if (kmin < kmax) {
         int passes = (kmin * g.b + lbits_of(kmin) + 7) / 8;
@@ -95,6 +111,8 @@ KeyGeom key_geom(int b, uint64_t n) {
     g.k = k;
     g.lbits = lbits_of(k);
     g.total = g.k * g.b + g.lbits;
+    g.flag_len = 0;
+    g.vbits = g.total + vbits <= 64 ? vbits : 0;
     return g;
 }
 

@@ -58,11 +58,14 @@ inline capssa_status engine_build(Ctx &c, const EngineArgs &a) {
 
 // Key geometry for b bits per symbol and n symbols (api.cu).
 struct KeyGeom {
-    int b;       // bits per symbol
-    int k;       // symbols per key
-    int lbits;   // bits of the length field
-    int total;   // k*b + lbits
+    int b;         // bits per symbol
+    int k;         // symbols per key
+    int lbits;     // bits of the length field
+    int total;     // k*b + lbits
+    int flag_len;  // 1: the length field is one "ended early" flag (plain texts)
+    int vbits;     // > 0: the position is packed below the key in vbits bits
 };
-KeyGeom key_geom(int b, uint64_t n);
+// plain: the limits are PlainText's (only the last k-1 suffixes end early).
+KeyGeom key_geom(int b, uint64_t n, bool plain);
 
 }  // namespace capssa

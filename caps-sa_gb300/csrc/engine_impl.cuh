@@ -122,12 +122,13 @@ struct Coder {
 // no separate histogram read of the keys).  Each thread owns kKeyPer
 // consecutive positions: the k-symbol window slides one symbol per
 // position over codes staged in shared memory, and only suffixes that end
-// inside the window (lim < k) are masked and padded.
+// inside the window (lim < k) are masked and padded.  With vbits > 0 the
+// position is packed below the key (one 64-bit word per suffix).
 template <typename S>
 __global__ void __launch_bounds__(kKeyThreads)
     key_kernel(const S *__restrict__ text, uint64_t n, DevLimits L, Coder<S> coder, int b,
-               int k, int lbits, int lf, int hist_shift, int n_passes,
-               uint64_t *__restrict__ keys, uint32_t *__restrict__ counts) {
+               int k, int lbits, int flag_len, int vbits, int lf, int hist_shift,
+               int n_passes, uint64_t *__restrict__ keys, uint32_t *__restrict__ counts) {
     __shared__ uint32_t codes[kKeyTile + 64];
     __shared__ uint32_t hist[8 * 256];
     const uint64_t t0 = (uint64_t)blockIdx.x * kKeyTile;
@@ -161,9 +162,15 @@ __global__ void __launch_bounds__(kKeyThreads)
                     uint64_t lowmask = (1ull << low) - 1;
                     content = lf ? (w | lowmask) : (w & ~lowmask);
                 }
-                key = (content << lbits) | (uint64_t)(lf ? k - take : take);
+                // length field: symbols taken (ShorterFirst) or missing
+                // (LongerFirst); or one flag that orders an early end first
+                // (ShorterFirst) or last (LongerFirst) among equal contents
+                const uint64_t field = flag_len ? (uint64_t)((take == k) != (lf != 0))
+                                                : (uint64_t)(lf ? k - take : take);
+                key = (content << lbits) | field;
                 for (int ps = 0; ps < n_passes; ps++)
                     atomicAdd(&hist[ps * 256 + ((key >> (hist_shift + 8 * ps)) & 255)], 1u);
+                if (vbits) key = (key << vbits) | p;
             }
             out[e] = key;
             w = ((w << b) | codes[i0 + e + k]) & kmask;
@@ -188,16 +195,16 @@ __global__ void __launch_bounds__(kKeyThreads)
 
 // First index of the run of `key` that contains sorted index i.
 __device__ __forceinline__ uint32_t run_head(const uint64_t *__restrict__ keys, uint32_t lo,
-                                             uint32_t i, uint64_t key) {
+                                             uint32_t i, uint64_t key, int vshift = 0) {
     uint32_t j = i;
     uint32_t stop = (i - lo > 32) ? i - 32 : lo;
-    while (j > stop && keys[j - 1] == key) j--;
+    while (j > stop && (keys[j - 1] >> vshift) == key) j--;
     if (j > stop || j == lo) return j;
     // long run: binary search for the first index in [lo, j) equal to key
     uint32_t a = lo, z = j;
     while (a < z) {
         uint32_t mid = a + ((z - a) >> 1);
-        if (keys[mid] < key)
+        if ((keys[mid] >> vshift) < key)
             a = mid + 1;
         else
             z = mid;
@@ -328,24 +335,43 @@ constexpr int kInitPer = 16;  // sorted keys per thread in init_groups_kernel
 // atomic per list.
 __global__ void __launch_bounds__(256)
     init_groups_kernel(const uint64_t *__restrict__ keys, uint32_t n, int k, uint64_t lmask,
-                       int lf, uint32_t *__restrict__ hd, GroupLists G) {
+                       int lf, int flag_len, int vshift, uint32_t *__restrict__ hd,
+                       uint32_t *__restrict__ sa_out, GroupLists G) {
     const uint32_t base = blockIdx.x * (256u * kInitPer);
+    const uint64_t vmask = (1ull << vshift) - 1;
+    // tie state of a key: complete (equal through both ends: nothing to
+    // refine), and the depth its group's members are known to agree on
+    // (0 for the early-ended suffixes of a flagged plain text)
+    auto state = [&](uint64_t key, bool &complete, uint64_t &depth) {
+        const uint32_t lenf = (uint32_t)(key & lmask);
+        if (flag_len) {
+            complete = false;
+            depth = lenf == (lf ? 0u : 1u) ? (uint64_t)k : 0ull;
+        } else {
+            const int take = lf ? k - (int)lenf : (int)lenf;
+            complete = take < k;
+            depth = (uint64_t)k;
+        }
+    };
     uint32_t cnt[kLists] = {0, 0, 0, 0, 0};
-    // pass 1: heads, and how many groups of each list this thread ends
+    // pass 1: heads (and positions), and how many groups of each list this
+    // thread ends
 #pragma unroll 4
     for (int j = 0; j < kInitPer; j++) {
         const uint32_t i = base + j * 256 + threadIdx.x;
         if (i >= n) break;
-        uint64_t key = keys[i];
-        bool head = (i == 0) || keys[i - 1] != key;
-        uint32_t g = head ? i : run_head(keys, 0, i, key);
-        bool last = (i == n - 1) || keys[i + 1] != key;
-        uint32_t lenf = (uint32_t)(key & lmask);
-        int take = lf ? k - (int)lenf : (int)lenf;
-        bool complete = take < k;
+        const uint64_t item = keys[i];
+        const uint64_t key = item >> vshift;
+        if (sa_out) sa_out[i] = (uint32_t)(item & vmask);
+        bool head = (i == 0) || (keys[i - 1] >> vshift) != key;
+        uint32_t g = head ? i : run_head(keys, 0, i, key, vshift);
+        bool last = (i == n - 1) || (keys[i + 1] >> vshift) != key;
+        bool complete;
+        uint64_t depth;
+        state(key, complete, depth);
         hd[i] = (complete && lf) ? i : g;
         if (!complete && last && i > g) {
-            int l = list_of(i - g + 1, (uint64_t)k);
+            int l = list_of(i - g + 1, depth);
             if (l == kLists)
                 append_big(G, 0, g, i - g + 1);
 #pragma unroll
@@ -365,22 +391,23 @@ __global__ void __launch_bounds__(256)
     for (int j = 0; j < kInitPer; j++) {
         const uint32_t i = base + j * 256 + threadIdx.x;
         if (i >= n) break;
-        uint64_t key = keys[i];
-        bool last = (i == n - 1) || keys[i + 1] != key;
+        const uint64_t key = keys[i] >> vshift;
+        bool last = (i == n - 1) || (keys[i + 1] >> vshift) != key;
         if (!last) continue;
-        uint32_t lenf = (uint32_t)(key & lmask);
-        int take = lf ? k - (int)lenf : (int)lenf;
-        if (take < k) continue;
-        bool head = (i == 0) || keys[i - 1] != key;
+        bool complete;
+        uint64_t depth;
+        state(key, complete, depth);
+        if (complete) continue;
+        bool head = (i == 0) || (keys[i - 1] >> vshift) != key;
         if (head) continue;
-        uint32_t g = run_head(keys, 0, i, key);
-        int l = list_of(i - g + 1, (uint64_t)k);
+        uint32_t g = run_head(keys, 0, i, key, vshift);
+        int l = list_of(i - g + 1, depth);
         if (l == kLists) continue;
         uint32_t slot = 0;
 #pragma unroll
         for (int q = 0; q < kLists; q++)
             if (l == q) slot = s_base[q] + off[q]++;
-        list_ptr(G, l, 0)[slot] = group_entry(g, i - g + 1, (uint64_t)k);
+        list_ptr(G, l, 0)[slot] = group_entry(g, i - g + 1, depth);
     }
 }
 
@@ -1201,7 +1228,7 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
         sigma_span = (uint64_t)h_mm[1] - h_mm[0] + 1;
     }
     const int b = bits_for(sigma_span > 1 ? sigma_span - 1 : 1);
-    const KeyGeom geo = key_geom(b, n);
+    const KeyGeom geo = key_geom(b, n, !a.lim.segmented);
     c.stats.key_symbols = geo.k;
     c.stats.key_bits_per_symbol = geo.b;
 
@@ -1220,14 +1247,17 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
     // contiguous, then each bucket is sorted on chip (bucket.cuh)
     const int bb = bucket::kBucketBits;
     const bool msd = a.bucket_front && n >= (1ull << 22) && geo.total > bb + 8;
+    // otherwise, when key and position fit one word, the sort moves 8 B per
+    // suffix and pass instead of 12
+    const int vbits = msd ? 0 : geo.vbits;
     const int hist_shift = msd ? geo.total - bb : 0;
     const int key_passes = msd ? (bb + 7) / 8 : (geo.total + 7) / 8;
     uint32_t *counts = radix::hist_buffer(c);
     if (!counts) return set_err(c, CAPSSA_ENOMEM, "radix histograms");
     CAPSSA_CUDA(c, cudaMemsetAsync(counts, 0, radix::kMaxPasses * 256 * 4, c.stream));
     key_kernel<S><<<grid_for(n, kKeyTile), kKeyThreads, 0, c.stream>>>(
-        text, n, a.lim, coder, geo.b, geo.k, geo.lbits, lf, hist_shift, key_passes, keys_a,
-        counts);
+        text, n, a.lim, coder, geo.b, geo.k, geo.lbits, geo.flag_len, vbits, lf, hist_shift,
+        key_passes, keys_a, counts);
     CAPSSA_LAUNCHED(c);
     // bit-packed copy of the text for direct comparisons of small groups
     const uint64_t nwords = (n * (uint64_t)geo.b + 63) / 64 + 4;
@@ -1244,10 +1274,14 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
     cudaEventRecord(c.pev[1], c.stream);
     bool in_b = false;
     int passes = 0;
-    capssa_status s = radix::sort_pairs(c, keys_a, vals_a, keys_b, vals_b, nn, hist_shift,
-                                        geo.total, true, 0, &in_b, &passes, /*hist_ready=*/true);
+    capssa_status s =
+        vbits ? radix::sort_keys(c, keys_a, keys_b, nn, vbits, vbits + geo.total, &in_b, &passes,
+                                 /*hist_ready=*/true)
+              : radix::sort_pairs(c, keys_a, vals_a, keys_b, vals_b, nn, hist_shift, geo.total,
+                                  true, 0, &in_b, &passes, /*hist_ready=*/true);
     if (s != CAPSSA_OK) return s;
     c.stats.sort_passes = (uint32_t)passes;
+    c.stats.sort_item_bytes = vbits ? 8u : 12u;
     if (msd) {
         uint64_t *xk = in_b ? keys_b : keys_a, *yk = in_b ? keys_a : keys_b;
         uint32_t *xv = in_b ? vals_b : vals_a, *yv = in_b ? vals_a : vals_b;
@@ -1270,8 +1304,9 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
     }
     cudaEventRecord(c.pev[2], c.stream);
     const uint64_t *skeys = in_b ? keys_b : keys_a;
-    uint32_t *sa = in_b ? vals_b : vals_a;
-    uint32_t *spare_vals = in_b ? vals_a : vals_b;
+    // packed positions are unpacked into vals_a by init_groups
+    uint32_t *sa = (in_b && !vbits) ? vals_b : vals_a;
+    uint32_t *spare_vals = sa == vals_a ? vals_b : vals_a;
 
     // ---- 4. tied groups: direct comparison while shallow, rank doubling when deep
     // list capacities from the smallest group each list can hold
@@ -1296,7 +1331,8 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
     uint64_t h = (uint64_t)geo.k;
     CAPSSA_CUDA(c, cudaMemsetAsync(G.ctr, 0, sizeof(Counters), c.stream));
     init_groups_kernel<<<grid_for(n, 256 * kInitPer), 256, 0, c.stream>>>(
-        skeys, nn, geo.k, (1ull << geo.lbits) - 1, lf, hd, G);
+        skeys, nn, geo.k, (1ull << geo.lbits) - 1, lf, geo.flag_len, vbits, hd,
+        vbits ? sa : nullptr, G);
     CAPSSA_LAUNCHED(c);
 
     const int k2bits = bits_for(n + 1);
@@ -1336,19 +1372,6 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
         for (int l = 0; l < kLists; l++)
             CAPSSA_CUDA(c, cudaMemsetAsync(&G.ctr->n[l][nxt], 0, 4, c.stream));
         CAPSSA_CUDA(c, cudaMemsetAsync(&G.ctr->big_packed[nxt], 0, 8, c.stream));
-        // gathers read ranks of the previous depth; they finish before any
-        // rank of this round is rewritten (stream order)
-        if (cnt[L_DEEP]) {
-            gather_small_kernel<<<grid_for(cnt[L_DEEP], 128), 128, 0, c.stream>>>(
-                G.list[L_DEEP][cur], cnt[L_DEEP], sa, rank, a.lim, h, lf, empty_lf, key2);
-            CAPSSA_LAUNCHED(c);
-        }
-        const int ord_bits = nb > 1 ? bits_for(nb - 1) : 1;
-        if (nb) {
-            gather_big_kernel<<<nb, 256, 0, c.stream>>>(G.big[cur], sa, rank, a.lim, h, lf,
-                                                        empty_lf, k2bits, keys_a, spare_vals);
-            CAPSSA_LAUNCHED(c);
-        }
         if (cnt[L_PAIR]) {
             direct_pair_kernel<<<grid_for(cnt[L_PAIR], 256), 256, 0, c.stream>>>(
                 G.list[L_PAIR][cur], cnt[L_PAIR], sa, hd, rk, a.lim, P, lf, G, nxt);
@@ -1364,18 +1387,29 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
                 G.list[L_SMALL][cur], cnt[L_SMALL], sa, hd, rk, a.lim, P, lf, G, nxt);
             CAPSSA_LAUNCHED(c);
         }
-        if (cnt[L_DEEP]) {
-            sort_small_kernel<<<grid_for(cnt[L_DEEP], 128), 128, 0, c.stream>>>(
-                G.list[L_DEEP][cur], cnt[L_DEEP], sa, key2, hd, rank, lf, empty, 2 * h, G, nxt);
-            CAPSSA_LAUNCHED(c);
-        }
         if (cnt[L_MEDIUM]) {
             direct_medium_kernel<<<std::min<unsigned>(cnt[L_MEDIUM], c.sm_count * 8), kMedThreads,
                                    0, c.stream>>>(G.list[L_MEDIUM][cur], cnt[L_MEDIUM], sa, hd,
                                                   rk, a.lim, P, lf, G, nxt);
             CAPSSA_LAUNCHED(c);
         }
+        // rank doubling last: the direct kernels above rewrote the ranks of
+        // every group they resolved, which only refines them (equal ranks
+        // still agree through h symbols) and settles the depth-0 groups of
+        // early-ended suffixes, whose ranks agree on nothing yet
+        if (cnt[L_DEEP]) {
+            gather_small_kernel<<<grid_for(cnt[L_DEEP], 128), 128, 0, c.stream>>>(
+                G.list[L_DEEP][cur], cnt[L_DEEP], sa, rank, a.lim, h, lf, empty_lf, key2);
+            CAPSSA_LAUNCHED(c);
+            sort_small_kernel<<<grid_for(cnt[L_DEEP], 128), 128, 0, c.stream>>>(
+                G.list[L_DEEP][cur], cnt[L_DEEP], sa, key2, hd, rank, lf, empty, 2 * h, G, nxt);
+            CAPSSA_LAUNCHED(c);
+        }
+        const int ord_bits = nb > 1 ? bits_for(nb - 1) : 1;
         if (nb) {
+            gather_big_kernel<<<nb, 256, 0, c.stream>>>(G.big[cur], sa, rank, a.lim, h, lf,
+                                                        empty_lf, k2bits, keys_a, spare_vals);
+            CAPSSA_LAUNCHED(c);
             bool tb = false;
             uint32_t *tv_b = (uint32_t *)key2;  // free once sort_small has run
             s = radix::sort_pairs(c, keys_a, spare_vals, keys_b, tv_b, big_total, 0,

@@ -79,7 +79,10 @@ __device__ __forceinline__ void st_volatile_u64(unsigned long long *p, unsigned 
     *(volatile unsigned long long *)p = v;
 }
 
-template <bool GEN_VALS>
+// MODE: kPairs (values read), kGenVals (value = val_base + index), kKeysOnly.
+constexpr int kPairs = 0, kGenVals = 1, kKeysOnly = 2;
+
+template <int MODE>
 __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
     onesweep_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
                     uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out,
@@ -87,9 +90,10 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
                     unsigned long long *__restrict__ status, uint32_t *__restrict__ tile_counter,
                     int *__restrict__ err, uint32_t val_base) {
     extern __shared__ __align__(16) unsigned char smem[];
+    constexpr bool kVals = MODE != kKeysOnly;
     uint64_t *s_keys = reinterpret_cast<uint64_t *>(smem);
     uint32_t *s_vals = reinterpret_cast<uint32_t *>(s_keys + kTile);
-    uint32_t *s_whist = s_vals + kTile;              // kWarps * kRadix
+    uint32_t *s_whist = s_vals + (kVals ? kTile : 0);  // kWarps * kRadix
     uint32_t *s_lstart = s_whist + kWarps * kRadix;  // kRadix
     uint32_t *s_gbase = s_lstart + kRadix;           // kRadix
     uint32_t *s_scan = s_gbase + kRadix;             // kWarps
@@ -114,7 +118,8 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
         uint32_t idx = wbase + j * 32 + lane;
         if (idx < n) {
             k[j] = keys_in[idx];
-            v[j] = GEN_VALS ? val_base + idx : vals_in[idx];
+            if (MODE == kGenVals) v[j] = val_base + idx;
+            if (MODE == kPairs) v[j] = vals_in[idx];
         } else {
             k[j] = ~0ull;  // past the end: digit 255, ranked after every valid key
             v[j] = 0;
@@ -212,7 +217,7 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
     for (int j = 0; j < kItems; j++) {
         uint32_t pos = s_lstart[d[j]] + wh[d[j]] + r[j];
         s_keys[pos] = k[j];
-        s_vals[pos] = v[j];
+        if (kVals) s_vals[pos] = v[j];
     }
     __syncthreads();
     for (uint32_t i = tid; i < valid; i += kThreads) {
@@ -221,7 +226,7 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
         uint32_t out = s_gbase[dd] + (i - s_lstart[dd]);
         if (out < n) {  // only false after a timed-out look-back (flagged)
             keys_out[out] = key;
-            vals_out[out] = s_vals[i];
+            if (kVals) vals_out[out] = s_vals[i];
         }
     }
 }
@@ -231,8 +236,8 @@ __global__ void iota_kernel(uint32_t *out, uint32_t n, uint32_t base) {
         out[i] = base + i;
 }
 
-static size_t pass_smem() {
-    return (size_t)kTile * 8 + (size_t)kTile * 4 + (size_t)kWarps * kRadix * 4 +
+static size_t pass_smem(bool vals) {
+    return (size_t)kTile * 8 + (vals ? (size_t)kTile * 4 : 0) + (size_t)kWarps * kRadix * 4 +
            (size_t)kRadix * 4 * 2 + (size_t)kWarps * 4;
 }
 
@@ -240,10 +245,12 @@ uint32_t *hist_buffer(Ctx &c) {
     return (uint32_t *)ws_get(c, WS_RADIX_HIST, (kMaxPasses + 1) * kRadix * 4 + 64);
 }
 
-capssa_status sort_pairs(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *keys_b,
-                         uint32_t *vals_b, uint32_t n, int begin_bit, int end_bit,
-                         bool gen_vals, uint32_t val_base, bool *result_in_b,
-                         int *passes_run, bool hist_ready) {
+namespace {
+
+capssa_status sort_impl(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *keys_b,
+                        uint32_t *vals_b, uint32_t n, int begin_bit, int end_bit, bool gen_vals,
+                        uint32_t val_base, bool *result_in_b, int *passes_run, bool hist_ready) {
+    const bool keys_only = vals_a == nullptr;
     *result_in_b = false;
     if (passes_run) *passes_run = 0;
     if (n == 0) return CAPSSA_OK;
@@ -277,10 +284,12 @@ capssa_status sort_pairs(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *k
 
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(onesweep_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)pass_smem());
-        cudaFuncSetAttribute(onesweep_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)pass_smem());
+        cudaFuncSetAttribute(onesweep_kernel<kPairs>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)pass_smem(true));
+        cudaFuncSetAttribute(onesweep_kernel<kGenVals>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pass_smem(true));
+        cudaFuncSetAttribute(onesweep_kernel<kKeysOnly>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pass_smem(false));
         attr_set = true;
     }
     // per-pass exclusive offsets live in the pinned scratch after the counts
@@ -308,12 +317,16 @@ capssa_status sort_pairs(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *k
         const uint32_t *vi = in_b ? vals_b : vals_a;
         uint64_t *ko = in_b ? keys_a : keys_b;
         uint32_t *vo = in_b ? vals_a : vals_b;
-        if (vals_pending)
-            onesweep_kernel<true><<<n_tiles, kThreads, pass_smem(), c.stream>>>(
+        if (keys_only)
+            onesweep_kernel<kKeysOnly><<<n_tiles, kThreads, pass_smem(false), c.stream>>>(
+                ki, nullptr, ko, nullptr, n, begin_bit + 8 * p, offsets, status, tile_counter,
+                c.d_flags, 0);
+        else if (vals_pending)
+            onesweep_kernel<kGenVals><<<n_tiles, kThreads, pass_smem(true), c.stream>>>(
                 ki, vi, ko, vo, n, begin_bit + 8 * p, offsets, status, tile_counter, c.d_flags,
                 val_base);
         else
-            onesweep_kernel<false><<<n_tiles, kThreads, pass_smem(), c.stream>>>(
+            onesweep_kernel<kPairs><<<n_tiles, kThreads, pass_smem(true), c.stream>>>(
                 ki, vi, ko, vo, n, begin_bit + 8 * p, offsets, status, tile_counter, c.d_flags,
                 val_base);
         CAPSSA_LAUNCHED(c);
@@ -325,13 +338,30 @@ capssa_status sort_pairs(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *k
         // this copy has been consumed, which stream order guarantees because
         // each pass reads its own slice of h_off.
     }
-    if (vals_pending) {
+    if (vals_pending && !keys_only) {
         uint32_t *dst = in_b ? vals_b : vals_a;
         iota_kernel<<<grid_for(n, 256, 4096), 256, 0, c.stream>>>(dst, n, val_base);
         CAPSSA_LAUNCHED(c);
     }
     *result_in_b = in_b;
     return CAPSSA_OK;
+}
+
+}  // namespace
+
+capssa_status sort_pairs(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *keys_b,
+                         uint32_t *vals_b, uint32_t n, int begin_bit, int end_bit,
+                         bool gen_vals, uint32_t val_base, bool *result_in_b,
+                         int *passes_run, bool hist_ready) {
+    if (!vals_a || !vals_b) return set_err(c, CAPSSA_EINVAL, "radix: null values");
+    return sort_impl(c, keys_a, vals_a, keys_b, vals_b, n, begin_bit, end_bit, gen_vals,
+                     val_base, result_in_b, passes_run, hist_ready);
+}
+
+capssa_status sort_keys(Ctx &c, uint64_t *keys_a, uint64_t *keys_b, uint32_t n, int begin_bit,
+                        int end_bit, bool *result_in_b, int *passes_run, bool hist_ready) {
+    return sort_impl(c, keys_a, nullptr, keys_b, nullptr, n, begin_bit, end_bit, false, 0,
+                     result_in_b, passes_run, hist_ready);
 }
 
 }  // namespace radix

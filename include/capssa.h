@@ -116,7 +116,8 @@ typedef struct capssa_stats {
     double refine_ms;     /* rank-doubling rounds */
     double finish_ms;     /* bounded-context pass, output ordering and copy */
     uint32_t sort_passes; /* radix passes executed by the initial sort */
-    uint32_t reserved0;
+    uint32_t sort_item_bytes; /* bytes per record the radix passes move: 8 (position packed
+                                 below the key) or 12 (key + separate u32 position) */
     double sort_pass_ms;  /* summed duration of those radix-pass kernels */
 } capssa_stats;
 
