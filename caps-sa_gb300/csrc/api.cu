@@ -65,11 +65,12 @@ capssa_status check_dev_flags(Ctx &c) {
     return CAPSSA_OK;
 }
 
-// Key geometry for b bits per symbol on a text of n symbols.  The widest
-// key holds kmax symbols (kmax*b + bits(kmax) <= 64).  Symbols past
-// log_{2^b}(n) + 4 rarely separate random suffixes, so the key keeps only
-// as many symbols as fit in the radix passes that this minimum needs:
-// DNA at n = 2^28 keeps 21 symbols in 6 passes instead of 29 in 8.
+// Key geometry for b bits per symbol on a text of n symbols.  Symbols past
+// log_{2^b}(n) + 3 rarely separate random suffixes, so the key keeps only
+// as many symbols as fit in the radix passes that this minimum needs (DNA
+// at n = 2^28: 17 symbols + a flag = 35 bits, 5 passes), with the position
+// packed below it when key and position fit 64 bits.  Otherwise the widest
+// key holds kmax symbols (kmax*b + bits(kmax) <= 64) and a length field.
 KeyGeom key_geom(int b, uint64_t n, bool plain) {
     KeyGeom g{};
     g.b = b < 1 ? 1 : b;

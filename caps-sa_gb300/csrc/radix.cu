@@ -79,6 +79,54 @@ __device__ __forceinline__ void st_volatile_u64(unsigned long long *p, unsigned 
     *(volatile unsigned long long *)p = v;
 }
 
+// Decoupled look-back for digit dg of `tile`: the sum of the counts of
+// every earlier tile, from their published aggregates (A) back to the
+// nearest inclusive prefix (P).  kLookBatch predecessors are read per round trip;
+// a predecessor that has published nothing yet is polled again (bounded by
+// kSpinLimit polls, then DEV_LOOKBACK_TIMEOUT).
+#ifndef CAPSSA_RADIX_LOOKBATCH
+#define CAPSSA_RADIX_LOOKBATCH 4
+#endif
+constexpr int kLookBatch = CAPSSA_RADIX_LOOKBATCH;
+
+__device__ __forceinline__ uint64_t lookback(const unsigned long long *status, uint32_t tile,
+                                             uint32_t dg, int *err) {
+    uint64_t excl = 0;
+    int64_t t = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    while (t >= 0) {
+        unsigned long long sv[kLookBatch];
+#pragma unroll
+        for (int q = 0; q < kLookBatch; q++)
+            sv[q] = t - q >= 0 ? ld_volatile_u64(status + (size_t)(t - q) * kRadix + dg) : kFlagP;
+        int used = 0;
+        bool found = false, stalled = false;
+#pragma unroll
+        for (int q = 0; q < kLookBatch; q++) {
+            if (!found && !stalled) {
+                const unsigned long long flag = sv[q] & ~kValMask;
+                if (flag == 0) {
+                    stalled = true;
+                } else {
+                    excl += sv[q] & kValMask;
+                    used++;
+                    if (flag == kFlagP) found = true;
+                }
+            }
+        }
+        if (found) break;
+        t -= used;
+        if (stalled) {
+            if (++spins > kSpinLimit) {
+                atomicCAS(err, DEV_OK, DEV_LOOKBACK_TIMEOUT);
+                break;
+            }
+            __nanosleep(32);
+        }
+    }
+    return excl;
+}
+
 // MODE: kPairs (values read), kGenVals (value = val_base + index), kKeysOnly.
 constexpr int kPairs = 0, kGenVals = 1, kKeysOnly = 2;
 
@@ -170,23 +218,7 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
         st_volatile_u64(st, kFlagP | counted);
     } else {
         st_volatile_u64(st, kFlagA | counted);
-        int64_t t = (int64_t)tile - 1;
-        uint32_t spins = 0;
-        while (t >= 0) {
-            unsigned long long s = ld_volatile_u64(status + (size_t)t * kRadix + dg);
-            unsigned long long flag = s & ~kValMask;
-            if (flag == 0) {
-                if (++spins > kSpinLimit) {
-                    atomicCAS(err, DEV_OK, DEV_LOOKBACK_TIMEOUT);
-                    break;
-                }
-                __nanosleep(64);
-                continue;
-            }
-            excl += s & kValMask;
-            if (flag == kFlagP) break;
-            t--;
-        }
+        excl = lookback(status, tile, dg, err);
         st_volatile_u64(st, kFlagP | (excl + counted));
     }
     s_gbase[dg] = digit_offsets[dg] + (uint32_t)excl;
