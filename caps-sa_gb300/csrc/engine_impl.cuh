@@ -34,13 +34,18 @@ struct BigGroup {
 // Work lists of one refinement round, by group size and depth.
 enum GroupList : int {
     L_PAIR = 0,    // 2 members: one thread
-    L_TINY = 1,    // 3..8 members: one thread
+    L_TINY = 1,    // 3..4 members: one thread
     L_SMALL = 2,   // 9..32 members: one warp
     L_MEDIUM = 3,  // 33..kMediumMax members: one block
     L_DEEP = 4,    // <= 32 members deeper than kDirectMaxH: rank doubling
-    kLists = 5     // larger groups: the radix (rank doubling) path
+    L_TINY8 = 5,   // 5..8 members: eight lanes
+    kLists = 6     // larger groups: the radix (rank doubling) path
 };
 constexpr uint32_t kTinyMax = 8;
+constexpr uint32_t kTiny4 = 4;
+#ifndef CAPSSA_PAIR_BURST
+#define CAPSSA_PAIR_BURST 4  // windows the pair kernel loads in its first round trip
+#endif
 
 // Device counters of the refinement rounds, double-buffered by round parity.
 struct Counters {
@@ -235,7 +240,8 @@ __device__ __forceinline__ BigGroup *big_ptr(const GroupLists &G, int q) {
 __device__ __forceinline__ int list_of(uint32_t len, uint64_t depth) {
     if (len <= kSmallMax && depth > kDirectMaxH) return L_DEEP;
     if (len == 2) return L_PAIR;
-    if (len <= kTinyMax) return L_TINY;
+    if (len <= kTiny4) return L_TINY;
+    if (len <= kTinyMax) return L_TINY8;
     if (len <= kSmallMax) return L_SMALL;
     if (len <= kMediumMax && depth <= kDirectMaxH) return L_MEDIUM;
     return kLists;
@@ -353,7 +359,7 @@ __global__ void __launch_bounds__(256)
             depth = (uint64_t)k;
         }
     };
-    uint32_t cnt[kLists] = {0, 0, 0, 0, 0};
+    uint32_t cnt[kLists] = {};
     // pass 1: heads (and positions), and how many groups of each list this
     // thread ends
 #pragma unroll 4
@@ -555,13 +561,12 @@ struct PackedStream {
     }
 };
 
-// A[q] for a runtime q < 5 without spilling the array to local memory.
-__device__ __forceinline__ uint64_t pick5(const uint64_t (&A)[5], int q) {
+// A[q] for a runtime q < N without spilling the array to local memory.
+template <int N>
+__device__ __forceinline__ uint64_t pickn(const uint64_t (&A)[N], int q) {
     uint64_t v = A[0];
-    v = q == 1 ? A[1] : v;
-    v = q == 2 ? A[2] : v;
-    v = q == 3 ? A[3] : v;
-    v = q == 4 ? A[4] : v;
+#pragma unroll
+    for (int i = 1; i < N; i++) v = q == i ? A[i] : v;
     return v;
 }
 
@@ -569,14 +574,14 @@ __device__ __forceinline__ uint64_t pick5(const uint64_t (&A)[5], int q) {
 // -1 / 1, 0 for a complete tie (ShorterFirst, equal limits), 2 when they
 // still agree `cap` symbols further (undecided).  Mirrors suffix_cmp_with
 // (src/lcp.rs:184-201) from offset o.
+template <int kBurst = 4>
 __device__ __forceinline__ int direct_cmp(const Packed &P, uint64_t a, uint64_t la, uint64_t b,
                                           uint64_t lb, uint64_t o, uint64_t cap, int lf) {
     const uint64_t lim = la < lb ? la : lb;
     const uint64_t end = lim < o + cap ? lim : o + cap;
-    // the first four windows of both suffixes are fetched with independent
+    // the first kBurst windows of both suffixes are fetched with independent
     // loads (one round trip covers the common short-LCP case), later ones
     // stream one word per window
-    constexpr int kBurst = 4;
     uint64_t t = o;
     if (t < end) {
         uint64_t sa0 = (a + t) * (uint64_t)P.b, sb0 = (b + t) * (uint64_t)P.b;
@@ -598,8 +603,8 @@ __device__ __forceinline__ int direct_cmp(const Packed &P, uint64_t a, uint64_t 
             if (t >= end) break;
             int qa = (int)(bit_a >> 6), qb = (int)(bit_b >> 6);
             uint32_t ra = bit_a & 63, rb = bit_b & 63;
-            uint64_t a0 = pick5(A, qa), a1 = pick5(A, qa + 1);
-            uint64_t b0 = pick5(B, qb), b1 = pick5(B, qb + 1);
+            uint64_t a0 = pickn(A, qa), a1 = pickn(A, qa + 1);
+            uint64_t b0 = pickn(B, qb), b1 = pickn(B, qb + 1);
             uint64_t va = (ra ? (a0 << ra) | (a1 >> (64 - ra)) : a0) & P.mask;
             uint64_t vb = (rb ? (b0 << rb) | (b1 >> (64 - rb)) : b0) & P.mask;
             uint64_t x = va ^ vb;
@@ -678,7 +683,7 @@ __global__ void __launch_bounds__(256)
         cap = o > kDirectCap ? o : kDirectCap;
         uint32_t p0 = sa[g.x], p1 = sa[g.x + 1];
         uint64_t l0 = dev_lim_at(L, p0), l1 = dev_lim_at(L, p1);
-        int r = direct_cmp(P, p0, l0, p1, l1, o, cap, lf);
+        int r = direct_cmp<CAPSSA_PAIR_BURST>(P, p0, l0, p1, l1, o, cap, lf);
         if (r == 1 || ((r == 0 || r == 2) && p0 > p1)) {
             uint32_t t = p0;
             p0 = p1;
@@ -699,96 +704,120 @@ __global__ void __launch_bounds__(256)
     block_append(G, nxt, again, g.x, 2, (uint64_t)g.z + cap);
 }
 
-// Two consecutive windows of the packed text starting at symbol p (three
-// word loads).
-__device__ __forceinline__ void windows2_at(const Packed &P, uint64_t p, uint64_t &w0,
-                                            uint64_t &w1) {
+// Four consecutive windows of the packed text from symbol p (five word
+// loads, all independent).
+__device__ __forceinline__ void windows4_at(const Packed &P, uint64_t p, uint64_t (&w)[4]) {
     const uint64_t s = p * (uint64_t)P.b;
     const uint64_t *q = P.w + (s >> 6);
     const uint32_t sh = (uint32_t)(s & 63);
-    const uint64_t x0 = __ldg(q), x1 = __ldg(q + 1), x2 = __ldg(q + 2);
-    w0 = (sh ? (x0 << sh) | (x1 >> (64 - sh)) : x0) & P.mask;
-    const uint32_t s2 = sh + (uint32_t)(P.spw * P.b);  // < 128
-    const uint64_t y0 = s2 >= 64 ? x1 : x0, y1 = s2 >= 64 ? x2 : x1;
-    const uint32_t r2 = s2 & 63;
-    w1 = (r2 ? (y0 << r2) | (y1 >> (64 - r2)) : y0) & P.mask;
+    uint64_t x[5];
+#pragma unroll
+    for (int i = 0; i < 5; i++) x[i] = __ldg(q + i);
+    const uint32_t wbits = (uint32_t)(P.spw * P.b);
+    if (wbits == 64) {  // b divides 64 (DNA): window i starts in word i
+#pragma unroll
+        for (int i = 0; i < 4; i++) w[i] = sh ? (x[i] << sh) | (x[i + 1] >> (64 - sh)) : x[i];
+        return;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const uint32_t bit = sh + i * wbits;  // < 256
+        const int wi = (int)(bit >> 6);
+        const uint32_t r = bit & 63;
+        const uint64_t a0 = pickn(x, wi), a1 = pickn(x, wi + 1);
+        w[i] = (r ? (a0 << r) | (a1 >> (64 - r)) : a0) & P.mask;
+    }
 }
 
-// Index of member pair (i, j), i < j < kTinyMax, in 0..27.
-__host__ __device__ constexpr int tiny_pair(int i, int j) {
-    return i * (2 * (int)kTinyMax - 1 - i) / 2 + (j - i - 1);
+template <int N>
+__device__ __forceinline__ uint32_t pick32(const uint32_t (&A)[N], int q) {
+    uint32_t v = A[0];
+#pragma unroll
+    for (int i = 1; i < N; i++) v = q == i ? A[i] : v;
+    return v;
 }
 
-// Tied groups of 3..kTinyMax members: one thread per group.  The first two
-// windows of every member past the shared depth are loaded up front (all
-// independent loads, one round trip for the group) and every member pair is
-// compared on those registers; only pairs that agree on both windows go on
-// with direct_cmp.  A member's place is the count of members before it, so
-// nothing moves until the final scatter.  Counts (4 bits per member) and
-// pair relations (2 bits per pair) live in packed registers.
+// Tied groups of 3..4 members: one thread per group, in rounds of four
+// windows (128 DNA symbols): a round loads the next four windows of
+// every member with independent loads (one round trip for the group) and
+// settles every still-undecided member pair that differs in them.  Near a
+// member's end (rare: the last symbols of a text or segment) the remaining
+// pairs are settled one by one by direct_cmp.  A member's place is the
+// count of members before it, so nothing moves until the final scatter;
+// counts (4 bits per member) and pair relations (2 bits per pair) live in
+// packed registers.
+template <int M>
 __global__ void __launch_bounds__(128)
     direct_tiny_kernel(const uint4 *__restrict__ groups, uint32_t count,
                        uint32_t *__restrict__ sa, uint32_t *__restrict__ hd,
                        uint32_t *__restrict__ rank, DevLimits L, Packed P, int lf, GroupLists G,
                        int nxt) {
-    constexpr int M = (int)kTinyMax;
     for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < count;
          gi += gridDim.x * blockDim.x) {
         const uint4 g = groups[gi];
         const int len = (int)g.y;
         const uint64_t o = g.z;
         const uint64_t cap = o > kDirectCap ? o : kDirectCap;
-        const uint64_t span = 2 * (uint64_t)P.spw;  // symbols held by the two windows
-        uint32_t pp[M];
-        uint64_t ll[M], w0[M], w1[M];
-        bool full[M];  // limit past both windows: the register compare is exact
+        uint32_t pp[M], lm[M];
+        uint64_t minend = o + cap;  // no comparison of the group looks past this
 #pragma unroll
         for (int t = 0; t < M; t++) {
             if (t < len) {
                 pp[t] = sa[g.x + t];
-                ll[t] = dev_lim_at(L, pp[t]);
-                full[t] = ll[t] >= o + span;
-                windows2_at(P, (uint64_t)pp[t] + o, w0[t], w1[t]);
+                lm[t] = (uint32_t)dev_lim_at(L, pp[t]);
+                minend = lm[t] < minend ? lm[t] : minend;
             }
         }
-        uint32_t bef = 0;      // 4 bits per member: members placed before it
-        uint64_t rel = 0;      // 2 bits per pair: 0 ordered, 1 complete tie, 2 undecided
-        uint32_t slow = 0;     // pairs left for direct_cmp
+        uint64_t und64 = 0;  // bit (i * M + j), i < j: pair not settled yet
 #pragma unroll
-        for (int i = 0; i < M; i++) {
+        for (int i = 0; i < M; i++)
 #pragma unroll
-            for (int j = i + 1; j < M; j++) {
-                if (j < len) {
-                    const int pi = tiny_pair(i, j);
-                    if (full[i] && full[j] && (w0[i] != w0[j] || w1[i] != w1[j])) {
-                        const bool i_first = w0[i] != w0[j] ? w0[i] < w0[j] : w1[i] < w1[j];
-                        bef += i_first ? (1u << (4 * j)) : (1u << (4 * i));
-                    } else {
-                        slow |= 1u << pi;
+            for (int j = i + 1; j < M; j++)
+                if (j < len) und64 |= 1ull << (i * M + j);
+        uint32_t bef = 0;            // 4 bits per member: members placed before it
+        uint64_t tie = 0, undc = 0;  // bit (i * M + j): complete tie / undecided at the cap
+        const uint64_t span = 4 * (uint64_t)P.spw;
+        uint64_t base = o;
+        while (und64) {
+            if (base + span <= minend) {
+                uint64_t w[M][4];
+#pragma unroll
+                for (int t = 0; t < M; t++)
+                    if (t < len) windows4_at(P, (uint64_t)pp[t] + base, w[t]);
+#pragma unroll
+                for (int i = 0; i < M; i++)
+#pragma unroll
+                    for (int j = i + 1; j < M; j++) {
+                        const uint64_t bit = 1ull << (i * M + j);
+                        if (j < len && (und64 & bit)) {
+                            int r = 0;
+#pragma unroll
+                            for (int q = 3; q >= 0; q--)
+                                r = w[i][q] != w[j][q] ? (w[i][q] < w[j][q] ? -1 : 1) : r;
+                            if (r) {
+                                bef += r < 0 ? (1u << (4 * j)) : (1u << (4 * i));
+                                und64 &= ~bit;
+                            }
+                        }
                     }
+                base += span;
+            } else {
+                // a member's end or the horizon is within reach: the rest
+                // pair by pair (direct_cmp settles a pair at its end too)
+                for (uint64_t m = und64; m; m &= m - 1) {
+                    const int pi = __ffsll((long long)m) - 1;
+                    const int i = pi / M, j = pi % M;
+                    const uint32_t a = pick32(pp, i), b = pick32(pp, j);
+                    const uint32_t la = pick32(lm, i), lb = pick32(lm, j);
+                    const uint64_t done = base - o;  // symbols known equal past o
+                    const int r = direct_cmp(P, a, la, b, lb, base, cap - done, lf);
+                    const bool i_first = r == -1 || ((r == 0 || r == 2) && a < b);
+                    bef += i_first ? (1u << (4 * j)) : (1u << (4 * i));
+                    if (r == 0) tie |= 1ull << pi;
+                    if (r == 2) undc |= 1ull << pi;
                 }
+                und64 = 0;
             }
-        }
-        // pairs that agree on both windows (or end inside them): one
-        // direct comparison each, members re-read from the slice
-        while (slow) {
-            const int pi = __ffs((int)slow) - 1;
-            slow &= slow - 1;
-            int i = 0, rem = pi;
-            while (rem >= M - 1 - i) {
-                rem -= M - 1 - i;
-                i++;
-            }
-            const int j = i + 1 + rem;
-            const uint32_t a = sa[g.x + i], b = sa[g.x + j];
-            const uint64_t la = dev_lim_at(L, a), lb = dev_lim_at(L, b);
-            const bool past = la >= o + span && lb >= o + span;
-            const int r = past ? direct_cmp(P, a, la, b, lb, o + span, cap - span, lf)
-                               : direct_cmp(P, a, la, b, lb, o, cap, lf);
-            const bool i_first = r == -1 || ((r == 0 || r == 2) && a < b);
-            bef += i_first ? (1u << (4 * j)) : (1u << (4 * i));
-            const uint64_t code = r == 0 ? 1u : (r == 2 ? 2u : 0u);
-            rel |= code << (2 * pi);
         }
         // slot of each member, relation of each slot to the one before it
         uint32_t starts = 1u;  // bit s: slot s begins a tie run
@@ -797,16 +826,17 @@ __global__ void __launch_bounds__(128)
         for (int t = 0; t < M; t++) {
             if (t < len) {
                 const uint32_t st = (bef >> (4 * t)) & 15u;
-                uint32_t code = 0;
+                bool tied = false, open = false;
 #pragma unroll
                 for (int u = 0; u < M; u++) {
                     if (u < len && u != t && ((bef >> (4 * u)) & 15u) + 1u == st) {
-                        const int pi = u < t ? tiny_pair(u, t) : tiny_pair(t, u);
-                        code = (uint32_t)(rel >> (2 * pi)) & 3u;
+                        const int pi = u < t ? u * M + t : t * M + u;
+                        tied = (tie >> pi) & 1ull;
+                        open = (undc >> pi) & 1ull;
                     }
                 }
-                if (st > 0 && code == 0) starts |= 1u << st;
-                if (st > 0 && code == 2) undec |= 1u << st;
+                if (st > 0 && !tied && !open) starts |= 1u << st;
+                if (st > 0 && open) undec |= 1u << st;
             }
         }
 #pragma unroll
@@ -829,6 +859,105 @@ __global__ void __launch_bounds__(128)
                     append_group(G, nxt, g.x + head, (uint32_t)s2 - head + 1, o + cap);
             }
         }
+    }
+}
+
+// Tied groups of 5..kTinyMax members: S lanes per group (32/S groups per
+// warp), one member per lane, in rounds of four windows: every lane loads
+// the next four windows of its member (one round trip for the group),
+// exchanges them with its group by shuffles and settles its undecided
+// relations that differ in them.  Near a member's end or the horizon the
+// rest is settled by direct_cmp.  A member's place is the count of members
+// before it.
+template <int S>
+__global__ void __launch_bounds__(128)
+    direct_tiny_seg_kernel(const uint4 *__restrict__ groups, uint32_t count,
+                           uint32_t *__restrict__ sa, uint32_t *__restrict__ hd,
+                           uint32_t *__restrict__ rank, DevLimits L, Packed P, int lf,
+                           GroupLists G, int nxt) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t sl = lane & (S - 1), sb = lane & ~(uint32_t)(S - 1);
+    const uint64_t gi = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / S;
+    const uint4 g = gi < count ? groups[gi] : make_uint4(0, 0, 0, 0);
+    const int len = (int)g.y;
+    const bool mine = (int)sl < len;
+    const uint64_t o = g.z;
+    const uint64_t cap = o > kDirectCap ? o : kDirectCap;
+    const uint64_t horizon = o + cap;
+    const uint32_t my_p = mine ? sa[g.x + sl] : 0u;
+    const uint32_t my_lim = mine ? (uint32_t)dev_lim_at(L, my_p) : 0u;
+    uint32_t op[S], ol[S];
+    uint32_t und = 0;  // bit u: relation with member u not settled yet
+    uint64_t minend = horizon;
+#pragma unroll
+    for (int u = 0; u < S; u++) {
+        op[u] = __shfl_sync(0xffffffffu, my_p, sb + u);
+        ol[u] = __shfl_sync(0xffffffffu, my_lim, sb + u);
+        if (u < len) minend = ol[u] < minend ? ol[u] : minend;
+        if (mine && u != (int)sl && u < len) und |= 1u << u;
+    }
+    uint32_t before = 0, tie = 0, undc = 0;  // tie / undc: bit u, relation with u
+    const uint64_t span = 4 * (uint64_t)P.spw;
+    uint64_t base = o;
+    while (__any_sync(0xffffffffu, und != 0)) {
+        const bool fast = base + span <= minend;
+        const bool seg_busy = (__ballot_sync(0xffffffffu, und != 0) >> sb) & ((1u << S) - 1u);
+        uint64_t w[4] = {0, 0, 0, 0};
+        if (mine && fast && seg_busy) windows4_at(P, (uint64_t)my_p + base, w);
+#pragma unroll
+        for (int u = 0; u < S; u++) {
+            int r = 0;
+#pragma unroll
+            for (int q = 3; q >= 0; q--) {
+                const uint64_t wu = __shfl_sync(0xffffffffu, w[q], sb + u);
+                r = w[q] != wu ? (w[q] < wu ? -1 : 1) : r;
+            }
+            if (fast && ((und >> u) & 1u) && r) {
+                before += r > 0 ? 1u : 0u;
+                und &= ~(1u << u);
+            }
+        }
+        if (fast) {
+            base += span;
+        } else {
+            for (uint32_t m = und; m; m &= m - 1) {
+                const int u = __ffs((int)m) - 1;
+                const uint32_t b = pick32(op, u), lb = pick32(ol, u);
+                const int r = direct_cmp(P, my_p, my_lim, b, lb, base, horizon - base, lf);
+                const bool me_first = r == -1 || ((r == 0 || r == 2) && my_p < b);
+                before += me_first ? 0u : 1u;
+                if (r == 0) tie |= 1u << u;
+                if (r == 2) undc |= 1u << u;
+            }
+            und = 0;
+        }
+    }
+    // sorted slot, relation to the slot before, tie-run heads
+    const uint32_t slot = before;
+    bool ptie = false, popen = false;
+#pragma unroll
+    for (int u = 0; u < S; u++) {
+        const uint32_t su = __shfl_sync(0xffffffffu, slot, sb + u);
+        if (mine && u != (int)sl && u < len && su + 1 == slot) {
+            ptie = (tie >> u) & 1u;
+            popen = (undc >> u) & 1u;
+        }
+    }
+    uint32_t starts = (mine && (slot == 0 || (!ptie && !popen))) ? (1u << slot) : 0u;
+    uint32_t undec = (mine && slot > 0 && popen) ? (1u << slot) : 0u;
+#pragma unroll
+    for (int x = 1; x < S; x <<= 1) {
+        starts |= __shfl_xor_sync(0xffffffffu, starts, x);
+        undec |= __shfl_xor_sync(0xffffffffu, undec, x);
+    }
+    if (mine) {
+        const uint32_t head = 31u - (uint32_t)__clz((int)(starts & ((2u << slot) - 1u)));
+        sa[g.x + slot] = my_p;
+        hd[g.x + slot] = g.x + head;
+        if (rank) rank[my_p] = g.x + head;
+        const bool run_end = (int)slot == len - 1 || ((starts >> (slot + 1)) & 1u);
+        if (run_end && head < slot && ((undec >> slot) & 1u))
+            append_group(G, nxt, g.x + head, slot - head + 1, o + cap);
     }
 }
 
@@ -1169,6 +1298,44 @@ inline bool profile_on() {
     return on;
 }
 
+// Per-kernel device times of one refinement round, printed with the
+// round's line when CAPSSA_PROFILE is set (events only in that case).
+struct KernelTimes {
+    static constexpr int kMax = 12;
+    cudaEvent_t ev[kMax + 1] = {};
+    const char *name[kMax] = {};
+    int used = 0;
+    bool on = false;
+    explicit KernelTimes(bool enable) : on(enable) {
+        if (on)
+            for (auto &e : ev) cudaEventCreate(&e);
+    }
+    ~KernelTimes() {
+        if (on)
+            for (auto &e : ev) cudaEventDestroy(e);
+    }
+    void start(cudaStream_t s) {
+        used = 0;
+        if (on) cudaEventRecord(ev[0], s);
+    }
+    void mark(cudaStream_t s, const char *what) {
+        if (!on || used >= kMax) return;
+        name[used] = what;
+        cudaEventRecord(ev[++used], s);
+    }
+    void print() {
+        if (!on || !used) return;
+        cudaEventSynchronize(ev[used]);
+        std::fprintf(stderr, "capssa profile    kernels:");
+        for (int i = 0; i < used; i++) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+            std::fprintf(stderr, " %s %.3f ms", name[i], ms);
+        }
+        std::fprintf(stderr, "\n");
+    }
+};
+
 inline int bits_for(uint64_t v) {  // bits to represent 0..v
     int b = 0;
     while (b < 64 && (v >> b) != 0) b++;
@@ -1310,8 +1477,8 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
 
     // ---- 4. tied groups: direct comparison while shallow, rank doubling when deep
     // list capacities from the smallest group each list can hold
-    const size_t cap_of[kLists] = {(size_t)n / 2 + 2, (size_t)n / 3 + 2, (size_t)n / 9 + 2,
-                                   (size_t)n / 33 + 2, (size_t)n / 2 + 2};
+    const size_t cap_of[kLists] = {(size_t)n / 2 + 2,  (size_t)n / 3 + 2, (size_t)n / 9 + 2,
+                                   (size_t)n / 33 + 2, (size_t)n / 2 + 2, (size_t)n / 5 + 2};
     const size_t big_cap = (size_t)n / (kSmallMax + 1) + 2;
     size_t list_bytes = 256 + big_cap * 16 * 2;
     for (int l = 0; l < kLists; l++) list_bytes += cap_of[l] * 16 * 2;
@@ -1340,6 +1507,7 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
     const uint64_t empty = lf ? empty_lf : 0ull;
     bool ranks_ready = false;
     int cur = 0;
+    KernelTimes kt(profile_on());
     Counters *hc = (Counters *)c.h_scratch;
     for (;;) {
         CAPSSA_CUDA(c, cudaMemcpyAsync(hc, G.ctr, sizeof(Counters), cudaMemcpyDeviceToHost,
@@ -1352,10 +1520,11 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
         const uint32_t big_total = (uint32_t)(hc->big_packed[cur] & kBigTotMask);
         if (profile_on())
             std::fprintf(stderr,
-                         "capssa profile  round %u depth %llu: pairs %u tiny %u small %u "
+                         "capssa profile  round %u depth %llu: pairs %u tiny %u+%u small %u "
                          "medium %u deep %u big %u (%u suffixes)\n",
                          c.stats.refine_rounds + 1, (unsigned long long)h, cnt[L_PAIR],
-                         cnt[L_TINY], cnt[L_SMALL], cnt[L_MEDIUM], cnt[L_DEEP], nb, big_total);
+                         cnt[L_TINY], cnt[L_TINY8], cnt[L_SMALL], cnt[L_MEDIUM], cnt[L_DEEP],
+                         nb, big_total);
         if (!any && !nb) break;
         if (c.stats.refine_rounds >= 70)
             return set_err(c, CAPSSA_EINVAL, "rank doubling did not converge");
@@ -1369,6 +1538,7 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
             ranks_ready = true;
         }
         uint32_t *rk = ranks_ready ? rank : nullptr;
+        kt.start(c.stream);
         for (int l = 0; l < kLists; l++)
             CAPSSA_CUDA(c, cudaMemsetAsync(&G.ctr->n[l][nxt], 0, 4, c.stream));
         CAPSSA_CUDA(c, cudaMemsetAsync(&G.ctr->big_packed[nxt], 0, 8, c.stream));
@@ -1376,22 +1546,33 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
             direct_pair_kernel<<<grid_for(cnt[L_PAIR], 256), 256, 0, c.stream>>>(
                 G.list[L_PAIR][cur], cnt[L_PAIR], sa, hd, rk, a.lim, P, lf, G, nxt);
             CAPSSA_LAUNCHED(c);
+            kt.mark(c.stream, "pair");
         }
         if (cnt[L_TINY]) {
-            direct_tiny_kernel<<<grid_for(cnt[L_TINY], 128), 128, 0, c.stream>>>(
+            direct_tiny_kernel<kTiny4><<<grid_for(cnt[L_TINY], 128), 128, 0, c.stream>>>(
                 G.list[L_TINY][cur], cnt[L_TINY], sa, hd, rk, a.lim, P, lf, G, nxt);
             CAPSSA_LAUNCHED(c);
+            kt.mark(c.stream, "tiny3-4");
+        }
+        if (cnt[L_TINY8]) {
+            direct_tiny_seg_kernel<kTinyMax>
+                <<<grid_for((uint64_t)cnt[L_TINY8] * kTinyMax, 128), 128, 0, c.stream>>>(
+                    G.list[L_TINY8][cur], cnt[L_TINY8], sa, hd, rk, a.lim, P, lf, G, nxt);
+            CAPSSA_LAUNCHED(c);
+            kt.mark(c.stream, "tiny5-8");
         }
         if (cnt[L_SMALL]) {
             direct_warp_kernel<<<grid_for((uint64_t)cnt[L_SMALL] * 32, 128), 128, 0, c.stream>>>(
                 G.list[L_SMALL][cur], cnt[L_SMALL], sa, hd, rk, a.lim, P, lf, G, nxt);
             CAPSSA_LAUNCHED(c);
+            kt.mark(c.stream, "small");
         }
         if (cnt[L_MEDIUM]) {
             direct_medium_kernel<<<std::min<unsigned>(cnt[L_MEDIUM], c.sm_count * 8), kMedThreads,
                                    0, c.stream>>>(G.list[L_MEDIUM][cur], cnt[L_MEDIUM], sa, hd,
                                                   rk, a.lim, P, lf, G, nxt);
             CAPSSA_LAUNCHED(c);
+            kt.mark(c.stream, "medium");
         }
         // rank doubling last: the direct kernels above rewrote the ranks of
         // every group they resolved, which only refines them (equal ranks
@@ -1404,6 +1585,7 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
             sort_small_kernel<<<grid_for(cnt[L_DEEP], 128), 128, 0, c.stream>>>(
                 G.list[L_DEEP][cur], cnt[L_DEEP], sa, key2, hd, rank, lf, empty, 2 * h, G, nxt);
             CAPSSA_LAUNCHED(c);
+            kt.mark(c.stream, "deep");
         }
         const int ord_bits = nb > 1 ? bits_for(nb - 1) : 1;
         if (nb) {
@@ -1421,7 +1603,9 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
                 tk, tv, big_total, G.big[cur], nb, k2bits, sa, hd, rank, lf, empty, 2 * h, G,
                 nxt);
             CAPSSA_LAUNCHED(c);
+            kt.mark(c.stream, "big");
         }
+        kt.print();
         c.stats.refined_suffixes += big_total;
         h *= 2;
         cur = nxt;
