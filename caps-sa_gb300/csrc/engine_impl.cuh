@@ -332,19 +332,58 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *excl) 
     return total;
 }
 
+// Exclusive block-wide prefix of one u64 per thread (used for several
+// 16-bit counters packed in one word); returns the block total.
+__device__ __forceinline__ uint64_t block_excl_scan64(uint64_t v, uint64_t *excl) {
+    __shared__ uint64_t s_w64[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_w64[warp] = x;
+    __syncthreads();
+    uint64_t before = 0, total = 0;
+    for (int w = 0; w < nw; w++) {
+        uint64_t t = s_w64[w];
+        if (w < warp) before += t;
+        total += t;
+    }
+    __syncthreads();
+    *excl = before + x - v;
+    return total;
+}
+
 constexpr int kInitPer = 16;  // sorted keys per thread in init_groups_kernel
+constexpr int kInitTile = 256 * kInitPer;
 
 // Group heads after the key sort, in SA order (hd[i] = first SA index of
 // i's group; equal heads == equal comparison so far); tied groups that need
 // more symbols become the first round's work (engine.cuh step 3 -> 4).
-// A block covers 256 * kInitPer keys and appends its groups with one
-// atomic per list.
+// A block stages its 256 * kInitPer sorted keys (and their neighbours) in
+// shared memory once, unpacks the positions when they ride below the keys,
+// and appends its groups with one atomic per list (per-list counts packed
+// as 16-bit fields, 4096 keys per block at most).
 __global__ void __launch_bounds__(256)
     init_groups_kernel(const uint64_t *__restrict__ keys, uint32_t n, int k, uint64_t lmask,
                        int lf, int flag_len, int vshift, uint32_t *__restrict__ hd,
                        uint32_t *__restrict__ sa_out, GroupLists G) {
-    const uint32_t base = blockIdx.x * (256u * kInitPer);
+    static_assert(kLists <= 8, "two packed words of four 16-bit counters");
+    __shared__ uint64_t sk[kInitTile + 2];  // sk[l + 1] = key of sorted index base + l
+    __shared__ uint32_t s_base[kLists];
+    const uint32_t base = blockIdx.x * (uint32_t)kInitTile;
+    const uint32_t valid = n - base < (uint32_t)kInitTile ? n - base : (uint32_t)kInitTile;
     const uint64_t vmask = (1ull << vshift) - 1;
+    for (uint32_t l = threadIdx.x; l < valid; l += 256) {
+        const uint64_t item = keys[base + l];
+        sk[l + 1] = item >> vshift;
+        if (sa_out) sa_out[base + l] = (uint32_t)(item & vmask);
+    }
+    if (threadIdx.x == 0) sk[0] = base > 0 ? keys[base - 1] >> vshift : 0ull;
+    if (threadIdx.x == 32) sk[valid + 1] = base + valid < n ? keys[base + valid] >> vshift : 0ull;
+    __syncthreads();
     // tie state of a key: complete (equal through both ends: nothing to
     // refine), and the depth its group's members are known to agree on
     // (0 for the early-ended suffixes of a flagged plain text)
@@ -359,61 +398,81 @@ __global__ void __launch_bounds__(256)
             depth = (uint64_t)k;
         }
     };
-    uint32_t cnt[kLists] = {};
-    // pass 1: heads (and positions), and how many groups of each list this
-    // thread ends
+    // first sorted index of the run of `key` that holds local index l
+    auto head_of = [&](uint32_t l, uint64_t key) -> uint32_t {
+        uint32_t m = l;
+        int steps = 0;
+        while (m > 0 && steps < 32 && sk[m] == key) {  // sk[m] = key of local m - 1
+            m--;
+            steps++;
+        }
+        if (steps < 32 && (m > 0 || base == 0 || sk[0] != key)) return base + m;
+        return run_head(keys, 0, base + m, key, vshift);  // long run or one that began earlier
+    };
+    uint64_t cnt_lo = 0, cnt_hi = 0;  // 16-bit counts: lists 0..3, lists 4..
+    // pass 1: heads, and how many groups of each list this thread ends
 #pragma unroll 4
     for (int j = 0; j < kInitPer; j++) {
-        const uint32_t i = base + j * 256 + threadIdx.x;
-        if (i >= n) break;
-        const uint64_t item = keys[i];
-        const uint64_t key = item >> vshift;
-        if (sa_out) sa_out[i] = (uint32_t)(item & vmask);
-        bool head = (i == 0) || (keys[i - 1] >> vshift) != key;
-        uint32_t g = head ? i : run_head(keys, 0, i, key, vshift);
-        bool last = (i == n - 1) || (keys[i + 1] >> vshift) != key;
+        const uint32_t l = j * 256 + threadIdx.x;
+        if (l >= valid) break;
+        const uint32_t i = base + l;
+        const uint64_t key = sk[l + 1];
+        const bool head = (i == 0) || sk[l] != key;
+        const uint32_t g = head ? i : head_of(l, key);
+        const bool last = (i == n - 1) || sk[l + 2] != key;
         bool complete;
         uint64_t depth;
         state(key, complete, depth);
         hd[i] = (complete && lf) ? i : g;
         if (!complete && last && i > g) {
-            int l = list_of(i - g + 1, depth);
-            if (l == kLists)
+            const int li = list_of(i - g + 1, depth);
+            if (li == kLists)
                 append_big(G, 0, g, i - g + 1);
-#pragma unroll
-            for (int q = 0; q < kLists; q++) cnt[q] += l == q ? 1u : 0u;
+            else if (li < 4)
+                cnt_lo += 1ull << (16 * li);
+            else
+                cnt_hi += 1ull << (16 * (li - 4));
         }
     }
-    __shared__ uint32_t s_base[kLists];
-    uint32_t off[kLists];
-#pragma unroll
-    for (int l = 0; l < kLists; l++) {
-        uint32_t total = block_excl_scan(cnt[l], &off[l]);
-        if (threadIdx.x == 0 && total) s_base[l] = atomicAdd(&G.ctr->n[l][0], total);
+    uint64_t off_lo, off_hi;
+    const uint64_t tot_lo = block_excl_scan64(cnt_lo, &off_lo);
+    const uint64_t tot_hi = block_excl_scan64(cnt_hi, &off_hi);
+    if (threadIdx.x < kLists) {
+        const int li = (int)threadIdx.x;
+        const uint32_t total =
+            (uint32_t)(((li < 4 ? tot_lo : tot_hi) >> (16 * (li & 3))) & 0xFFFFu);
+        if (total) s_base[li] = atomicAdd(&G.ctr->n[li][0], total);
     }
     __syncthreads();
-    // pass 2: write the entries (keys are in L1/L2 from pass 1)
+    // pass 2: write the entries
 #pragma unroll 4
     for (int j = 0; j < kInitPer; j++) {
-        const uint32_t i = base + j * 256 + threadIdx.x;
-        if (i >= n) break;
-        const uint64_t key = keys[i] >> vshift;
-        bool last = (i == n - 1) || (keys[i + 1] >> vshift) != key;
+        const uint32_t l = j * 256 + threadIdx.x;
+        if (l >= valid) break;
+        const uint32_t i = base + l;
+        const uint64_t key = sk[l + 1];
+        const bool last = (i == n - 1) || sk[l + 2] != key;
         if (!last) continue;
         bool complete;
         uint64_t depth;
         state(key, complete, depth);
         if (complete) continue;
-        bool head = (i == 0) || (keys[i - 1] >> vshift) != key;
+        const bool head = (i == 0) || sk[l] != key;
         if (head) continue;
-        uint32_t g = run_head(keys, 0, i, key, vshift);
-        int l = list_of(i - g + 1, depth);
-        if (l == kLists) continue;
+        const uint32_t g = head_of(l, key);
+        const int li = list_of(i - g + 1, depth);
+        if (li == kLists) continue;
         uint32_t slot = 0;
 #pragma unroll
-        for (int q = 0; q < kLists; q++)
-            if (l == q) slot = s_base[q] + off[q]++;
-        list_ptr(G, l, 0)[slot] = group_entry(g, i - g + 1, depth);
+        for (int q = 0; q < kLists; q++) {
+            if (li == q) {
+                uint64_t &off = q < 4 ? off_lo : off_hi;
+                const int sh = 16 * (q & 3);
+                slot = s_base[q] + (uint32_t)((off >> sh) & 0xFFFFu);
+                off += 1ull << sh;
+            }
+        }
+        list_ptr(G, li, 0)[slot] = group_entry(g, i - g + 1, depth);
     }
 }
 
@@ -1497,7 +1556,7 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
     G.big[1] = G.big[0] + big_cap;
     uint64_t h = (uint64_t)geo.k;
     CAPSSA_CUDA(c, cudaMemsetAsync(G.ctr, 0, sizeof(Counters), c.stream));
-    init_groups_kernel<<<grid_for(n, 256 * kInitPer), 256, 0, c.stream>>>(
+    init_groups_kernel<<<grid_for(n, kInitTile), 256, 0, c.stream>>>(
         skeys, nn, geo.k, (1ull << geo.lbits) - 1, lf, geo.flag_len, vbits, hd,
         vbits ? sa : nullptr, G);
     CAPSSA_LAUNCHED(c);
