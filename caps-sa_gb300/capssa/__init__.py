@@ -73,6 +73,9 @@ class BoundaryRank(enum.IntEnum):
     LONGER_FIRST = 1
 
 
+CDF_PARAMS = 257  # CAPSSA_CDF_PARAMS
+
+
 class Partition(enum.IntEnum):
     AUTO = 0
     SPLITTERS = 1
@@ -87,7 +90,10 @@ class _Limits(C.Structure):
 class _Opts(C.Structure):
     _fields_ = [("max_context", C.c_uint64), ("subproblem_count", C.c_uint64),
                 ("partition", C.c_int32), ("host_threads", C.c_int32),
-                ("reserved", C.c_uint64 * 6)]
+                ("flags", C.c_uint64), ("reserved", C.c_uint64 * 5)]
+
+
+FLAG_BUCKET_FRONT = 1
 
 
 class _Stats(C.Structure):
@@ -100,7 +106,9 @@ class _Stats(C.Structure):
                 ("d2h_bytes", C.c_uint64), ("keys_ms", C.c_double), ("sort_ms", C.c_double),
                 ("refine_ms", C.c_double), ("finish_ms", C.c_double),
                 ("sort_passes", C.c_uint32), ("sort_item_bytes", C.c_uint32),
-                ("sort_pass_ms", C.c_double)]
+                ("sort_pass_ms", C.c_double), ("partition_ms", C.c_double),
+                ("train_ms", C.c_double), ("partition_probes", C.c_uint64),
+                ("train_samples", C.c_uint32), ("model_loss", C.c_float)]
 
 
 class _Packer(C.Structure):
@@ -128,6 +136,8 @@ def _load():
     L.capssa_ctx_workspace_bytes.argtypes = [vp]
     L.capssa_ctx_workspace_bytes.restype = u64
     L.capssa_ctx_trim.argtypes = [vp]
+    L.capssa_cdf_grad.argtypes = [vp, vp, vp, vp, u64, vp, vp]
+    L.capssa_cdf_train.argtypes = [vp, vp, vp, u64, i32, vp, vp]
     L.capssa_ctx_set_stream.argtypes = [vp, vp]
     L.capssa_opts_default.argtypes = [C.POINTER(_Opts)]
     for s in ("u8", "u16", "u32"):
@@ -147,6 +157,8 @@ def _load():
         getattr(L, "capssa_build_in_memory_sample_sort_for_positions_%s" % s).argtypes = [
             vp, vp, u64, vp, u64, C.POINTER(_Limits), C.POINTER(_Opts), EMIT_FN, vp]
         getattr(L, "capssa_lcp_%s" % s).argtypes = [vp, vp, u64, vp, vp, u64, u64, vp]
+        getattr(L, "capssa_sample_sort_plan_%s" % s).argtypes = [
+            vp, vp, u64, vp, u64, C.POINTER(_Limits), C.POINTER(_Opts), vp, vp, vp]
         getattr(L, "capssa_suffix_cmp_%s" % s).argtypes = [
             vp, vp, u64, C.POINTER(_Limits), vp, vp, u64, u64, vp]
     L.capssa_pack_params_u8.argtypes = [vp, vp, u64, i32, u64, C.POINTER(_Packer),
@@ -215,8 +227,10 @@ class SegmentedText:
 
 @dataclass
 class Opts:
-    """src/sample_sort.rs:70-85."""
+    """src/sample_sort.rs:70-85.  bucket_front: sort through the 16-bit bucket
+    front end (same output; CAPSSA_FLAG_BUCKET_FRONT)."""
     max_context: int = UNBOUNDED
+    bucket_front: bool = False
 
 
 @dataclass
@@ -226,6 +240,7 @@ class ExtMemOpts:
     subproblem_count: int = 0
     partition: Partition = Partition.AUTO
     host_threads: int = 0
+    bucket_front: bool = False
 
 
 def _copts(o) -> _Opts:
@@ -236,6 +251,7 @@ def _copts(o) -> _Opts:
         c.subproblem_count = int(getattr(o, "subproblem_count", 0))
         c.partition = int(getattr(o, "partition", 0))
         c.host_threads = int(getattr(o, "host_threads", 0))
+        c.flags = FLAG_BUCKET_FRONT if getattr(o, "bucket_front", False) else 0
     return c
 
 
@@ -420,6 +436,50 @@ class Context:
             return np.concatenate(chunks) if chunks else np.zeros(0, dtype=np.uint64)
         self.try_build_in_memory_sample_sort(text, opts, emit, lp, positions)
         return None
+
+    def sample_sort_plan(self, text, opts=None, lp=None, positions=None):
+        """The partition plan of build_in_memory_sample_sort (phases 1-3,
+        src/ext_mem.rs:1191-1428): (p, pivots[p-1], partition sizes[p]).  With
+        ExtMemOpts(partition=Partition.LEARNED) the partition comes from the
+        learned CDF model with neighbour fixup (same plan)."""
+        text, tp, n, s = _text(text)
+        lim = (lp or PlainText(n))._c()
+        o = _copts(opts)
+        fn = getattr(lib, "capssa_sample_sort_plan_%s" % s)
+        pp, m = None, 0
+        if positions is not None:
+            pos = np.ascontiguousarray(positions, dtype=np.uint64)
+            pp, m = pos.ctypes.data, len(pos)
+        p = C.c_uint64(0)
+        self._check(fn(self._h, tp, n, pp, m, C.byref(lim), C.byref(o), C.byref(p), None, None))
+        pv = np.zeros(max(int(p.value) - 1, 0) + 1, dtype=np.uint64)
+        sz = np.zeros(max(int(p.value), 1), dtype=np.uint64)
+        self._check(fn(self._h, tp, n, pp, m, C.byref(lim), C.byref(o), C.byref(p),
+                       pv.ctypes.data, sz.ctypes.data))
+        k = int(p.value)
+        return k, pv[:max(k - 1, 0)], sz[:k]
+
+    def cdf_grad(self, params, prefixes, targets):
+        """(mean squared error, gradient) of the learned CDF model over the
+        samples, from the GPU forward/backward kernels."""
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        x = np.ascontiguousarray(prefixes, dtype=np.uint64)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        g = np.zeros(CDF_PARAMS, dtype=np.float32)
+        loss = C.c_float(0)
+        self._check(lib.capssa_cdf_grad(self._h, params.ctypes.data, x.ctypes.data,
+                                        t.ctypes.data, len(x), g.ctypes.data, C.byref(loss)))
+        return float(loss.value), g
+
+    def cdf_train(self, prefixes, targets, steps=300):
+        """(trained parameters, final loss) after `steps` Adam steps on the GPU."""
+        x = np.ascontiguousarray(prefixes, dtype=np.uint64)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        params = np.zeros(CDF_PARAMS, dtype=np.float32)
+        loss = C.c_float(0)
+        self._check(lib.capssa_cdf_train(self._h, x.ctypes.data, t.ctypes.data, len(x),
+                                         int(steps), params.ctypes.data, C.byref(loss)))
+        return params, float(loss.value)
 
     def build_batched(self, texts, offsets, index=np.uint32, opts=None):
         """Many independent texts: out[offsets[t]:offsets[t+1]] is the SA of

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "cdf.cuh"
 #include "engine.cuh"
 #include "lcp.cuh"
 #include "radix.cuh"
@@ -268,11 +269,21 @@ capssa_status stage_text(Ctx &c, const ST *text, uint64_t n, void **d_text) {
     return stage_in(c, WS_TEXT, text, n * sizeof(ST), 64 + sizeof(ST) * 8, d_text);
 }
 
+// The sample sort's partition plan, requested from a build (see
+// capssa_sample_sort_plan_*).
+struct PartRequest {
+    uint32_t p;
+    int mode;
+    uint64_t *pivots;  // host, p - 1
+    uint64_t *sizes;   // host, p
+};
+
 // Every builder funnels through here.
 template <typename ST>
 capssa_status build_common(Ctx &c, const ST *text, uint64_t n, const void *positions,
                            int pos_bytes, uint64_t m, const capssa_limits *lp,
-                           const capssa_opts *opts, void *out_sa, int out_bytes, void *out_lcp) {
+                           const capssa_opts *opts, void *out_sa, int out_bytes, void *out_lcp,
+                           const PartRequest *part = nullptr) {
     if (!text && n) return set_err(c, CAPSSA_EINVAL, "null text");
     if (!out_sa && (positions ? m : n)) return set_err(c, CAPSSA_EINVAL, "null output");
     if (out_bytes == 4 && n > 0xFFFFFFFFull)
@@ -314,7 +325,13 @@ capssa_status build_common(Ctx &c, const ST *text, uint64_t n, const void *posit
     a.out_sa = d_out;
     a.out_bytes = out_bytes;
     a.out_lcp = d_lcp;
-    a.bucket_front = opts && opts->partition != CAPSSA_PARTITION_AUTO ? 1 : 0;
+    a.bucket_front = opts && (opts->flags & CAPSSA_FLAG_BUCKET_FRONT) ? 1 : 0;
+    if (part) {
+        a.part_p = part->p;
+        a.part_mode = part->mode;
+        a.part_pivots = part->pivots;
+        a.part_sizes = part->sizes;
+    }
     if (positions && m == 0) return CAPSSA_OK;
     s = engine_build(c, a);
     if (s != CAPSSA_OK) return s;
@@ -358,9 +375,13 @@ capssa_status sample_sort_common(Ctx &c, const ST *text, uint64_t n, const uint6
     if (count == 0) return CAPSSA_OK;
     uint64_t *d_sa = (uint64_t *)ws_get(c, WS_OUT, count * 8 + 64);
     if (!d_sa) return set_err(c, CAPSSA_ENOMEM, "output buffer");
-    c.stats.partitions = (uint32_t)effective_p(count, opts ? opts->subproblem_count : 0,
-                                               opts ? opts->host_threads : 0);
-    capssa_status s = build_common<ST>(c, text, n, positions, 8, m, lp, opts, d_sa, 8, nullptr);
+    PartRequest pr{(uint32_t)effective_p(count, opts ? opts->subproblem_count : 0,
+                                         opts ? opts->host_threads : 0),
+                   opts && opts->partition == CAPSSA_PARTITION_LEARNED ? CAPSSA_PARTITION_LEARNED
+                                                                       : CAPSSA_PARTITION_SPLITTERS,
+                   nullptr, nullptr};
+    capssa_status s =
+        build_common<ST>(c, text, n, positions, 8, m, lp, opts, d_sa, 8, nullptr, &pr);
     if (s != CAPSSA_OK) return s;
     const uint64_t batch = 1u << 22;  // 4 Mi positions (32 MiB) per emit
     uint64_t *h = nullptr;
@@ -670,6 +691,16 @@ uint64_t capssa_ctx_workspace_bytes(const capssa_ctx *ctx) {
 #define DEFINE_FOR_S(S, ST)                                                                   \
     DEFINE_FOR_I(S, ST, u32, uint32_t, 4)                                                     \
     DEFINE_FOR_I(S, ST, u64, uint64_t, 8)                                                     \
+    capssa_status capssa_sample_sort_plan_##S(capssa_ctx *ctx, const ST *text, uint64_t n,    \
+                                              const uint64_t *positions, uint64_t m,          \
+                                              const capssa_limits *lp,                        \
+                                              const capssa_opts *opts, uint64_t *p_out,       \
+                                              uint64_t *pivots, uint64_t *sizes) {            \
+        CTX_OR_EINVAL(ctx);                                                                   \
+        if (positions == nullptr && m) return scope.finish(set_err(c, CAPSSA_EINVAL, "null positions")); \
+        return scope.finish(plan_common<ST>(c, text, n, positions, m, lp, opts, p_out, pivots, \
+                                            sizes));                                          \
+    }                                                                                         \
     capssa_status capssa_build_in_memory_sample_sort_##S(                                     \
         capssa_ctx *ctx, const ST *text, uint64_t n, const capssa_limits *lp,                 \
         const capssa_opts *opts, capssa_emit_fn emit, void *user) {                           \
@@ -802,9 +833,84 @@ capssa_status pairs_common(Ctx &c, const ST *text, uint64_t n, const capssa_limi
 }  // namespace capssa
 
 extern "C" {
+}  // extern "C"
+
+namespace capssa {
+namespace {
+
+// capssa_sample_sort_plan_*: p, and with output arrays the pivots and the
+// partition sizes of the sample sort's plan.
+template <typename ST>
+capssa_status plan_common(Ctx &c, const ST *text, uint64_t n, const uint64_t *positions,
+                          uint64_t m, const capssa_limits *lp, const capssa_opts *opts,
+                          uint64_t *p_out, uint64_t *pivots, uint64_t *sizes) {
+    const uint64_t count = positions ? m : n;
+    const uint64_t p =
+        effective_p(count, opts ? opts->subproblem_count : 0, opts ? opts->host_threads : 0);
+    if (p_out) *p_out = p;
+    if (!pivots || !sizes || count == 0) return CAPSSA_OK;
+    if (p > 0xFFFFFFFFull) return set_err(c, CAPSSA_EUNSUPPORTED, "more than 2^32-1 subproblems");
+    uint64_t *d_sa = (uint64_t *)ws_get(c, WS_OUT, count * 8 + 64);
+    if (!d_sa) return set_err(c, CAPSSA_ENOMEM, "output buffer");
+    PartRequest pr{(uint32_t)p,
+                   opts && opts->partition == CAPSSA_PARTITION_LEARNED ? CAPSSA_PARTITION_LEARNED
+                                                                       : CAPSSA_PARTITION_SPLITTERS,
+                   pivots, sizes};
+    return build_common<ST>(c, text, n, positions, 8, m, lp, opts, d_sa, 8, nullptr, &pr);
+}
+
+}  // namespace
+}  // namespace capssa
+
+extern "C" {
+
 DEFINE_FOR_S(u8, uint8_t)
 DEFINE_FOR_S(u16, uint16_t)
 DEFINE_FOR_S(u32, uint32_t)
+
+capssa_status capssa_cdf_grad(capssa_ctx *ctx, const float *params, const uint64_t *prefixes,
+                              const float *targets, uint64_t n, float *grad, float *loss) {
+    CTX_OR_EINVAL(ctx);
+    if (!params || !grad || !loss || (n && (!prefixes || !targets)))
+        return scope.finish(set_err(c, CAPSSA_EINVAL, "null model buffer"));
+    if (n > 0xFFFFFFFFull) return scope.finish(set_err(c, CAPSSA_EUNSUPPORTED, "2^32 samples"));
+    void *dp = nullptr, *dx = nullptr, *dt = nullptr;
+    capssa_status s = stage_in(c, WS_MISC, params, cdf::kParams * 4, 64, &dp);
+    if (s == CAPSSA_OK) s = stage_in(c, WS_MISC2, prefixes, n * 8, 64, &dx);
+    if (s == CAPSSA_OK) s = stage_in(c, WS_MISC3, targets, n * 4, 64, &dt);
+    if (s != CAPSSA_OK) return scope.finish(s);
+    float *dg = (float *)ws_get(c, WS_OUT2, (cdf::kParams + 1) * 4 + 64);
+    if (!dg) return scope.finish(set_err(c, CAPSSA_ENOMEM, "gradient buffer"));
+    if (cudaMemsetAsync(dg, 0, (cdf::kParams + 1) * 4, c.stream) != cudaSuccess)
+        return scope.finish(set_err(c, CAPSSA_ECUDA, "gradient clear"));
+    s = cdf::grad(c, (const float *)dp, (const uint64_t *)dx, (const float *)dt, (uint32_t)n, dg,
+                  dg + cdf::kParams);
+    if (s == CAPSSA_OK) s = stage_out(c, grad, dg, cdf::kParams * 4);
+    float lsum = 0.0f;
+    if (s == CAPSSA_OK) s = stage_out(c, &lsum, dg + cdf::kParams, 4);
+    if (s == CAPSSA_OK) *loss = n ? lsum / (float)n : 0.0f;
+    return scope.finish(s);
+}
+
+capssa_status capssa_cdf_train(capssa_ctx *ctx, const uint64_t *prefixes, const float *targets,
+                               uint64_t n, int32_t steps, float *params, float *loss) {
+    CTX_OR_EINVAL(ctx);
+    if (!params || !loss || (n && (!prefixes || !targets)) || steps < 0)
+        return scope.finish(set_err(c, CAPSSA_EINVAL, "bad model training arguments"));
+    if (n > 0xFFFFFFFFull) return scope.finish(set_err(c, CAPSSA_EUNSUPPORTED, "2^32 samples"));
+    void *dx = nullptr, *dt = nullptr;
+    capssa_status s = stage_in(c, WS_MISC2, prefixes, n * 8, 64, &dx);
+    if (s == CAPSSA_OK) s = stage_in(c, WS_MISC3, targets, n * 4, 64, &dt);
+    if (s != CAPSSA_OK) return scope.finish(s);
+    float *dp = (float *)ws_get(c, WS_OUT2, cdf::kParams * 6 + 64);
+    if (!dp) return scope.finish(set_err(c, CAPSSA_ENOMEM, "model buffer"));
+    float fl = 0.0f;
+    s = cdf::train(c, (const uint64_t *)dx, (const float *)dt, (uint32_t)n, steps, dp,
+                   (__nv_bfloat16 *)(dp + cdf::kParams + 3), &fl);
+    if (s == CAPSSA_OK) s = stage_out(c, params, dp, cdf::kParams * 4);
+    if (s == CAPSSA_OK) *loss = fl;
+    return scope.finish(s);
+}
 
 // Packer::new + seed_params (src/pack.rs:103-176, 217-234): the byte
 // presence scan runs on the device, the 256-entry map on the host.

@@ -41,6 +41,12 @@ struct EngineArgs {
     int out_bytes;         // 4 or 8
     void *out_lcp;         // device or nullptr
     int bucket_front;      // 1: bucket the keys by their top 16 bits first (bucket.cuh)
+    // sample-sort partition plan (build_in_memory_sample_sort's phases 1-3,
+    // src/ext_mem.rs:1191-1428), computed after the sort when part_p > 0
+    uint32_t part_p;         // subproblems
+    int part_mode;           // CAPSSA_PARTITION_SPLITTERS or CAPSSA_PARTITION_LEARNED
+    uint64_t *part_pivots;   // host, part_p - 1 entries (out) or nullptr
+    uint64_t *part_sizes;    // host, part_p entries (out) or nullptr
 };
 
 // Runs the whole sort; all buffers are device buffers.

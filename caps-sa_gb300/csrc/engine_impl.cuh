@@ -11,6 +11,7 @@
 
 #include "engine.cuh"
 #include "bucket.cuh"
+#include "cdf.cuh"
 #include "lcp.cuh"
 #include "radix.cuh"
 #include "scan.cuh"
@@ -1345,6 +1346,199 @@ __global__ void subset_isa_key_kernel(const PT *__restrict__ pos, uint64_t m, ui
     }
 }
 
+// ---------------------------------------------------------------- sample-sort partition
+
+// suffix_cmp_with (src/lcp.rs:184-201) of suffixes a and b with limits la,
+// lb and max_context, from their first packed windows xa, xb and, when
+// those do not decide, direct comparison on the packed text.  -1 / 0 / 1.
+__device__ __forceinline__ int suffix_cmp_full(const Packed &P, uint64_t a, uint64_t la,
+                                               uint64_t xa, uint64_t b, uint64_t lb,
+                                               uint64_t xb, uint64_t max_ctx, int lf) {
+    uint64_t lim = la < lb ? la : lb;
+    lim = lim < max_ctx ? lim : max_ctx;
+    const uint64_t x = xa ^ xb;
+    if (x) {
+        const uint64_t d = (uint64_t)__clzll((long long)x) / (uint64_t)P.b;
+        if (d < lim) return xa < xb ? -1 : 1;
+    }
+    int r = direct_cmp(P, a, la, b, lb, 0, max_ctx, lf);
+    if (r == 2) {  // equal through max_context: boundary order on the full limits
+        if (!lf)
+            r = (la > lb) - (la < lb);
+        else
+            r = la != lb ? (lb > la) - (lb < la) : (a > b) - (a < b);
+    }
+    return r;
+}
+
+// Chunk-major order of the sorted suffixes (full text): key = chunk of the
+// position, value = the position, in SA order (a stable sort by the key then
+// lists every chunk's positions in sorted order).
+__global__ void chunk_key_kernel(const uint32_t *__restrict__ sa, uint32_t n, uint32_t chunk,
+                                 uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t p = sa[j];
+        keys[j] = p / chunk;
+        vals[j] = p;
+    }
+}
+
+// Subsets: key = (chunk of the input index, rank of the suffix), value =
+// the position.
+template <typename PT>
+__global__ void chunk_key_subset_kernel(const PT *__restrict__ pos, uint64_t m, uint64_t n,
+                                        uint32_t chunk, const uint32_t *__restrict__ isa, int lf,
+                                        int rbits, uint64_t *__restrict__ keys,
+                                        uint32_t *__restrict__ vals) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t p = (uint64_t)pos[i];
+        const uint64_t rk = p >= n ? (lf ? n + 1 : 0ull) : (uint64_t)__ldg(isa + p) + 1;
+        keys[i] = ((i / chunk) << rbits) | rk;
+        vals[i] = (uint32_t)p;
+    }
+}
+
+// Evenly spaced midpoints of every sorted chunk (evenly_spaced,
+// src/ext_mem.rs:1291-1305), with each sample's rank key.
+__global__ void sample_kernel(const uint32_t *__restrict__ chunked, uint64_t m, uint32_t chunk,
+                              uint32_t p, uint32_t per, const uint32_t *__restrict__ soff,
+                              uint64_t n, const uint32_t *__restrict__ isa, int lf,
+                              uint64_t *__restrict__ skey, uint32_t *__restrict__ spos) {
+    const uint64_t total = (uint64_t)p * per;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = (uint32_t)(t / per), sidx = (uint32_t)(t % per);
+        const uint64_t start = (uint64_t)i * chunk;
+        if (start >= m) continue;
+        const uint64_t len = m - start < chunk ? m - start : chunk;
+        const uint64_t cnt = per < len ? per : len;
+        if (sidx >= cnt) continue;
+        const uint64_t at = cnt >= len ? sidx : (2 * (uint64_t)sidx + 1) * len / (2 * cnt);
+        const uint32_t q = chunked[start + at];
+        const uint32_t o = soff[i] + sidx;
+        spos[o] = q;
+        skey[o] = q >= n ? (lf ? n + 1 : 0ull) : (uint64_t)__ldg(isa + q) + 1;
+    }
+}
+
+// Pivots samples[j * ns / p] (phase 2, src/ext_mem.rs:1309-1342) with their
+// limits and first windows.
+__global__ void pivot_kernel(const uint32_t *__restrict__ sorted_samples, uint32_t ns, uint32_t p,
+                             Packed P, DevLimits L, uint32_t *__restrict__ piv_pos,
+                             uint64_t *__restrict__ piv_lim, uint64_t *__restrict__ piv_x) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j + 1 < p;
+         j += gridDim.x * blockDim.x) {
+        const uint32_t q = sorted_samples[(uint64_t)(j + 1) * ns / p];
+        piv_pos[j] = q;
+        piv_lim[j] = dev_lim_at(L, q);
+        piv_x[j] = window_at(P, q);
+    }
+}
+
+// Training set of the learned CDF model: every stride-th sorted sample,
+// its packed prefix and its rank fraction among all ns samples.
+__global__ void train_set_kernel(const uint32_t *__restrict__ sorted_samples, uint32_t ns,
+                                 uint32_t stride, uint32_t tn, Packed P,
+                                 uint64_t *__restrict__ x, float *__restrict__ t) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < tn; j += gridDim.x * blockDim.x) {
+        const uint32_t q = j * stride;
+        x[j] = window_at(P, sorted_samples[q]);
+        t[j] = ((float)q + 0.5f) / (float)ns;
+    }
+}
+
+// Partition of every suffix (phase 3, src/ext_mem.rs:1361-1428, with
+// upper_bound_by_pivot :1705-1734): b = the number of pivots that compare
+// less than the suffix.  SPLITTERS: binary search over the pivots.
+// LEARNED: the CDF model predicts b from the suffix's packed prefix; the
+// prediction is checked against its two neighbouring pivots and moved until
+// both hold.  The suffixes come in sorted order, so b must never decrease
+// along them (checked by the caller).  Pivot windows and the bucket
+// histogram live in shared memory when they fit (SMEM).
+template <bool LEARNED, bool SMEM>
+__global__ void __launch_bounds__(256)
+    partition_kernel(const uint32_t *__restrict__ sorted, uint32_t m, Packed P, DevLimits L,
+                     int lf, uint64_t max_ctx, const uint32_t *__restrict__ piv_pos,
+                     const uint64_t *__restrict__ piv_lim, const uint64_t *__restrict__ piv_x,
+                     uint32_t n_piv, uint32_t p, const __nv_bfloat16 *__restrict__ w,
+                     uint32_t *__restrict__ bucket_of, unsigned long long *__restrict__ sizes,
+                     unsigned long long *__restrict__ stats) {
+    extern __shared__ __align__(16) unsigned char psm[];
+    uint64_t *sx = reinterpret_cast<uint64_t *>(psm);
+    uint32_t *hist = reinterpret_cast<uint32_t *>(sx + (SMEM ? n_piv : 0));
+    __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(hist + (SMEM ? p : 0));
+    if (SMEM) {
+        for (uint32_t j = threadIdx.x; j < n_piv; j += blockDim.x) sx[j] = piv_x[j];
+        for (uint32_t j = threadIdx.x; j < p; j += blockDim.x) hist[j] = 0;
+    }
+    if (LEARNED)
+        for (int j = threadIdx.x; j < cdf::kParams; j += blockDim.x) sw[j] = w[j];
+    __syncthreads();
+    const uint64_t *X = SMEM ? sx : piv_x;
+    unsigned long long probes = 0, mis = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        const uint32_t s = sorted[i];
+        const uint64_t ls = dev_lim_at(L, s);
+        const uint64_t xs = window_at(P, s);
+        // pivot j < suffix s
+        auto below = [&](uint32_t j) -> bool {
+            probes++;
+            return suffix_cmp_full(P, piv_pos[j], piv_lim[j], X[j], s, ls, xs, max_ctx, lf) < 0;
+        };
+        uint32_t b;
+        if (LEARNED) {
+            const float y = cdf::infer_bf16(sw, xs);
+            float g = floorf(y * (float)p);
+            g = g < 0.0f ? 0.0f : (g > (float)n_piv ? (float)n_piv : g);
+            b = (uint32_t)g;
+            const uint32_t guess = b;
+            while (b > 0 && !below(b - 1)) b--;
+            if (b == guess)
+                while (b < n_piv && below(b)) b++;
+            mis += b != guess ? 1u : 0u;
+        } else {
+            uint32_t lo = 0, hi = n_piv;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (below(mid))
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            b = lo;
+        }
+        if (SMEM)
+            atomicAdd(&hist[b], 1u);
+        else
+            atomicAdd(&sizes[b], 1ull);
+        bucket_of[i] = b;
+    }
+    // block sums of the probe and misprediction counts, then the histogram
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        probes += __shfl_xor_sync(0xffffffffu, probes, o);
+        mis += __shfl_xor_sync(0xffffffffu, mis, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&stats[0], probes);
+        atomicAdd(&stats[1], mis);
+    }
+    if (SMEM) {
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < p; j += blockDim.x)
+            if (hist[j]) atomicAdd(&sizes[j], (unsigned long long)hist[j]);
+    }
+}
+
+// Partitions along the sorted order never decrease (else flag).
+__global__ void partition_check_kernel(const uint32_t *__restrict__ bucket_of, uint32_t m,
+                                       int *__restrict__ bad) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + 1; i < m;
+         i += gridDim.x * blockDim.x)
+        if (bucket_of[i] < bucket_of[i - 1]) atomicExch(bad, 1);
+}
+
 }  // namespace eng
 
 // ---------------------------------------------------------------- host
@@ -1404,7 +1598,7 @@ inline int bits_for(uint64_t v) {  // bits to represent 0..v
 // Steps 1-4 of engine.cuh over every text position under the unbounded
 // comparator; *sa_out receives the device SA (n entries).
 template <typename S>
-capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
+capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Packed *pk_out) {
     using namespace eng;
     const uint64_t n = a.n;
     const int lf = a.lim.longer_first;
@@ -1692,6 +1886,7 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out) {
                      (unsigned long long)n, geo.k, geo.b, t01, t12, passes, pass_ms, t23,
                      c.stats.refine_rounds);
     *sa_out = sa;
+    *pk_out = P;
     return CAPSSA_OK;
 }
 
@@ -1762,6 +1957,193 @@ struct FinishTimer {
     }
 };
 
+// Sample-sort partition plan over the sorted suffixes `sorted` (m entries):
+// samples as the reference draws them (evenly spaced midpoints of every
+// chunk of the input order, each chunk sorted), pivots, then the partition
+// of every suffix by splitter search or by the learned CDF model with
+// neighbour fixup.  Outputs: a.part_pivots / a.part_sizes (host) and the
+// partition statistics.
+template <typename S>
+capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
+                              const uint32_t *sa_full, const uint32_t *sorted, uint64_t m) {
+    using namespace eng;
+    const uint64_t n = a.n;
+    const int lf = a.lim.longer_first;
+    const uint32_t p = a.part_p;
+    if (p == 0 || m == 0) return CAPSSA_OK;
+    const uint32_t chunk = (uint32_t)((m + p - 1) / p);
+    double ln_m = std::log((double)m);
+    if (ln_m < 1.0) ln_m = 1.0;
+    uint64_t total = (uint64_t)p * (uint64_t)std::ceil(4.0 * ln_m);
+    total = std::min<uint64_t>(std::max<uint64_t>(total, p), m);
+    const uint32_t per = (uint32_t)((total + p - 1) / p);
+    // scratch: chunk-major keys/values (ping-pong), samples, pivots, buckets
+    const size_t m8 = (size_t)m * 8 + 64, m4 = (size_t)m * 4 + 64;
+    char *w = (char *)ws_get(c, WS_PART, 2 * m8 + 3 * m4);
+    uint32_t *isa = (uint32_t *)ws_get(c, WS_RANK, (size_t)n * 4 + 64);
+    if (!w || !isa) return set_err(c, CAPSSA_ENOMEM, "partition workspace");
+    uint64_t *ka = (uint64_t *)w, *kb = (uint64_t *)(w + m8);
+    uint32_t *va = (uint32_t *)(w + 2 * m8), *vb = (uint32_t *)(w + 2 * m8 + m4);
+    uint32_t *bucket_of = (uint32_t *)(w + 2 * m8 + 2 * m4);
+    const bool subset = a.positions != nullptr;
+    if (!subset) {
+        isa_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa_full, (uint32_t)n, isa);
+        CAPSSA_LAUNCHED(c);
+    }  // (subsets: the caller's isa is already in place)
+    // 1. every chunk's positions in sorted order
+    const int cbits = bits_for(p > 1 ? p - 1 : 1);
+    bool in_b = false;
+    capssa_status s;
+    if (!subset) {
+        chunk_key_kernel<<<grid_for(m, 256), 256, 0, c.stream>>>(sa_full, (uint32_t)m, chunk, ka,
+                                                                 va);
+        CAPSSA_LAUNCHED(c);
+        s = radix::sort_pairs(c, ka, va, kb, vb, (uint32_t)m, 0, cbits, false, 0, &in_b);
+    } else {
+        const int rbits = bits_for(n + 1);
+        if (a.pos_bytes == 4)
+            chunk_key_subset_kernel<uint32_t><<<grid_for(m, 256), 256, 0, c.stream>>>(
+                (const uint32_t *)a.positions, m, n, chunk, isa, lf, rbits, ka, va);
+        else
+            chunk_key_subset_kernel<uint64_t><<<grid_for(m, 256), 256, 0, c.stream>>>(
+                (const uint64_t *)a.positions, m, n, chunk, isa, lf, rbits, ka, va);
+        CAPSSA_LAUNCHED(c);
+        s = radix::sort_pairs(c, ka, va, kb, vb, (uint32_t)m, 0, rbits + cbits, false, 0, &in_b);
+    }
+    if (s != CAPSSA_OK) return s;
+    const uint32_t *chunked = in_b ? vb : va;
+    // 2. samples and their rank keys, sorted; pivots
+    std::vector<uint32_t> soff(p + 1, 0);
+    for (uint32_t i = 0; i < p; i++) {
+        const uint64_t start = (uint64_t)i * chunk;
+        const uint64_t len = start >= m ? 0 : std::min<uint64_t>(chunk, m - start);
+        soff[i + 1] = soff[i] + (uint32_t)std::min<uint64_t>(per, len);
+    }
+    const uint32_t ns = soff[p];
+    const uint32_t n_piv = (p > 1 && ns > 0) ? p - 1 : 0;
+    const size_t nsb = (size_t)ns + 64;
+    char *sw = (char *)ws_get(c, WS_SAMPLE, (p + 1) * 4 + nsb * 8 * 2 + nsb * 4 * 2 +
+                                                (size_t)p * (4 + 8 + 8) + (size_t)p * 8 + 256 +
+                                                (size_t)65536 * 12 + cdf::kParams * 6 + 64);
+    if (!sw) return set_err(c, CAPSSA_ENOMEM, "sample workspace");
+    uint32_t *d_soff = (uint32_t *)sw;
+    uint64_t *sk_a = (uint64_t *)(sw + ((((size_t)p + 1) * 4 + 15) & ~(size_t)15));
+    uint64_t *sk_b = sk_a + nsb;
+    uint32_t *sp_a = (uint32_t *)(sk_b + nsb), *sp_b = sp_a + nsb;
+    uint32_t *piv_pos = sp_b + nsb;
+    uint64_t *piv_lim = (uint64_t *)(((uintptr_t)(piv_pos + p) + 15) & ~(uintptr_t)15);
+    uint64_t *piv_x = piv_lim + p;
+    unsigned long long *sizes = (unsigned long long *)(piv_x + p);
+    unsigned long long *pstats = sizes + p;  // probes, mispredictions
+    uint64_t *tx = (uint64_t *)(pstats + 4);
+    float *tt = (float *)(tx + 65536);
+    float *params = tt + 65536;
+    __nv_bfloat16 *wbf = (__nv_bfloat16 *)(params + cdf::kParams + 3);
+    CAPSSA_CUDA(c, cudaMemcpyAsync(d_soff, soff.data(), (p + 1) * 4, cudaMemcpyHostToDevice,
+                                   c.stream));
+    sample_kernel<<<grid_for((uint64_t)p * per, 256), 256, 0, c.stream>>>(
+        chunked, m, chunk, p, per, d_soff, n, isa, lf, sk_a, sp_a);
+    CAPSSA_LAUNCHED(c);
+    bool s_in_b = false;
+    s = radix::sort_pairs(c, sk_a, sp_a, sk_b, sp_b, ns, 0, bits_for(n + 1), false, 0, &s_in_b);
+    if (s != CAPSSA_OK) return s;
+    const uint32_t *sorted_samples = s_in_b ? sp_b : sp_a;
+    if (n_piv) {
+        pivot_kernel<<<grid_for(n_piv, 256), 256, 0, c.stream>>>(sorted_samples, ns, p, P, a.lim,
+                                                                piv_pos, piv_lim, piv_x);
+        CAPSSA_LAUNCHED(c);
+    }
+    // 3. learned CDF model on the sample (learned mode)
+    const bool learned = a.part_mode == CAPSSA_PARTITION_LEARNED && n_piv > 0;
+    if (learned) {
+        const uint32_t tn = std::min<uint32_t>(ns, 65536);
+        const uint32_t stride = (ns + tn - 1) / tn;
+        const uint32_t tn_eff = (ns + stride - 1) / stride;
+        train_set_kernel<<<grid_for(tn_eff, 256), 256, 0, c.stream>>>(sorted_samples, ns, stride,
+                                                                     tn_eff, P, tx, tt);
+        CAPSSA_LAUNCHED(c);
+        cudaEvent_t t0, t1;
+        cudaEventCreate(&t0);
+        cudaEventCreate(&t1);
+        cudaEventRecord(t0, c.stream);
+        float loss = 0.0f;
+        s = cdf::train(c, tx, tt, tn_eff, 300, params, wbf, &loss);
+        cudaEventRecord(t1, c.stream);
+        cudaEventSynchronize(t1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, t0, t1);
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+        if (s != CAPSSA_OK) return s;
+        c.stats.train_ms = ms;
+        c.stats.model_loss = loss;
+        c.stats.train_samples = tn_eff;
+    }
+    // 4. partition of every suffix
+    CAPSSA_CUDA(c, cudaMemsetAsync(sizes, 0, (size_t)p * 8 + 32, c.stream));
+    const size_t smem = (size_t)n_piv * 8 + (size_t)p * 4 + (learned ? cdf::kParams * 2 + 16 : 0);
+    const bool in_smem = smem <= 160 * 1024;
+    const size_t dyn = in_smem ? smem : (learned ? cdf::kParams * 2 + 16 : 0);
+    const unsigned grid = std::min<unsigned>(grid_for(m, 256), (unsigned)c.sm_count * 4);
+    cudaEvent_t q0, q1;
+    cudaEventCreate(&q0);
+    cudaEventCreate(&q1);
+    cudaEventRecord(q0, c.stream);
+#define CAPSSA_PART_LAUNCH(LRN, SM)                                                            \
+    do {                                                                                       \
+        cudaFuncSetAttribute(partition_kernel<LRN, SM>,                                        \
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);           \
+        partition_kernel<LRN, SM><<<grid, 256, dyn, c.stream>>>(                               \
+            sorted, (uint32_t)m, P, a.lim, lf, a.max_ctx, piv_pos, piv_lim, piv_x, n_piv, p,  \
+            wbf, bucket_of, sizes, pstats);                                                    \
+    } while (0)
+    if (learned) {
+        if (in_smem)
+            CAPSSA_PART_LAUNCH(true, true);
+        else
+            CAPSSA_PART_LAUNCH(true, false);
+    } else {
+        if (in_smem)
+            CAPSSA_PART_LAUNCH(false, true);
+        else
+            CAPSSA_PART_LAUNCH(false, false);
+    }
+#undef CAPSSA_PART_LAUNCH
+    CAPSSA_LAUNCHED(c);
+    cudaEventRecord(q1, c.stream);
+    int *bad = c.d_flags + 1;
+    CAPSSA_CUDA(c, cudaMemsetAsync(bad, 0, 4, c.stream));
+    partition_check_kernel<<<grid_for(m, 256), 256, 0, c.stream>>>(bucket_of, (uint32_t)m, bad);
+    CAPSSA_LAUNCHED(c);
+    std::vector<unsigned long long> h_sizes((size_t)p + 4);
+    std::vector<uint32_t> h_piv(n_piv + 1);
+    CAPSSA_CUDA(c, cudaMemcpyAsync(h_sizes.data(), sizes, ((size_t)p + 4) * 8,
+                                   cudaMemcpyDeviceToHost, c.stream));
+    if (n_piv)
+        CAPSSA_CUDA(c, cudaMemcpyAsync(h_piv.data(), piv_pos, (size_t)n_piv * 4,
+                                       cudaMemcpyDeviceToHost, c.stream));
+    int h_bad = 0;
+    CAPSSA_CUDA(c, cudaMemcpyAsync(&h_bad, bad, 4, cudaMemcpyDeviceToHost, c.stream));
+    CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+    float pms = 0.0f;
+    cudaEventElapsedTime(&pms, q0, q1);
+    cudaEventDestroy(q0);
+    cudaEventDestroy(q1);
+    if (h_bad) return set_err(c, CAPSSA_ECUDA, "partition disagrees with the sorted order");
+    c.stats.partition_ms = pms;
+    c.stats.partitions = p;
+    c.stats.partition_probes = h_sizes[p];
+    c.stats.mispredicted = h_sizes[p + 1];
+    uint64_t mx = 0;
+    for (uint32_t j = 0; j < p; j++) mx = std::max<uint64_t>(mx, h_sizes[j]);
+    c.stats.max_partition = mx;
+    if (a.part_sizes)
+        for (uint32_t j = 0; j < p; j++) a.part_sizes[j] = h_sizes[j];
+    if (a.part_pivots)
+        for (uint32_t j = 0; j < n_piv; j++) a.part_pivots[j] = h_piv[j];
+    return CAPSSA_OK;
+}
+
 template <typename S>
 capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
     using namespace eng;
@@ -1776,13 +2158,18 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
     const bool bounded = a.max_ctx != CAPSSA_UNBOUNDED && a.max_ctx < n;
 
     uint32_t *sa = nullptr;
+    eng::Packed P{};
     if (n > 0) {
-        capssa_status s = core_sort<S>(c, a, &sa);
+        capssa_status s = core_sort<S>(c, a, &sa, &P);
         if (s != CAPSSA_OK) return s;
         if (bounded) {
             s = bounded_pass<S>(c, a, sa);
             if (s != CAPSSA_OK) return s;
         }
+    }
+    if (!subset && a.part_p) {
+        capssa_status s = partition_phase<S>(c, a, P, sa, sa, n);
+        if (s != CAPSSA_OK) return s;
     }
     FinishTimer ft(c);
     if (!subset) {
@@ -1831,6 +2218,10 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
                                         false, 0, &in_b);
     if (s != CAPSSA_OK) return s;
     const uint32_t *res = in_b ? sv_b : sv;
+    if (a.part_p) {
+        s = partition_phase<S>(c, a, P, sa, res, m);
+        if (s != CAPSSA_OK) return s;
+    }
     if (a.out_bytes == 4) {
         CAPSSA_CUDA(c, cudaMemcpyAsync(a.out_sa, res, m * 4, cudaMemcpyDeviceToDevice, c.stream));
     } else {

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define CAPSSA_ABI_VERSION 1
+#define CAPSSA_ABI_VERSION 2
 
 typedef enum capssa_status {
     CAPSSA_OK = 0,
@@ -88,8 +88,14 @@ typedef struct capssa_opts {
                                   effective_subproblem_count, src/ext_mem.rs:1159-1178 */
     int32_t partition;         /* capssa_partition (sample-sort builders) */
     int32_t host_threads;      /* thread count the auto p rule assumes; 0 = all cores */
-    uint64_t reserved[6];
+    uint64_t flags;            /* CAPSSA_FLAG_* */
+    uint64_t reserved[5];
 } capssa_opts;
+
+/* capssa_opts.flags: sort through the 16-bit bucket front end (two global
+ * passes on the top key bits, then one shared-memory sort per bucket)
+ * instead of the full LSD sort; same output. */
+#define CAPSSA_FLAG_BUCKET_FRONT 1ull
 
 void capssa_opts_default(capssa_opts *o);
 
@@ -119,6 +125,12 @@ typedef struct capssa_stats {
     uint32_t sort_item_bytes; /* bytes per record the radix passes move: 8 (position packed
                                  below the key) or 12 (key + separate u32 position) */
     double sort_pass_ms;  /* summed duration of those radix-pass kernels */
+    /* sample-sort partition (capssa_build_in_memory_sample_sort_*) */
+    double partition_ms;        /* bucket of every suffix (search or prediction + fixup) */
+    double train_ms;            /* learned partition: model training */
+    uint64_t partition_probes;  /* suffix-vs-splitter comparisons of the partition */
+    uint32_t train_samples;     /* learned partition: samples the model trained on */
+    float model_loss;           /* learned partition: final mean squared CDF error */
 } capssa_stats;
 
 typedef struct capssa_ctx capssa_ctx;
@@ -302,6 +314,52 @@ capssa_status capssa_merge_noalloc_u8_u32(void *cuda_stream, const uint8_t *text
                                           const uint32_t *y, const uint32_t *lcp_y,
                                           uint64_t len_y, uint64_t max_context, uint32_t *z,
                                           uint32_t *lcp_z);
+
+/* ---------------------------------------------------------------------
+ * Sample-sort partition plan.
+ *
+ * The partition that capssa_build_in_memory_sample_sort_* computes before it
+ * emits: the subproblem count p (effective_subproblem_count,
+ * src/ext_mem.rs:1159-1178), the p - 1 pivots (phase 2, src/ext_mem.rs:
+ * 1309-1342: samples drawn as evenly spaced midpoints of every sorted chunk,
+ * :1191-1305, sorted, pivots at samples[j*ns/p]) and the size of every
+ * partition (phase 3, src/ext_mem.rs:1361-1428: a suffix s belongs to
+ * partition b = the number of pivots that compare less than s under
+ * suffix_cmp_with).  opts->partition selects how b is found: by binary
+ * search over the pivots (SPLITTERS, also AUTO), or by the learned CDF model
+ * trained on the sample and checked against its neighbouring pivots
+ * (LEARNED); both give the same b.  Pass null pivots/sizes to learn p first
+ * (*p_out); otherwise they hold p - 1 and p entries.  positions may be null
+ * (every suffix) or host/device u64 (m entries).
+ * ------------------------------------------------------------------- */
+#define CAPSSA_DECL_PLAN(S, ST)                                                               \
+    capssa_status capssa_sample_sort_plan_##S(capssa_ctx *ctx, const ST *text, uint64_t n,   \
+                                              const uint64_t *positions, uint64_t m,         \
+                                              const capssa_limits *lp,                       \
+                                              const capssa_opts *opts, uint64_t *p_out,      \
+                                              uint64_t *pivots, uint64_t *sizes);
+CAPSSA_DECL_PLAN(u8, uint8_t)
+CAPSSA_DECL_PLAN(u16, uint16_t)
+CAPSSA_DECL_PLAN(u32, uint32_t)
+
+/* ---------------------------------------------------------------------
+ * Learned CDF model of the learned partition (no reference counterpart).
+ * 2 inputs from a 64-bit packed prefix (hi32 * 2^-31 - 1, lo32 * 2^-31 - 1),
+ * 64 ReLU units, 1 output; CAPSSA_CDF_PARAMS floats laid out w1[h*2+d],
+ * b1[h], w2[h], b2.  Host or device buffers.
+ *
+ * capssa_cdf_grad: mean-squared-error loss and its gradient over n
+ * (prefix, target) samples, from the GPU forward/backward kernels that the
+ * learned partition trains with.
+ * capssa_cdf_train: `steps` full-batch Adam steps from the built-in
+ * initialisation (the training the learned partition runs); writes the
+ * trained parameters and the final loss.
+ * ------------------------------------------------------------------- */
+#define CAPSSA_CDF_PARAMS 257
+capssa_status capssa_cdf_grad(capssa_ctx *ctx, const float *params, const uint64_t *prefixes,
+                              const float *targets, uint64_t n, float *grad, float *loss);
+capssa_status capssa_cdf_train(capssa_ctx *ctx, const uint64_t *prefixes, const float *targets,
+                               uint64_t n, int32_t steps, float *params, float *loss);
 
 #ifdef __cplusplus
 }

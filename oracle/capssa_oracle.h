@@ -120,6 +120,15 @@ int or_brute_sa(const void *text, uint64_t n, int sym_bytes,
 
 int or_max_threads(void);
 
+/* Learned CDF model (no reference counterpart; cdf_oracle.c): 2 inputs from
+ * the 64-bit packed prefix, OR_CDF_HIDDEN ReLU units, 1 output. */
+#define OR_CDF_HIDDEN 64
+#define OR_CDF_PARAMS (4 * OR_CDF_HIDDEN + 1)
+void or_cdf_features(uint64_t prefix, float f[2]);
+double or_cdf_forward(const float *params, uint64_t prefix);
+double or_cdf_loss_grad(const float *params, const uint64_t *prefix, const float *target,
+                        uint64_t n, double *grad);
+
 #ifdef __cplusplus
 }
 #endif

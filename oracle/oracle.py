@@ -30,7 +30,7 @@ def build(force: bool = False) -> str:
 
 def _stale() -> bool:
     t = os.path.getmtime(LIB_PATH)
-    for f in ("capssa_oracle.c", "oracle_tmpl.h", "capssa_oracle.h"):
+    for f in ("capssa_oracle.c", "cdf_oracle.c", "oracle_tmpl.h", "capssa_oracle.h"):
         if os.path.getmtime(os.path.join(HERE, f)) > t:
             return True
     return False
@@ -81,6 +81,11 @@ def lib():
                                        C.c_uint32, C.c_uint32, vp, vp, u64]
         L.or_brute_sa.argtypes = [vp, u64, i, C.POINTER(_Limits), u64, vp, u64, vp]
         L.or_max_threads.restype = i
+        L.or_cdf_forward.argtypes = [vp, u64]
+        L.or_cdf_forward.restype = C.c_double
+        L.or_cdf_loss_grad.argtypes = [vp, vp, vp, u64, vp]
+        L.or_cdf_loss_grad.restype = C.c_double
+        L.or_cdf_features.argtypes = [u64, vp]
         _lib = L
     return _lib
 
@@ -252,3 +257,33 @@ def brute_sa(text, positions=None, limits=None, max_ctx=UNBOUNDED):
 
 def max_threads():
     return int(lib().or_max_threads())
+
+
+# ---------------------------------------------------------------- learned CDF model
+
+CDF_HIDDEN = 64
+CDF_PARAMS = 4 * CDF_HIDDEN + 1
+
+
+def cdf_features(prefix):
+    """The model's two float inputs for one 64-bit packed prefix."""
+    f = np.zeros(2, dtype=np.float32)
+    lib().or_cdf_features(int(prefix), _ptr(f))
+    return f
+
+
+def cdf_forward(params, prefixes):
+    """Model output per prefix (double accumulation)."""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    return np.array([lib().or_cdf_forward(_ptr(params), int(x)) for x in prefixes])
+
+
+def cdf_loss_grad(params, prefixes, targets):
+    """(mean squared error, gradient of it w.r.t. the 257 parameters)."""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    prefixes = np.ascontiguousarray(prefixes, dtype=np.uint64)
+    targets = np.ascontiguousarray(targets, dtype=np.float32)
+    grad = np.zeros(CDF_PARAMS, dtype=np.float64)
+    loss = lib().or_cdf_loss_grad(_ptr(params), _ptr(prefixes), _ptr(targets),
+                                  len(prefixes), _ptr(grad))
+    return loss, grad

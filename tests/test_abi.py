@@ -24,7 +24,7 @@ def declared_symbols():
               "capssa_build_batched_%s_%s"]
     fam_s = ["capssa_build_in_memory_sample_sort_%s",
              "capssa_build_in_memory_sample_sort_for_positions_%s", "capssa_lcp_%s",
-             "capssa_suffix_cmp_%s"]
+             "capssa_suffix_cmp_%s", "capssa_sample_sort_plan_%s"]
     for f in fam_si:
         for s in sym:
             for i in idx:
@@ -50,6 +50,8 @@ def test_header_declares_expected_families():
     names = declared_symbols()
     assert "capssa_build_in_memory_u8_u32" in names
     assert "capssa_seed_subarray_u8_u64" in names
+    assert "capssa_sample_sort_plan_u16" in names
+    assert "capssa_cdf_grad" in names and "capssa_cdf_train" in names
     assert len(names) >= 55
 
 
@@ -59,7 +61,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_defaults(lib):
-    assert lib.capssa_abi_version() == 1
+    assert lib.capssa_abi_version() == 2
 
     class Opts(ctypes.Structure):
         _fields_ = [("max_context", ctypes.c_uint64), ("subproblem_count", ctypes.c_uint64),

@@ -225,3 +225,33 @@ def test_merge_restatement_on_halves():
         z, lz = orc.merge(t, x, lx, y, ly)
         sa, lcp = orc.build_in_memory(t, with_lcp=True)
         assert z.tolist() == sa.tolist() and lz.tolist() == lcp.tolist()
+
+
+def test_cdf_oracle_gradient_matches_finite_differences():
+    """The CPU restatement of the learned CDF model: its analytic gradient
+    agrees with central differences of its own forward pass."""
+    rng = np.random.default_rng(7)
+    params = rng.normal(0, 0.3, orc.CDF_PARAMS).astype(np.float32)
+    x = (rng.integers(0, 2 ** 63, 300, dtype=np.uint64) << np.uint64(1)) | np.uint64(1)
+    t = rng.random(300).astype(np.float32)
+    loss, g = orc.cdf_loss_grad(params, x, t)
+
+    def f(p):
+        y = orc.cdf_forward(p, x)
+        return float(np.mean((y - t.astype(np.float64)) ** 2))
+
+    assert abs(loss - f(params)) < 1e-9
+    eps = 1e-3
+    for i in (0, 1, 7, 64, 100, 150, 200, 256):
+        pp, pm = params.copy(), params.copy()
+        pp[i] += eps
+        pm[i] -= eps
+        num = (f(pp) - f(pm)) / (2 * eps)
+        assert abs(num - g[i]) <= 1e-3 * max(1.0, abs(g[i])), (i, num, g[i])
+
+
+def test_cdf_oracle_features():
+    f = orc.cdf_features(0)
+    assert f.tolist() == [-1.0, -1.0]
+    f = orc.cdf_features(1 << 63)
+    assert f.tolist() == [0.0, -1.0]
