@@ -45,6 +45,9 @@ def parse():
     ap.add_argument("--log2n", type=int, default=28)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the secondary forms (sample sort with splitter / learned "
+                         "partition, batched texts, segmented filtered subset)")
     return ap.parse_args()
 
 
@@ -217,6 +220,86 @@ def run_reference(args):
 
 # ------------------------------------------------------------------ our arm
 
+def _timed(fn, reps):
+    """Median wall time (ms) of fn() over reps calls (each call synchronises)."""
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn()
+        ts.append((time.perf_counter() - t0) * 1e3)
+    return statistics.median(ts)
+
+
+def run_forms(ctx, t_dev, n):
+    """The secondary forms of the metric, each on its own workload:
+    sample sort of the bench text with p = 4096 partitions found by splitter
+    binary search vs the learned CDF model (65,536 training samples); 8,192
+    independent texts sorted in one batched call vs a per-text loop; the
+    segmented, filtered subset build (n = 2^29, u64 index)."""
+    import torch
+
+    import capssa
+    from capssa import workloads
+
+    out = {}
+    # ---- sample sort: splitter vs learned partition (plan = SA + partition)
+    ss = {}
+    for name, part in (("splitters", capssa.Partition.SPLITTERS),
+                       ("learned", capssa.Partition.LEARNED)):
+        opts = capssa.ExtMemOpts(subproblem_count=4096, partition=part)
+        ctx.sample_sort_plan(t_dev, opts)  # warm
+        ms = _timed(lambda: ctx.sample_sort_plan(t_dev, opts), 3)
+        k, pv, sz = ctx.sample_sort_plan(t_dev, opts)
+        st = ctx.stats()
+        ss[name] = {"value": n / (ms / 1e3) / 1e6, "unit": "Msuffixes/s", "ms": ms,
+                    "partition_ms": st["partition_ms"],
+                    "probes_per_suffix": st["partition_probes"] / n,
+                    "mispredicted_rate": st["mispredicted"] / n,
+                    "imbalance_max_over_mean": float(sz.max()) / (n / k),
+                    "train_ms": st["train_ms"], "train_samples": st["train_samples"],
+                    "model_loss": st["model_loss"], "p": k,
+                    "sizes_sha": hash(sz.tobytes()) & 0xFFFFFFFF}
+    ss["same_partition"] = ss["splitters"]["sizes_sha"] == ss["learned"]["sizes_sha"]
+    out["sample_sort_p4096"] = ss
+    # ---- batched: 8,192 texts, log-uniform 2^10..2^20, 10% repeats
+    cat, offs = workloads.batched_texts()
+    c_dev = torch.from_numpy(cat).to("cuda")
+    total = int(offs[-1])
+    ctx.build_batched(c_dev, offs)  # warm
+    b_ms = _timed(lambda: ctx.build_batched(c_dev, offs), 2)
+    # per-text loop of plain builds on every 16th text (bounded sample)
+    idx = list(range(0, len(offs) - 1, 16))
+    sample_syms = sum(int(offs[i + 1] - offs[i]) for i in idx)
+
+    def loop():
+        for i in idx:
+            ctx.build_in_memory(c_dev[int(offs[i]):int(offs[i + 1])])
+
+    loop()
+    l_ms = _timed(loop, 1)
+    out["batched_8192_texts"] = {
+        "value": total / (b_ms / 1e3) / 1e6, "unit": "Msuffixes/s", "ms": b_ms,
+        "symbols": total,
+        "per_text_loop": {"value": sample_syms / (l_ms / 1e3) / 1e6, "unit": "Msuffixes/s",
+                          "sample": "every 16th text (%d texts, %d symbols)"
+                                    % (len(idx), sample_syms)}}
+    del c_dev
+    # ---- segmented filtered subset (config 3)
+    text3, ends3, pos3 = workloads.segmented_filtered(1 << 29)
+    t3 = torch.from_numpy(text3).to("cuda")
+    p3 = torch.from_numpy(pos3.view(np.int64)).to("cuda")
+    o3 = torch.empty(len(pos3), dtype=torch.int64, device="cuda")
+    lp3 = capssa.SegmentedText(len(text3), ends3)
+    ctx.build_in_memory_for_positions(t3, p3, lp3, out=o3)  # warm
+    s_ms = _timed(lambda: ctx.build_in_memory_for_positions(t3, p3, lp3, out=o3), 2)
+    out["segmented_filtered_2p29"] = {"value": len(pos3) / (s_ms / 1e3) / 1e6,
+                                      "unit": "Msuffixes/s", "ms": s_ms,
+                                      "positions": int(len(pos3)), "segments": int(len(ends3))}
+    del t3, p3, o3
+    torch.cuda.synchronize()
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -321,6 +404,10 @@ def run_ours(args):
         if not np.array_equal(h_out.numpy().view(np.uint32), sa_dev.cpu().numpy().view(np.uint32)):
             raise SystemExit("host-path suffix array differs from the device-path one")
 
+    forms = None
+    if rank == 0 and ws == 1 and not args.no_forms:
+        forms = run_forms(ctx, t_dev, n)
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(text)
@@ -331,7 +418,7 @@ def run_ours(args):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
                 "data": "synthetic (seeded generator, caps-sa_gb300/capssa/workloads.py)",
                 "config": config(log2n, n), "roofline": roofline, "cpu_baseline": cpu,
-                "e2e": e2e, "clocks": clk, "gpu_launches": launches}
+                "e2e": e2e, "clocks": clk, "gpu_launches": launches, "forms": forms}
         print(json.dumps(line), flush=True)
     ctx.close()
     if dist is not None:

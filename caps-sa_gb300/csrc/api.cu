@@ -1,6 +1,7 @@
 // api.cu — the C ABI (include/capssa.h): contexts, workspace, staging of
 // host/device buffers, and the exported entry points.
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -67,19 +68,21 @@ capssa_status check_dev_flags(Ctx &c) {
 }
 
 // Key geometry for b bits per symbol on a text of n symbols.  Symbols past
-// log_{2^b}(n) + 3 rarely separate random suffixes, so the key keeps only
+// log2(n) / H + 3 (H the symbols' entropy) rarely separate random suffixes, so the key keeps only
 // as many symbols as fit in the radix passes that this minimum needs (DNA
 // at n = 2^28: 17 symbols + a flag = 35 bits, 5 passes), with the position
 // packed below it when key and position fit 64 bits.  Otherwise the widest
 // key holds kmax symbols (kmax*b + bits(kmax) <= 64) and a length field.
-KeyGeom key_geom(int b, uint64_t n, bool plain) {
+KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits) {
     KeyGeom g{};
     g.b = b < 1 ? 1 : b;
     int logn = 0;
     while (logn < 64 && (n >> logn) > 1) logn++;
-    // log_sigma(n) + 3 symbols: random suffixes then tie in about n / (2 sigma^3)
-    // pairs, which the refinement resolves cheaply
-    const int kmin = (logn + g.b - 1) / g.b + 3;
+    // log2(n) / H + 3 symbols (H = symbol entropy in bits, <= b): random
+    // suffixes then tie in about n / 2^(3H+1) pairs, which the refinement
+    // resolves cheaply
+    const double h = hbits > 0.25 ? (hbits < g.b ? hbits : (double)g.b) : 0.25;
+    const int kmin = (int)std::ceil((double)logn / h - 1e-9) + 3;
     // the position rides below the key when both fit in 64 bits; a plain
     // text then marks its k-1 short suffixes with one flag bit instead of a
     // length field (they are refined from depth 0)

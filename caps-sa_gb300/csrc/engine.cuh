@@ -71,7 +71,8 @@ struct KeyGeom {
     int flag_len;  // 1: the length field is one "ended early" flag (plain texts)
     int vbits;     // > 0: the position is packed below the key in vbits bits
 };
-// plain: the limits are PlainText's (only the last k-1 suffixes end early).
-KeyGeom key_geom(int b, uint64_t n, bool plain);
+// plain: the limits are PlainText's (only the last k-1 suffixes end early);
+// hbits: entropy of the symbols in bits (<= b).
+KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits);
 
 }  // namespace capssa

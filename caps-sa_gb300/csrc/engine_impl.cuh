@@ -5,6 +5,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -89,6 +90,15 @@ __global__ void presence_kernel(const S *__restrict__ text, uint64_t n,
         uint32_t s = (uint32_t)text[i];
         if (__ldcg(present + s) == 0) present[s] = 1;
     }
+}
+
+// Every stride-th symbol (the entropy estimate's sample).
+template <typename S>
+__global__ void strided_sample_kernel(const S *__restrict__ text, uint64_t ns, uint64_t stride,
+                                      S *__restrict__ out) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < ns;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = text[i * stride];
 }
 
 __global__ void minmax_kernel(const uint32_t *__restrict__ text, uint64_t n,
@@ -513,18 +523,30 @@ __global__ void gather_small_kernel(const uint4 *__restrict__ groups, uint32_t c
     }
 }
 
-__global__ void gather_big_kernel(const BigGroup *__restrict__ groups,
-                                  const uint32_t *__restrict__ sa,
+// Rank-doubling keys of the big groups' members, one thread per member
+// (a single group can hold millions: runs of one symbol): member t belongs
+// to the group whose flattened offset range holds it (groups' offsets grow
+// with their ordinals).
+__global__ void gather_big_kernel(const BigGroup *__restrict__ groups, uint32_t nb,
+                                  uint32_t total, const uint32_t *__restrict__ sa,
                                   const uint32_t *__restrict__ rank, DevLimits L, uint64_t h,
                                   int lf, uint64_t empty_lf, int k2bits,
                                   uint64_t *__restrict__ tkeys, uint32_t *__restrict__ tvals) {
-    const uint32_t ord = blockIdx.x;
-    BigGroup g = groups[ord];
-    for (uint32_t t = threadIdx.x; t < g.len; t += blockDim.x) {
-        uint32_t p = sa[g.start + t];
-        uint64_t k2 = doubling_key(L, rank, p, h, lf, empty_lf);
-        tkeys[g.toff + t] = ((uint64_t)ord << k2bits) | k2;
-        tvals[g.toff + t] = p;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = nb;  // last group with toff <= t
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (groups[mid].toff <= t)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        const BigGroup g = groups[lo];
+        const uint32_t p = sa[g.start + (t - g.toff)];
+        const uint64_t k2 = doubling_key(L, rank, p, h, lf, empty_lf);
+        tkeys[t] = ((uint64_t)lo << k2bits) | k2;
+        tvals[t] = p;
     }
 }
 
@@ -1348,27 +1370,38 @@ __global__ void subset_isa_key_kernel(const PT *__restrict__ pos, uint64_t m, ui
 
 // ---------------------------------------------------------------- sample-sort partition
 
-// suffix_cmp_with (src/lcp.rs:184-201) of suffixes a and b with limits la,
-// lb and max_context, from their first packed windows xa, xb and, when
-// those do not decide, direct comparison on the packed text.  -1 / 0 / 1.
-__device__ __forceinline__ int suffix_cmp_full(const Packed &P, uint64_t a, uint64_t la,
-                                               uint64_t xa, uint64_t b, uint64_t lb,
-                                               uint64_t xb, uint64_t max_ctx, int lf) {
-    uint64_t lim = la < lb ? la : lb;
-    lim = lim < max_ctx ? lim : max_ctx;
-    const uint64_t x = xa ^ xb;
-    if (x) {
-        const uint64_t d = (uint64_t)__clzll((long long)x) / (uint64_t)P.b;
-        if (d < lim) return xa < xb ? -1 : 1;
+// Comparison keys of the sorted text for the partition: suffixes that
+// suffix_cmp_with (src/lcp.rs:184-201) calls Equal form contiguous runs of
+// the sorted order, and every suffix's key is 1 + the SA index where its run
+// starts, so key order is exactly the comparator's order (ties included);
+// the empty suffix (position n) gets 0 (ShorterFirst) or n + 1
+// (LongerFirst).  Ties exist only under SegmentedText with ShorterFirst
+// (equal limits, equal symbols through min(limit, max_context)); head[j] =
+// j for a run start, else 0, and a max-scan spreads the starts.
+__global__ void tie_head_kernel(const uint32_t *__restrict__ sa, uint32_t n,
+                                const uint8_t *__restrict__ text, int sym_bytes, DevLimits L,
+                                uint64_t max_ctx, uint32_t *__restrict__ head) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        bool tie = false;
+        if (j > 0) {
+            const uint32_t a = sa[j - 1], b = sa[j];
+            const uint64_t la = dev_lim_at(L, a), lb = dev_lim_at(L, b);
+            if (la == lb) {
+                const uint64_t lim = la < max_ctx ? la : max_ctx;
+                const uint64_t k = (uint64_t)sym_bytes;
+                tie = thread_lcp_bytes(text, (uint64_t)a * k, (uint64_t)b * k, lim * k) >= lim * k;
+            }
+        }
+        head[j] = tie ? 0u : j;
     }
-    int r = direct_cmp(P, a, la, b, lb, 0, max_ctx, lf);
-    if (r == 2) {  // equal through max_context: boundary order on the full limits
-        if (!lf)
-            r = (la > lb) - (la < lb);
-        else
-            r = la != lb ? (lb > la) - (lb < la) : (a > b) - (a < b);
-    }
-    return r;
+}
+
+__global__ void head_key_kernel(const uint32_t *__restrict__ sa, uint32_t n,
+                                const uint32_t *__restrict__ head, int lf,
+                                uint32_t *__restrict__ hkey) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        hkey[sa[j]] = (head ? head[j] : j) + 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) hkey[n] = lf ? n + 1 : 0u;
 }
 
 // Chunk-major order of the sorted suffixes (full text): key = chunk of the
@@ -1423,16 +1456,15 @@ __global__ void sample_kernel(const uint32_t *__restrict__ chunked, uint64_t m, 
 }
 
 // Pivots samples[j * ns / p] (phase 2, src/ext_mem.rs:1309-1342) with their
-// limits and first windows.
+// comparison keys.
 __global__ void pivot_kernel(const uint32_t *__restrict__ sorted_samples, uint32_t ns, uint32_t p,
-                             Packed P, DevLimits L, uint32_t *__restrict__ piv_pos,
-                             uint64_t *__restrict__ piv_lim, uint64_t *__restrict__ piv_x) {
+                             const uint32_t *__restrict__ hkey, uint32_t *__restrict__ piv_pos,
+                             uint32_t *__restrict__ piv_key) {
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j + 1 < p;
          j += gridDim.x * blockDim.x) {
         const uint32_t q = sorted_samples[(uint64_t)(j + 1) * ns / p];
         piv_pos[j] = q;
-        piv_lim[j] = dev_lim_at(L, q);
-        piv_x[j] = window_at(P, q);
+        piv_key[j] = hkey[q];
     }
 }
 
@@ -1450,71 +1482,60 @@ __global__ void train_set_kernel(const uint32_t *__restrict__ sorted_samples, ui
 
 // Partition of every suffix (phase 3, src/ext_mem.rs:1361-1428, with
 // upper_bound_by_pivot :1705-1734): b = the number of pivots that compare
-// less than the suffix.  SPLITTERS: binary search over the pivots.
-// LEARNED: the CDF model predicts b from the suffix's packed prefix; the
-// prediction is checked against its two neighbouring pivots and moved until
-// both hold.  The suffixes come in sorted order, so b must never decrease
-// along them (checked by the caller).  Pivot windows and the bucket
-// histogram live in shared memory when they fit (SMEM).
-template <bool LEARNED, bool SMEM>
+// less than the suffix, every comparison an exact suffix_cmp_with read from
+// the comparison keys.  SPLITTERS: binary search over the pivots.  LEARNED:
+// the CDF model predicts b from the suffix's packed prefix; the prediction
+// is checked against its two neighbouring pivots and moved until both hold.
+// `items` lists the suffixes (nullptr: every position 0..m-1, read in text
+// order so that keys and prefixes stream); b must never decrease along the
+// sorted order (checked by the caller).  Pivot keys and the bucket histogram
+// live in shared memory.
+template <bool LEARNED>
 __global__ void __launch_bounds__(256)
-    partition_kernel(const uint32_t *__restrict__ sorted, uint32_t m, Packed P, DevLimits L,
-                     int lf, uint64_t max_ctx, const uint32_t *__restrict__ piv_pos,
-                     const uint64_t *__restrict__ piv_lim, const uint64_t *__restrict__ piv_x,
+    partition_kernel(const uint32_t *__restrict__ items, uint32_t m, Packed P,
+                     const uint32_t *__restrict__ hkey, const uint32_t *__restrict__ piv_key,
                      uint32_t n_piv, uint32_t p, const __nv_bfloat16 *__restrict__ w,
                      uint32_t *__restrict__ bucket_of, unsigned long long *__restrict__ sizes,
                      unsigned long long *__restrict__ stats) {
     extern __shared__ __align__(16) unsigned char psm[];
-    uint64_t *sx = reinterpret_cast<uint64_t *>(psm);
-    uint32_t *hist = reinterpret_cast<uint32_t *>(sx + (SMEM ? n_piv : 0));
-    __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(hist + (SMEM ? p : 0));
-    if (SMEM) {
-        for (uint32_t j = threadIdx.x; j < n_piv; j += blockDim.x) sx[j] = piv_x[j];
-        for (uint32_t j = threadIdx.x; j < p; j += blockDim.x) hist[j] = 0;
-    }
+    uint32_t *sk = reinterpret_cast<uint32_t *>(psm);
+    uint32_t *hist = sk + n_piv;
+    __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(hist + p);
+    for (uint32_t j = threadIdx.x; j < n_piv; j += blockDim.x) sk[j] = piv_key[j];
+    for (uint32_t j = threadIdx.x; j < p; j += blockDim.x) hist[j] = 0;
     if (LEARNED)
         for (int j = threadIdx.x; j < cdf::kParams; j += blockDim.x) sw[j] = w[j];
     __syncthreads();
-    const uint64_t *X = SMEM ? sx : piv_x;
     unsigned long long probes = 0, mis = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-        const uint32_t s = sorted[i];
-        const uint64_t ls = dev_lim_at(L, s);
-        const uint64_t xs = window_at(P, s);
-        // pivot j < suffix s
-        auto below = [&](uint32_t j) -> bool {
-            probes++;
-            return suffix_cmp_full(P, piv_pos[j], piv_lim[j], X[j], s, ls, xs, max_ctx, lf) < 0;
-        };
+        const uint32_t s = items ? items[i] : i;
+        const uint32_t ks = hkey[s];
         uint32_t b;
         if (LEARNED) {
-            const float y = cdf::infer_bf16(sw, xs);
+            const float y = cdf::infer_bf16(sw, window_at(P, s));
             float g = floorf(y * (float)p);
             g = g < 0.0f ? 0.0f : (g > (float)n_piv ? (float)n_piv : g);
             b = (uint32_t)g;
             const uint32_t guess = b;
-            while (b > 0 && !below(b - 1)) b--;
+            while (b > 0 && (probes++, !(sk[b - 1] < ks))) b--;
             if (b == guess)
-                while (b < n_piv && below(b)) b++;
+                while (b < n_piv && (probes++, sk[b] < ks)) b++;
             mis += b != guess ? 1u : 0u;
         } else {
             uint32_t lo = 0, hi = n_piv;
             while (lo < hi) {
                 const uint32_t mid = (lo + hi) >> 1;
-                if (below(mid))
+                probes++;
+                if (sk[mid] < ks)
                     lo = mid + 1;
                 else
                     hi = mid;
             }
             b = lo;
         }
-        if (SMEM)
-            atomicAdd(&hist[b], 1u);
-        else
-            atomicAdd(&sizes[b], 1ull);
+        atomicAdd(&hist[b], 1u);
         bucket_of[i] = b;
     }
-    // block sums of the probe and misprediction counts, then the histogram
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         probes += __shfl_xor_sync(0xffffffffu, probes, o);
@@ -1524,19 +1545,21 @@ __global__ void __launch_bounds__(256)
         atomicAdd(&stats[0], probes);
         atomicAdd(&stats[1], mis);
     }
-    if (SMEM) {
-        __syncthreads();
-        for (uint32_t j = threadIdx.x; j < p; j += blockDim.x)
-            if (hist[j]) atomicAdd(&sizes[j], (unsigned long long)hist[j]);
-    }
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < p; j += blockDim.x)
+        if (hist[j]) atomicAdd(&sizes[j], (unsigned long long)hist[j]);
 }
 
-// Partitions along the sorted order never decrease (else flag).
-__global__ void partition_check_kernel(const uint32_t *__restrict__ bucket_of, uint32_t m,
+// Partitions along the sorted order never decrease (else flag); `sa`
+// non-null: bucket_of is indexed by position and the order is sa's.
+__global__ void partition_check_kernel(const uint32_t *__restrict__ bucket_of,
+                                       const uint32_t *__restrict__ sa, uint32_t m,
                                        int *__restrict__ bad) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + 1; i < m;
-         i += gridDim.x * blockDim.x)
-        if (bucket_of[i] < bucket_of[i - 1]) atomicExch(bad, 1);
+         i += gridDim.x * blockDim.x) {
+        const uint32_t b0 = bucket_of[sa ? sa[i - 1] : i - 1], b1 = bucket_of[sa ? sa[i] : i];
+        if (b1 < b0) atomicExch(bad, 1);
+    }
 }
 
 }  // namespace eng
@@ -1648,7 +1671,43 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
         sigma_span = (uint64_t)h_mm[1] - h_mm[0] + 1;
     }
     const int b = bits_for(sigma_span > 1 ? sigma_span - 1 : 1);
-    const KeyGeom geo = key_geom(b, n, !a.lim.segmented);
+    // order-0 entropy of the symbols from an evenly strided sample: the key
+    // must hold about log2(n) / H + 3 symbols to leave few random ties
+    // (the b-bit code width overstates H for skewed alphabets)
+    double hbits = (double)b;
+    if (n >= (1u << 20) && b > 1) {  // small texts: ties are cheap either way
+        const uint64_t ns = 65536, stride = n / ns;
+        S *d_hs = (S *)ws_get(c, WS_MISC3, ns * sizeof(S) + 64);
+        if (!d_hs) return set_err(c, CAPSSA_ENOMEM, "entropy sample");
+        strided_sample_kernel<S><<<grid_for(ns, 256), 256, 0, c.stream>>>(text, ns, stride, d_hs);
+        CAPSSA_LAUNCHED(c);
+        std::vector<S> hs(ns);
+        CAPSSA_CUDA(c, cudaMemcpyAsync(hs.data(), d_hs, ns * sizeof(S), cudaMemcpyDeviceToHost,
+                                       c.stream));
+        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+        double hsum = 0.0;
+        auto add = [&](uint64_t cnt) {
+            const double q = (double)cnt / (double)ns;
+            hsum -= q * std::log2(q);
+        };
+        if (sizeof(S) <= 2) {  // counts per value
+            std::vector<uint32_t> cnt(sizeof(S) == 1 ? 256 : 65536, 0);
+            for (S v : hs) cnt[v]++;
+            for (uint32_t x : cnt)
+                if (x) add(x);
+        } else {
+            std::sort(hs.begin(), hs.end());
+            for (uint64_t i = 0; i < ns;) {
+                uint64_t j = i;
+                while (j < ns && hs[j] == hs[i]) j++;
+                add(j - i);
+                i = j;
+            }
+        }
+        // within 3% of the code width counts as full (sampling noise)
+        hbits = hsum >= 0.97 * b ? (double)b : std::max<double>(hsum, 0.25);
+    }
+    const KeyGeom geo = key_geom(b, n, !a.lim.segmented, hbits);
     c.stats.key_symbols = geo.k;
     c.stats.key_bits_per_symbol = geo.b;
 
@@ -1842,7 +1901,8 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
         }
         const int ord_bits = nb > 1 ? bits_for(nb - 1) : 1;
         if (nb) {
-            gather_big_kernel<<<nb, 256, 0, c.stream>>>(G.big[cur], sa, rank, a.lim, h, lf,
+            gather_big_kernel<<<grid_for(big_total, 256), 256, 0, c.stream>>>(
+                G.big[cur], nb, big_total, sa, rank, a.lim, h, lf,
                                                         empty_lf, k2bits, keys_a, spare_vals);
             CAPSSA_LAUNCHED(c);
             bool tb = false;
@@ -1971,25 +2031,40 @@ capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
     const int lf = a.lim.longer_first;
     const uint32_t p = a.part_p;
     if (p == 0 || m == 0) return CAPSSA_OK;
+    if (p > 24576) return set_err(c, CAPSSA_EUNSUPPORTED, "more than 24,576 subproblems");
     const uint32_t chunk = (uint32_t)((m + p - 1) / p);
     double ln_m = std::log((double)m);
     if (ln_m < 1.0) ln_m = 1.0;
     uint64_t total = (uint64_t)p * (uint64_t)std::ceil(4.0 * ln_m);
     total = std::min<uint64_t>(std::max<uint64_t>(total, p), m);
     const uint32_t per = (uint32_t)((total + p - 1) / p);
-    // scratch: chunk-major keys/values (ping-pong), samples, pivots, buckets
-    const size_t m8 = (size_t)m * 8 + 64, m4 = (size_t)m * 4 + 64;
-    char *w = (char *)ws_get(c, WS_PART, 2 * m8 + 3 * m4);
+    // scratch: chunk-major keys/values (ping-pong), buckets, head runs, keys
+    const size_t m8 = (size_t)m * 8 + 64, m4 = (size_t)m * 4 + 64, n4 = (size_t)n * 4 + 64;
+    char *w = (char *)ws_get(c, WS_PART, 2 * m8 + 3 * m4 + 2 * n4);
     uint32_t *isa = (uint32_t *)ws_get(c, WS_RANK, (size_t)n * 4 + 64);
     if (!w || !isa) return set_err(c, CAPSSA_ENOMEM, "partition workspace");
     uint64_t *ka = (uint64_t *)w, *kb = (uint64_t *)(w + m8);
     uint32_t *va = (uint32_t *)(w + 2 * m8), *vb = (uint32_t *)(w + 2 * m8 + m4);
     uint32_t *bucket_of = (uint32_t *)(w + 2 * m8 + 2 * m4);
+    uint32_t *head = (uint32_t *)(w + 2 * m8 + 3 * m4);
+    uint32_t *hkey = (uint32_t *)(w + 2 * m8 + 3 * m4 + n4);
     const bool subset = a.positions != nullptr;
     if (!subset) {
         isa_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa_full, (uint32_t)n, isa);
         CAPSSA_LAUNCHED(c);
     }  // (subsets: the caller's isa is already in place)
+    // 0. comparison keys (run heads of the comparator's ties)
+    const bool ties = a.lim.segmented && !lf;
+    if (ties) {
+        tie_head_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(
+            sa_full, (uint32_t)n, (const uint8_t *)a.text, a.sym_bytes, a.lim, a.max_ctx, head);
+        CAPSSA_LAUNCHED(c);
+        capssa_status s0 = scan_u32(c, head, head, n, /*max_op=*/true, /*inclusive=*/true);
+        if (s0 != CAPSSA_OK) return s0;
+    }
+    head_key_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa_full, (uint32_t)n,
+                                                            ties ? head : nullptr, lf, hkey);
+    CAPSSA_LAUNCHED(c);
     // 1. every chunk's positions in sorted order
     const int cbits = bits_for(p > 1 ? p - 1 : 1);
     bool in_b = false;
@@ -2022,18 +2097,18 @@ capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
     const uint32_t ns = soff[p];
     const uint32_t n_piv = (p > 1 && ns > 0) ? p - 1 : 0;
     const size_t nsb = (size_t)ns + 64;
-    char *sw = (char *)ws_get(c, WS_SAMPLE, (p + 1) * 4 + nsb * 8 * 2 + nsb * 4 * 2 +
-                                                (size_t)p * (4 + 8 + 8) + (size_t)p * 8 + 256 +
-                                                (size_t)65536 * 12 + cdf::kParams * 6 + 64);
+    char *sw = (char *)ws_get(c, WS_SAMPLE, (p + 1) * 4 + 16 + nsb * 8 * 2 + nsb * 4 * 2 +
+                                                (size_t)p * 16 + 256 + (size_t)65536 * 12 +
+                                                cdf::kParams * 6 + 64);
     if (!sw) return set_err(c, CAPSSA_ENOMEM, "sample workspace");
     uint32_t *d_soff = (uint32_t *)sw;
     uint64_t *sk_a = (uint64_t *)(sw + ((((size_t)p + 1) * 4 + 15) & ~(size_t)15));
     uint64_t *sk_b = sk_a + nsb;
     uint32_t *sp_a = (uint32_t *)(sk_b + nsb), *sp_b = sp_a + nsb;
     uint32_t *piv_pos = sp_b + nsb;
-    uint64_t *piv_lim = (uint64_t *)(((uintptr_t)(piv_pos + p) + 15) & ~(uintptr_t)15);
-    uint64_t *piv_x = piv_lim + p;
-    unsigned long long *sizes = (unsigned long long *)(piv_x + p);
+    uint32_t *piv_key = piv_pos + p;
+    unsigned long long *sizes =
+        (unsigned long long *)(((uintptr_t)(piv_key + p) + 15) & ~(uintptr_t)15);
     unsigned long long *pstats = sizes + p;  // probes, mispredictions
     uint64_t *tx = (uint64_t *)(pstats + 4);
     float *tt = (float *)(tx + 65536);
@@ -2049,8 +2124,8 @@ capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
     if (s != CAPSSA_OK) return s;
     const uint32_t *sorted_samples = s_in_b ? sp_b : sp_a;
     if (n_piv) {
-        pivot_kernel<<<grid_for(n_piv, 256), 256, 0, c.stream>>>(sorted_samples, ns, p, P, a.lim,
-                                                                piv_pos, piv_lim, piv_x);
+        pivot_kernel<<<grid_for(n_piv, 256), 256, 0, c.stream>>>(sorted_samples, ns, p, hkey,
+                                                                piv_pos, piv_key);
         CAPSSA_LAUNCHED(c);
     }
     // 3. learned CDF model on the sample (learned mode)
@@ -2081,39 +2156,34 @@ capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
     }
     // 4. partition of every suffix
     CAPSSA_CUDA(c, cudaMemsetAsync(sizes, 0, (size_t)p * 8 + 32, c.stream));
-    const size_t smem = (size_t)n_piv * 8 + (size_t)p * 4 + (learned ? cdf::kParams * 2 + 16 : 0);
-    const bool in_smem = smem <= 160 * 1024;
-    const size_t dyn = in_smem ? smem : (learned ? cdf::kParams * 2 + 16 : 0);
+    const size_t smem = (size_t)n_piv * 4 + (size_t)p * 4 + (learned ? cdf::kParams * 2 + 16 : 0);
     const unsigned grid = std::min<unsigned>(grid_for(m, 256), (unsigned)c.sm_count * 4);
+    if (learned)
+        cudaFuncSetAttribute(partition_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    else
+        cudaFuncSetAttribute(partition_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
     cudaEvent_t q0, q1;
     cudaEventCreate(&q0);
     cudaEventCreate(&q1);
     cudaEventRecord(q0, c.stream);
-#define CAPSSA_PART_LAUNCH(LRN, SM)                                                            \
-    do {                                                                                       \
-        cudaFuncSetAttribute(partition_kernel<LRN, SM>,                                        \
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);           \
-        partition_kernel<LRN, SM><<<grid, 256, dyn, c.stream>>>(                               \
-            sorted, (uint32_t)m, P, a.lim, lf, a.max_ctx, piv_pos, piv_lim, piv_x, n_piv, p,  \
-            wbf, bucket_of, sizes, pstats);                                                    \
-    } while (0)
-    if (learned) {
-        if (in_smem)
-            CAPSSA_PART_LAUNCH(true, true);
-        else
-            CAPSSA_PART_LAUNCH(true, false);
-    } else {
-        if (in_smem)
-            CAPSSA_PART_LAUNCH(false, true);
-        else
-            CAPSSA_PART_LAUNCH(false, false);
-    }
-#undef CAPSSA_PART_LAUNCH
+    // every position in text order (full text) or the sorted subset
+    const uint32_t *items = subset ? sorted : nullptr;
+    if (learned)
+        partition_kernel<true><<<grid, 256, smem, c.stream>>>(items, (uint32_t)m, P, hkey,
+                                                              piv_key, n_piv, p, wbf, bucket_of,
+                                                              sizes, pstats);
+    else
+        partition_kernel<false><<<grid, 256, smem, c.stream>>>(items, (uint32_t)m, P, hkey,
+                                                               piv_key, n_piv, p, wbf, bucket_of,
+                                                               sizes, pstats);
     CAPSSA_LAUNCHED(c);
     cudaEventRecord(q1, c.stream);
     int *bad = c.d_flags + 1;
     CAPSSA_CUDA(c, cudaMemsetAsync(bad, 0, 4, c.stream));
-    partition_check_kernel<<<grid_for(m, 256), 256, 0, c.stream>>>(bucket_of, (uint32_t)m, bad);
+    partition_check_kernel<<<grid_for(m, 256), 256, 0, c.stream>>>(
+        bucket_of, subset ? nullptr : sa_full, (uint32_t)m, bad);
     CAPSSA_LAUNCHED(c);
     std::vector<unsigned long long> h_sizes((size_t)p + 4);
     std::vector<uint32_t> h_piv(n_piv + 1);
