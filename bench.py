@@ -75,6 +75,22 @@ def dist_init():
     return rank, ws, local, dist
 
 
+def max_over_ranks(x, dist, device):
+    """The largest value of x over all ranks (x itself without a process
+    group): the job's time is its slowest replica's."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(n_per_rank, world, steps, elapsed_s):
+    """Whole-job Msuffixes/s: every rank's suffixes over the max-over-ranks time."""
+    return n_per_rank * world * steps / elapsed_s / 1e6
+
+
 # ------------------------------------------------------------------ clocks
 
 class ClockSampler:
@@ -358,12 +374,9 @@ def run_ours(args):
         dist.barrier()
     elapsed_ms = ev0.elapsed_time(ev1)
     clk = clocks.stop()
-    if dist is not None:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(elapsed_ms, dist, "cuda")
     ms_per_step = elapsed_ms / args.steps
-    value = n * ws * args.steps / (elapsed_ms / 1e3) / 1e6
+    value = job_throughput(n, ws, args.steps, elapsed_ms / 1e3)
 
     # roofline of the dominant kernel: one onesweep radix pass over the n
     # suffix records reads and writes each record once (8 B when the
@@ -394,11 +407,8 @@ def run_ours(args):
             ctx.build_in_memory(h_text.numpy(), out=h_out.numpy().view(np.uint32))
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
-        if dist is not None:
-            t = torch.tensor([el], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            el = float(t.item())
-        e2e = {"value": n * ws * args.steps / el / 1e6, "unit": "Msuffixes/s",
+        el = max_over_ranks(el, dist, "cuda")
+        e2e = {"value": job_throughput(n, ws, args.steps, el), "unit": "Msuffixes/s",
                "h2d_bytes_per_step": int(n), "d2h_bytes_per_step": int(4 * n),
                "ms_per_step": el / args.steps * 1e3}
         if not np.array_equal(h_out.numpy().view(np.uint32), sa_dev.cpu().numpy().view(np.uint32)):

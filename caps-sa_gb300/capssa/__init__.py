@@ -137,6 +137,7 @@ def _load():
     L.capssa_ctx_workspace_bytes.restype = u64
     L.capssa_ctx_trim.argtypes = [vp]
     L.capssa_cdf_grad.argtypes = [vp, vp, vp, vp, u64, vp, vp]
+    L.capssa_selftest_bounded_wait.argtypes = [vp, C.c_uint32]
     L.capssa_cdf_train.argtypes = [vp, vp, vp, u64, i32, vp, vp]
     L.capssa_ctx_set_stream.argtypes = [vp, vp]
     L.capssa_opts_default.argtypes = [C.POINTER(_Opts)]
@@ -458,6 +459,11 @@ class Context:
                        pv.ctypes.data, sz.ctypes.data))
         k = int(p.value)
         return k, pv[:max(k - 1, 0)], sz[:k]
+
+    def selftest_bounded_wait(self, polls=4096):
+        """Runs a bounded device wait that nothing satisfies; raises the
+        CAPSSA_ETIMEOUT CapsSaError it must produce."""
+        self._check(lib.capssa_selftest_bounded_wait(self._h, int(polls)))
 
     def cdf_grad(self, params, prefixes, targets):
         """(mean squared error, gradient) of the learned CDF model over the

@@ -499,6 +499,18 @@ capssa_status batched_common(Ctx &c, const ST *texts, const uint64_t *offsets, u
 
 }  // namespace
 
+// Failure-detection self-test: waits on a status word that nothing sets,
+// with the same bounded polling as every look-back, then records
+// DEV_LOOKBACK_TIMEOUT (the host call returns CAPSSA_ETIMEOUT).
+__global__ void bounded_wait_kernel(const unsigned long long *word, uint32_t polls, int *err) {
+    if (threadIdx.x != 0) return;
+    for (uint32_t i = 0; i < polls; i++) {
+        if (*(const volatile unsigned long long *)word != 0ull) return;
+        __nanosleep(64);
+    }
+    atomicCAS(err, DEV_OK, DEV_LOOKBACK_TIMEOUT);
+}
+
 __global__ void widen_u32_u64_kernel(const uint32_t *in, uint64_t *out, uint64_t n) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x)
@@ -870,6 +882,19 @@ extern "C" {
 DEFINE_FOR_S(u8, uint8_t)
 DEFINE_FOR_S(u16, uint16_t)
 DEFINE_FOR_S(u32, uint32_t)
+
+capssa_status capssa_selftest_bounded_wait(capssa_ctx *ctx, uint32_t polls) {
+    CTX_OR_EINVAL(ctx);
+    if (polls == 0 || polls > (1u << 20))
+        return scope.finish(set_err(c, CAPSSA_EINVAL, "polls must be 1..2^20"));
+    unsigned long long *word = (unsigned long long *)ws_get(c, WS_MISC, 64);
+    if (!word) return scope.finish(set_err(c, CAPSSA_ENOMEM, "self-test word"));
+    if (cudaMemsetAsync(word, 0, 64, c.stream) != cudaSuccess)
+        return scope.finish(set_err(c, CAPSSA_ECUDA, "self-test word clear"));
+    bounded_wait_kernel<<<1, 32, 0, c.stream>>>(word, polls, c.d_flags);
+    c.launches++;
+    return scope.finish(CAPSSA_OK);
+}
 
 capssa_status capssa_cdf_grad(capssa_ctx *ctx, const float *params, const uint64_t *prefixes,
                               const float *targets, uint64_t n, float *grad, float *loss) {

@@ -355,6 +355,12 @@ CAPSSA_DECL_PLAN(u32, uint32_t)
  * initialisation (the training the learned partition runs); writes the
  * trained parameters and the final loss.
  * ------------------------------------------------------------------- */
+/* Failure-detection self-test (no reference counterpart): one kernel
+ * waits on a device word that nothing sets, polling `polls` times (1..2^20)
+ * with the bounded wait every look-back uses, and gives up; the call returns
+ * CAPSSA_ETIMEOUT and the context stays usable.  No GPU fault is involved. */
+capssa_status capssa_selftest_bounded_wait(capssa_ctx *ctx, uint32_t polls);
+
 #define CAPSSA_CDF_PARAMS 257
 capssa_status capssa_cdf_grad(capssa_ctx *ctx, const float *params, const uint64_t *prefixes,
                               const float *targets, uint64_t n, float *grad, float *loss);

@@ -430,3 +430,14 @@ def test_bucket_front_end_text_alphabet(ctx):
     t = rng.integers(0, 20, (1 << 22) + 99).astype(np.uint8)
     t[5000:25000] = 7
     check_against_oracle(ctx, t, partition=capssa.Partition.SPLITTERS)
+
+
+def test_bounded_wait_times_out_and_context_survives(ctx):
+    """Failure detection without a GPU fault: a device wait that nothing
+    satisfies gives up after its poll limit, the call reports ETIMEOUT, and
+    the same context keeps working."""
+    with pytest.raises(capssa.CapsSaError) as ei:
+        ctx.selftest_bounded_wait(4096)
+    assert ei.value.status == capssa.Status.ETIMEOUT
+    t = np.frombuffer(b"mississippi", np.uint8)
+    assert ctx.build_in_memory(t).tolist() == py_brute(b"mississippi")
