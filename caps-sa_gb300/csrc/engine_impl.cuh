@@ -421,7 +421,11 @@ __global__ void __launch_bounds__(256)
         return run_head(keys, 0, base + m, key, vshift);  // long run or one that began earlier
     };
     uint64_t cnt_lo = 0, cnt_hi = 0;  // 16-bit counts: lists 0..3, lists 4..
-    // pass 1: heads, and how many groups of each list this thread ends
+    uint32_t ends = 0;                 // bit j: key j ends a group that needs refining
+    // only LongerFirst with a length field separates complete ties by position
+    const bool lf_field = lf && !flag_len;
+    // pass 1: heads, and the groups this thread ends (singletons, the bulk,
+    // take the shortest path)
 #pragma unroll 4
     for (int j = 0; j < kInitPer; j++) {
         const uint32_t l = j * 256 + threadIdx.x;
@@ -429,20 +433,27 @@ __global__ void __launch_bounds__(256)
         const uint32_t i = base + l;
         const uint64_t key = sk[l + 1];
         const bool head = (i == 0) || sk[l] != key;
-        const uint32_t g = head ? i : head_of(l, key);
         const bool last = (i == n - 1) || sk[l + 2] != key;
-        bool complete;
-        uint64_t depth;
-        state(key, complete, depth);
+        if (head && last) {
+            hd[i] = i;
+            continue;
+        }
+        const uint32_t g = head ? i : head_of(l, key);
+        bool complete = false;
+        uint64_t depth = (uint64_t)k;
+        if (lf_field || (last && !head)) state(key, complete, depth);
         hd[i] = (complete && lf) ? i : g;
-        if (!complete && last && i > g) {
+        if (!complete && last && !head) {
             const int li = list_of(i - g + 1, depth);
-            if (li == kLists)
+            if (li == kLists) {
                 append_big(G, 0, g, i - g + 1);
-            else if (li < 4)
-                cnt_lo += 1ull << (16 * li);
-            else
-                cnt_hi += 1ull << (16 * (li - 4));
+            } else {
+                if (li < 4)
+                    cnt_lo += 1ull << (16 * li);
+                else
+                    cnt_hi += 1ull << (16 * (li - 4));
+                ends |= 1u << j;
+            }
         }
     }
     uint64_t off_lo, off_hi;
@@ -455,24 +466,17 @@ __global__ void __launch_bounds__(256)
         if (total) s_base[li] = atomicAdd(&G.ctr->n[li][0], total);
     }
     __syncthreads();
-    // pass 2: write the entries
-#pragma unroll 4
-    for (int j = 0; j < kInitPer; j++) {
+    // pass 2: write the entries of the groups found in pass 1
+    for (; ends; ends &= ends - 1) {
+        const int j = __ffs((int)ends) - 1;
         const uint32_t l = j * 256 + threadIdx.x;
-        if (l >= valid) break;
         const uint32_t i = base + l;
         const uint64_t key = sk[l + 1];
-        const bool last = (i == n - 1) || sk[l + 2] != key;
-        if (!last) continue;
         bool complete;
         uint64_t depth;
         state(key, complete, depth);
-        if (complete) continue;
-        const bool head = (i == 0) || sk[l] != key;
-        if (head) continue;
         const uint32_t g = head_of(l, key);
         const int li = list_of(i - g + 1, depth);
-        if (li == kLists) continue;
         uint32_t slot = 0;
 #pragma unroll
         for (int q = 0; q < kLists; q++) {
