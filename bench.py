@@ -308,9 +308,14 @@ def run_forms(ctx, t_dev, n):
     lp3 = capssa.SegmentedText(len(text3), ends3)
     ctx.build_in_memory_for_positions(t3, p3, lp3, out=o3)  # warm
     s_ms = _timed(lambda: ctx.build_in_memory_for_positions(t3, p3, lp3, out=o3), 2)
+    # the same through the GPU filter source (positions selected on the device)
+    ctx.build_in_memory_for_filter(t3, 0, 4, lp3, out=o3)
+    f_ms = _timed(lambda: ctx.build_in_memory_for_filter(t3, 0, 4, lp3, out=o3), 2)
     out["segmented_filtered_2p29"] = {"value": len(pos3) / (s_ms / 1e3) / 1e6,
                                       "unit": "Msuffixes/s", "ms": s_ms,
-                                      "positions": int(len(pos3)), "segments": int(len(ends3))}
+                                      "positions": int(len(pos3)), "segments": int(len(ends3)),
+                                      "filter_source": {"value": len(pos3) / (f_ms / 1e3) / 1e6,
+                                                        "unit": "Msuffixes/s", "ms": f_ms}}
     del t3, p3, o3
     torch.cuda.synchronize()
     return out

@@ -151,6 +151,8 @@ def _load():
                 vp, vp, u64, vp, u64, C.POINTER(_Limits), C.POINTER(_Opts), vp, vp]
             getattr(L, "capssa_merge_%s_%s" % (s, i)).argtypes = [
                 vp, vp, u64, C.POINTER(_Limits), vp, vp, u64, vp, vp, u64, u64, vp, vp]
+            getattr(L, "capssa_build_in_memory_for_filter_%s_%s" % (s, i)).argtypes = [
+                vp, vp, u64, u64, u64, C.POINTER(_Limits), C.POINTER(_Opts), vp, vp]
             getattr(L, "capssa_build_batched_%s_%s" % (s, i)).argtypes = [
                 vp, vp, vp, u64, C.POINTER(_Opts), vp]
         getattr(L, "capssa_build_in_memory_sample_sort_%s" % s).argtypes = [
@@ -437,6 +439,28 @@ class Context:
             return np.concatenate(chunks) if chunks else np.zeros(0, dtype=np.uint64)
         self.try_build_in_memory_sample_sort(text, opts, emit, lp, positions)
         return None
+
+    def build_in_memory_for_filter(self, text, lo, hi, lp=None, opts=None, index=np.uint64,
+                                   out=None):
+        """The positions p with lo <= text[p] < hi in suffix order: the filter
+        source of build_ext_mem_for_filter (src/ext_mem.rs:927-1092), selected on
+        the GPU.  Returns out[:m]."""
+        text, tp, n, s = _text(text)
+        lim = (lp or PlainText(n))._c()
+        o = _copts(opts)
+        idx = np.dtype(index) if out is None else _ptr_len_dtype(out)[2]
+        fn = getattr(lib, "capssa_build_in_memory_for_filter_%s_%s" % (s, _IDX[idx]))
+        m = C.c_uint64(0)
+        if out is None:
+            self._check(fn(self._h, tp, n, int(lo), int(hi), C.byref(lim), C.byref(o), None,
+                           C.byref(m)))
+            out = np.empty(int(m.value), dtype=idx)
+        op, cap, _ = _ptr_len_dtype(out)
+        self._check(fn(self._h, tp, n, int(lo), int(hi), C.byref(lim), C.byref(o), op,
+                       C.byref(m)))
+        if int(m.value) > cap:
+            raise ValueError("output holds %d positions, %d kept" % (cap, int(m.value)))
+        return out[:int(m.value)]
 
     def sample_sort_plan(self, text, opts=None, lp=None, positions=None):
         """The partition plan of build_in_memory_sample_sort (phases 1-3,

@@ -13,6 +13,7 @@
 #include "common.cuh"
 #include "cdf.cuh"
 #include "engine.cuh"
+#include "scan.cuh"
 #include "lcp.cuh"
 #include "radix.cuh"
 
@@ -142,7 +143,7 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 capssa_status stage_in(Ctx &c, int slot, const void *src, size_t bytes, size_t pad, void **out) {
     void *d = ws_get(c, slot, bytes + pad);
     if (!d) return set_err(c, CAPSSA_ENOMEM, "staging buffer");
-    if (bytes) {
+    if (bytes && d != src) {
         bool dev = is_device_ptr(src);
         auto t0 = std::chrono::steady_clock::now();
         CAPSSA_CUDA(c, cudaMemcpyAsync(d, src, bytes,
@@ -434,6 +435,58 @@ __global__ void text_id_kernel(const uint32_t *__restrict__ sa, uint32_t n,
     }
 }
 
+// Positions kept by the symbol range [lo, hi): flag[p] = 1.
+template <typename ST>
+__global__ void filter_flag_kernel(const ST *__restrict__ text, uint64_t n, uint64_t lo,
+                                   uint64_t hi, uint32_t *__restrict__ flag) {
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n;
+         p += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t v = (uint64_t)text[p];
+        flag[p] = (v >= lo && v < hi) ? 1u : 0u;
+    }
+}
+
+// Compaction: every kept p lands at its inclusive count - 1.
+__global__ void filter_scatter_kernel(const uint32_t *__restrict__ incl, uint64_t n,
+                                      uint32_t *__restrict__ pos) {
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n;
+         p += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = incl[p], before = p ? incl[p - 1] : 0u;
+        if (c != before) pos[c - 1] = (uint32_t)p;
+    }
+}
+
+template <typename ST>
+capssa_status filter_common(Ctx &c, const ST *text, uint64_t n, uint64_t lo, uint64_t hi,
+                            const capssa_limits *lp, const capssa_opts *opts, void *out_sa,
+                            int out_bytes, uint64_t *m_out) {
+    if (!m_out) return set_err(c, CAPSSA_EINVAL, "null count output");
+    *m_out = 0;
+    if (n == 0) return CAPSSA_OK;
+    if (!text) return set_err(c, CAPSSA_EINVAL, "null text");
+    if (n > 0xFFFFFFFEull) return set_err(c, CAPSSA_EUNSUPPORTED, "texts of 2^32-1 or more symbols");
+    void *d_text = nullptr;
+    capssa_status s = stage_text(c, text, n, &d_text);
+    if (s != CAPSSA_OK) return s;
+    uint32_t *flag = (uint32_t *)ws_get(c, WS_MISC, n * 4 + 64);
+    uint32_t *pos = (uint32_t *)ws_get(c, WS_MISC2, n * 4 + 64);
+    if (!flag || !pos) return set_err(c, CAPSSA_ENOMEM, "filter workspace");
+    filter_flag_kernel<ST><<<grid_for(n, 256), 256, 0, c.stream>>>((const ST *)d_text, n, lo,
+                                                                    hi, flag);
+    CAPSSA_LAUNCHED(c);
+    s = scan_u32(c, flag, flag, n, /*max_op=*/false, /*inclusive=*/true);
+    if (s != CAPSSA_OK) return s;
+    uint32_t m32 = 0;
+    CAPSSA_CUDA(c, cudaMemcpyAsync(&m32, flag + (n - 1), 4, cudaMemcpyDeviceToHost, c.stream));
+    CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+    *m_out = m32;
+    if (!out_sa || m32 == 0) return CAPSSA_OK;
+    filter_scatter_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(flag, n, pos);
+    CAPSSA_LAUNCHED(c);
+    return build_common<ST>(c, (const ST *)d_text, n, pos, 4, m32, lp, opts, out_sa, out_bytes,
+                            nullptr);
+}
+
 // Many texts: one segmented sort of the concatenation, then a stable split
 // of the global order by text (within one text the segmented comparator is
 // exactly PlainText's).
@@ -664,6 +717,13 @@ uint64_t capssa_ctx_workspace_bytes(const capssa_ctx *ctx) {
     CallScope scope(c);
 
 #define DEFINE_FOR_I(S, ST, I, IT, IB)                                                        \
+    capssa_status capssa_build_in_memory_for_filter_##S##_##I(                                \
+        capssa_ctx *ctx, const ST *text, uint64_t n, uint64_t lo, uint64_t hi,                \
+        const capssa_limits *lp, const capssa_opts *opts, IT *out_sa, uint64_t *m_out) {      \
+        CTX_OR_EINVAL(ctx);                                                                   \
+        return scope.finish(filter_common<ST>(c, text, n, lo, hi, lp, opts, out_sa, IB,       \
+                                              m_out));                                        \
+    }                                                                                         \
     capssa_status capssa_build_in_memory_##S##_##I(capssa_ctx *ctx, const ST *text,           \
                                                    uint64_t n, const capssa_limits *lp,       \
                                                    const capssa_opts *opts, IT *out_sa) {     \

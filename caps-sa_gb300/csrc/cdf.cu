@@ -10,7 +10,7 @@ namespace cdf {
 namespace {
 
 constexpr int kGradThreads = 256;
-constexpr int kGradBlocks = 64;
+constexpr int kGradBlocks = 304;  // two per SM
 
 // One warp handles 32 samples at a time (a lane each); for every hidden
 // unit the four per-unit gradient terms are summed over the warp with
@@ -33,6 +33,9 @@ __global__ void __launch_bounds__(kGradThreads)
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const float inv_n = 1.0f / (float)n;
+    // lane h & 31 keeps the sums of hidden units h and h + 32 in registers
+    float a2[2] = {0.0f, 0.0f}, ab[2] = {0.0f, 0.0f}, a0[2] = {0.0f, 0.0f}, a1[2] = {0.0f, 0.0f};
+    float aloss = 0.0f, adsum = 0.0f;
     for (uint32_t base = warp * 32; base < n; base += nwarps * 32) {
         const uint32_t i = base + lane;
         const bool valid = i < n;
@@ -42,6 +45,7 @@ __global__ void __launch_bounds__(kGradThreads)
             tg = t[i];
         }
         float y = sp[4 * kHidden];
+#pragma unroll 4
         for (int h = 0; h < kHidden; h++) {
             const float z = fmaf(w1[2 * h], f0, fmaf(w1[2 * h + 1], f1, b1[h]));
             y = fmaf(w2[h], fmaxf(z, 0.0f), y);
@@ -49,6 +53,7 @@ __global__ void __launch_bounds__(kGradThreads)
         const float e = valid ? y - tg : 0.0f;
         const float dy = 2.0f * e * inv_n;
         float le = e * e, dsum = dy;
+#pragma unroll 2
         for (int h = 0; h < kHidden; h++) {
             const float z = fmaf(w1[2 * h], f0, fmaf(w1[2 * h + 1], f1, b1[h]));
             const bool on = z > 0.0f;
@@ -63,21 +68,38 @@ __global__ void __launch_bounds__(kGradThreads)
                 gw1 += __shfl_xor_sync(0xffffffffu, gw1, o);
             }
             if (lane == (h & 31)) {
-                atomicAdd(&sg[3 * kHidden + h], gw2);
-                atomicAdd(&sg[2 * kHidden + h], gb1);
-                atomicAdd(&sg[2 * h], gw0);
-                atomicAdd(&sg[2 * h + 1], gw1);
+                if (h < 32) {
+                    a2[0] += gw2;
+                    ab[0] += gb1;
+                    a0[0] += gw0;
+                    a1[0] += gw1;
+                } else {
+                    a2[1] += gw2;
+                    ab[1] += gb1;
+                    a0[1] += gw0;
+                    a1[1] += gw1;
+                }
             }
         }
+        aloss += le;
+        adsum += dsum;
+    }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            le += __shfl_xor_sync(0xffffffffu, le, o);
-            dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
-        }
-        if (lane == 0) {
-            atomicAdd(&sg[4 * kHidden], dsum);
-            atomicAdd(&sg[kParams], le);
-        }
+    for (int o = 16; o > 0; o >>= 1) {
+        aloss += __shfl_xor_sync(0xffffffffu, aloss, o);
+        adsum += __shfl_xor_sync(0xffffffffu, adsum, o);
+    }
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        const int h = lane + 32 * q;
+        atomicAdd(&sg[3 * kHidden + h], a2[q]);
+        atomicAdd(&sg[2 * kHidden + h], ab[q]);
+        atomicAdd(&sg[2 * h], a0[q]);
+        atomicAdd(&sg[2 * h + 1], a1[q]);
+    }
+    if (lane == 0) {
+        atomicAdd(&sg[4 * kHidden], adsum);
+        atomicAdd(&sg[kParams], aloss);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < kParams; i += blockDim.x)

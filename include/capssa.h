@@ -225,6 +225,17 @@ typedef int (*capssa_emit_fn)(void *user, const uint64_t *positions, uint64_t le
         capssa_ctx *ctx, const ST *texts, const uint64_t *offsets, uint64_t n_texts,      \
         const capssa_opts *opts, IT *out_sa);
 
+/* build_ext_mem_for_filter's position source (FilteredSource, bitmap +
+ * popcount select, src/ext_mem.rs:927-1092) for the in-memory builder: the
+ * positions p with lo <= text[p] < hi, sorted by suffix (as
+ * build_in_memory_for_positions_with would sort them), selected on the GPU
+ * by stream compaction.  *m_out = their count; out_sa (capacity >= the
+ * count) may be null to learn the count only. */
+#define CAPSSA_DECL_FILTER(S, ST, I, IT)                                                  \
+    capssa_status capssa_build_in_memory_for_filter_##S##_##I(                            \
+        capssa_ctx *ctx, const ST *text, uint64_t n, uint64_t lo, uint64_t hi,            \
+        const capssa_limits *lp, const capssa_opts *opts, IT *out_sa, uint64_t *m_out);
+
 #define CAPSSA_DECL_ALL_I(S, ST)                                                          \
     CAPSSA_DECL_BUILD(S, ST, u32, uint32_t)                                               \
     CAPSSA_DECL_BUILD(S, ST, u64, uint64_t)                                               \
@@ -236,6 +247,8 @@ typedef int (*capssa_emit_fn)(void *user, const uint64_t *positions, uint64_t le
     CAPSSA_DECL_MERGE(S, ST, u64, uint64_t)                                               \
     CAPSSA_DECL_BATCHED(S, ST, u32, uint32_t)                                             \
     CAPSSA_DECL_BATCHED(S, ST, u64, uint64_t)                                             \
+    CAPSSA_DECL_FILTER(S, ST, u32, uint32_t)                                              \
+    CAPSSA_DECL_FILTER(S, ST, u64, uint64_t)                                              \
     CAPSSA_DECL_SS(S, ST)
 
 CAPSSA_DECL_ALL_I(u8, uint8_t)

@@ -21,7 +21,7 @@ def declared_symbols():
     idx = ["u32", "u64"]
     fam_si = ["capssa_build_in_memory_%s_%s", "capssa_build_in_memory_for_positions_%s_%s",
               "capssa_build_in_memory_lcp_%s_%s", "capssa_merge_%s_%s",
-              "capssa_build_batched_%s_%s"]
+              "capssa_build_batched_%s_%s", "capssa_build_in_memory_for_filter_%s_%s"]
     fam_s = ["capssa_build_in_memory_sample_sort_%s",
              "capssa_build_in_memory_sample_sort_for_positions_%s", "capssa_lcp_%s",
              "capssa_suffix_cmp_%s", "capssa_sample_sort_plan_%s"]

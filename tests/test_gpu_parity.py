@@ -441,3 +441,25 @@ def test_bounded_wait_times_out_and_context_survives(ctx):
     assert ei.value.status == capssa.Status.ETIMEOUT
     t = np.frombuffer(b"mississippi", np.uint8)
     assert ctx.build_in_memory(t).tolist() == py_brute(b"mississippi")
+
+
+@pytest.mark.parametrize("index", [np.uint32, np.uint64])
+def test_filter_source_matches_positions(ctx, index):
+    """build_ext_mem_for_filter's position source on the GPU: the positions
+    with lo <= text[p] < hi, sorted exactly like the same positions passed to
+    build_in_memory_for_positions (segmented, ShorterFirst: canonical ties)."""
+    rng = np.random.default_rng(31)
+    from capssa import workloads
+    t, ends, pos = workloads.segmented_filtered(300000, seed=9, run_max=5000, run_min=500)
+    got = ctx.build_in_memory_for_filter(t, 0, 4, lp=capssa.SegmentedText(len(t), ends),
+                                         index=index)
+    want = ctx.build_in_memory_for_positions(t, pos.astype(index),
+                                             capssa.SegmentedText(len(t), ends))
+    assert got.dtype == np.dtype(index) and np.array_equal(got, want)
+    # plain text, u16 symbols, a middle range; bit-exact against the oracle
+    t2 = rng.integers(0, 700, 50000).astype(np.uint16)
+    got2 = ctx.build_in_memory_for_filter(t2, 100, 400, index=index)
+    keep = np.nonzero((t2 >= 100) & (t2 < 400))[0].astype(index)
+    assert np.array_equal(got2, orc.build_in_memory(t2, keep, index=index))
+    # nothing kept
+    assert len(ctx.build_in_memory_for_filter(t2, 900, 1000, index=index)) == 0
