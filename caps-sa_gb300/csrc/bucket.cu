@@ -215,12 +215,9 @@ capssa_status sort_buckets(Ctx &c, uint64_t *keys, uint32_t *vals, uint64_t *t1k
                            uint64_t *t2k, uint32_t *t2v, uint32_t n, const uint32_t *d_start,
                            const uint32_t *h_start, int low_bits) {
     (void)n;
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(bucket_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)kSmem);
-        attr = true;
-    }
+    // per-device attribute: set on every call (cheap)
+    cudaFuncSetAttribute(bucket_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSmem);
     bucket_sort_kernel<<<(unsigned)c.sm_count, kThreads, kSmem, c.stream>>>(keys, vals, d_start,
                                                                            kBuckets, low_bits);
     CAPSSA_LAUNCHED(c);

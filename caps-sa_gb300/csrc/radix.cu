@@ -35,8 +35,13 @@ namespace radix {
 
 constexpr int kRadix = 256;
 constexpr int kThreads = 256;
+#ifndef CAPSSA_RADIX_ITEMS_KEYS
+#define CAPSSA_RADIX_ITEMS_KEYS 20  // packed records: no value registers, a larger tile
+#endif
 constexpr int kItems = CAPSSA_RADIX_ITEMS;
 constexpr int kTile = kThreads * kItems;
+constexpr int kItemsKeys = CAPSSA_RADIX_ITEMS_KEYS;
+constexpr int kTileKeys = kThreads * kItemsKeys;
 constexpr int kWarps = kThreads / 32;
 constexpr unsigned long long kFlagA = 1ull << 62;
 constexpr unsigned long long kFlagP = 2ull << 62;
@@ -139,9 +144,11 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
                     int *__restrict__ err, uint32_t val_base) {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr bool kVals = MODE != kKeysOnly;
+    constexpr int IT = kVals ? kItems : kItemsKeys;  // records per thread
+    constexpr int TILE = kThreads * IT;
     uint64_t *s_keys = reinterpret_cast<uint64_t *>(smem);
-    uint32_t *s_vals = reinterpret_cast<uint32_t *>(s_keys + kTile);
-    uint32_t *s_whist = s_vals + (kVals ? kTile : 0);  // kWarps * kRadix
+    uint32_t *s_vals = reinterpret_cast<uint32_t *>(s_keys + TILE);
+    uint32_t *s_whist = s_vals + (kVals ? TILE : 0);  // kWarps * kRadix
     uint32_t *s_lstart = s_whist + kWarps * kRadix;  // kRadix
     uint32_t *s_gbase = s_lstart + kRadix;           // kRadix
     uint32_t *s_scan = s_gbase + kRadix;             // kWarps
@@ -153,16 +160,16 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
     for (int i = tid; i < kWarps * kRadix; i += kThreads) s_whist[i] = 0;
     __syncthreads();
     const uint32_t tile = s_tile;
-    const uint32_t base = tile * (uint32_t)kTile;
-    const uint32_t valid = (n - base) < (uint32_t)kTile ? (n - base) : (uint32_t)kTile;
+    const uint32_t base = tile * (uint32_t)TILE;
+    const uint32_t valid = (n - base) < (uint32_t)TILE ? (n - base) : (uint32_t)TILE;
 
-    uint64_t k[kItems];
-    uint32_t v[kItems];
-    uint32_t d[kItems];
-    uint32_t r[kItems];
-    const uint32_t wbase = base + warp * 32 * kItems;
+    uint64_t k[IT];
+    uint32_t v[IT];
+    uint32_t d[IT];
+    uint32_t r[IT];
+    const uint32_t wbase = base + warp * 32 * IT;
 #pragma unroll
-    for (int j = 0; j < kItems; j++) {
+    for (int j = 0; j < IT; j++) {
         uint32_t idx = wbase + j * 32 + lane;
         if (idx < n) {
             k[j] = keys_in[idx];
@@ -179,7 +186,7 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
     const unsigned lt_mask = (1u << lane) - 1u;
 #if CAPSSA_RADIX_RANK == 0
 #pragma unroll
-    for (int j = 0; j < kItems; j++) {
+    for (int j = 0; j < IT; j++) {
         unsigned peers = __match_any_sync(0xffffffffu, d[j]);
         uint32_t pre = __popc(peers & lt_mask);
         uint32_t cnt = wh[d[j]];
@@ -190,7 +197,7 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
     }
 #else
 #pragma unroll
-    for (int j = 0; j < kItems; j++) {
+    for (int j = 0; j < IT; j++) {
 #if CAPSSA_RADIX_RANK == 1
         const unsigned peers = __match_any_sync(0xffffffffu, d[j]);
 #else
@@ -211,7 +218,7 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
         total += c;
     }
     uint32_t counted = total;
-    if (dg == 255) counted -= (uint32_t)kTile - valid;  // drop the padding items
+    if (dg == 255) counted -= (uint32_t)TILE - valid;  // drop the padding items
     unsigned long long *st = status + (size_t)tile * kRadix + dg;
     uint64_t excl = 0;
     if (tile == 0) {
@@ -246,7 +253,7 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
     __syncthreads();
 
 #pragma unroll
-    for (int j = 0; j < kItems; j++) {
+    for (int j = 0; j < IT; j++) {
         uint32_t pos = s_lstart[d[j]] + wh[d[j]] + r[j];
         s_keys[pos] = k[j];
         if (kVals) s_vals[pos] = v[j];
@@ -269,7 +276,8 @@ __global__ void iota_kernel(uint32_t *out, uint32_t n, uint32_t base) {
 }
 
 static size_t pass_smem(bool vals) {
-    return (size_t)kTile * 8 + (vals ? (size_t)kTile * 4 : 0) + (size_t)kWarps * kRadix * 4 +
+    const size_t tile = vals ? (size_t)kTile : (size_t)kTileKeys;
+    return tile * 8 + (vals ? tile * 4 : 0) + (size_t)kWarps * kRadix * 4 +
            (size_t)kRadix * 4 * 2 + (size_t)kWarps * 4;
 }
 
@@ -296,7 +304,8 @@ capssa_status sort_impl(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *ke
         return CAPSSA_OK;
     }
     uint32_t *counts = hist_buffer(c);
-    uint32_t n_tiles = (n + kTile - 1) / kTile;
+    const uint32_t tile_sz = keys_only ? (uint32_t)kTileKeys : (uint32_t)kTile;
+    uint32_t n_tiles = (n + tile_sz - 1) / tile_sz;
     unsigned long long *status = (unsigned long long *)ws_get(
         c, WS_RADIX_STATUS, (size_t)n_tiles * kRadix * sizeof(unsigned long long));
     if (!counts || !status) return set_err(c, CAPSSA_ENOMEM, "radix workspace");
@@ -314,16 +323,14 @@ capssa_status sort_impl(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *ke
                                    c.stream));
     CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
 
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(onesweep_kernel<kPairs>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)pass_smem(true));
-        cudaFuncSetAttribute(onesweep_kernel<kGenVals>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pass_smem(true));
-        cudaFuncSetAttribute(onesweep_kernel<kKeysOnly>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pass_smem(false));
-        attr_set = true;
-    }
+    // function attributes are per device: set them on the context's device
+    // (cheap, and correct when several devices share the process)
+    cudaFuncSetAttribute(onesweep_kernel<kPairs>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)pass_smem(true));
+    cudaFuncSetAttribute(onesweep_kernel<kGenVals>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)pass_smem(true));
+    cudaFuncSetAttribute(onesweep_kernel<kKeysOnly>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)pass_smem(false));
     // per-pass exclusive offsets live in the pinned scratch after the counts
     uint32_t *h_off = h + kMaxPasses * kRadix;
     bool in_b = false;
