@@ -36,7 +36,7 @@ namespace radix {
 constexpr int kRadix = 256;
 constexpr int kThreads = 256;
 #ifndef CAPSSA_RADIX_ITEMS_KEYS
-#define CAPSSA_RADIX_ITEMS_KEYS 20  // packed records: no value registers, a larger tile
+#define CAPSSA_RADIX_ITEMS_KEYS 24  // packed records: no value registers, a larger tile
 #endif
 constexpr int kItems = CAPSSA_RADIX_ITEMS;
 constexpr int kTile = kThreads * kItems;
