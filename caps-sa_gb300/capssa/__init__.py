@@ -511,16 +511,18 @@ class Context:
                                          int(steps), params.ctypes.data, C.byref(loss)))
         return params, float(loss.value)
 
-    def build_batched(self, texts, offsets, index=np.uint32, opts=None):
+    def build_batched(self, texts, offsets, index=np.uint32, opts=None, out=None):
         """Many independent texts: out[offsets[t]:offsets[t+1]] is the SA of
-        texts[offsets[t]:offsets[t+1]] in local positions."""
+        texts[offsets[t]:offsets[t+1]] in local positions.  `out` may be a
+        CUDA tensor (the result then stays on the device)."""
         text, tp, n, s = _text(texts)
         offs = np.ascontiguousarray(offsets, dtype=np.uint64)
-        out = np.empty(n, dtype=index)
-        fn = getattr(lib, "capssa_build_batched_%s_%s" % (s, _IDX[np.dtype(index)]))
+        if out is None:
+            out = np.empty(n, dtype=index)
+        op, _, odt = _ptr_len_dtype(out)
+        fn = getattr(lib, "capssa_build_batched_%s_%s" % (s, _IDX[odt]))
         o = _copts(opts)
-        self._check(fn(self._h, tp, offs.ctypes.data, len(offs) - 1, C.byref(o),
-                       out.ctypes.data))
+        self._check(fn(self._h, tp, offs.ctypes.data, len(offs) - 1, C.byref(o), op))
         return out
 
     # ---- primitives
