@@ -108,7 +108,8 @@ class _Stats(C.Structure):
                 ("sort_passes", C.c_uint32), ("sort_item_bytes", C.c_uint32),
                 ("sort_pass_ms", C.c_double), ("partition_ms", C.c_double),
                 ("train_ms", C.c_double), ("partition_probes", C.c_uint64),
-                ("train_samples", C.c_uint32), ("model_loss", C.c_float)]
+                ("train_samples", C.c_uint32), ("model_loss", C.c_float),
+                ("radix_items", C.c_uint32), ("reserved1", C.c_uint32)]
 
 
 class _Packer(C.Structure):

@@ -634,6 +634,8 @@ capssa_status capssa_ctx_create(capssa_ctx **out, int device) {
                 if (cudaEventCreate(&e) != cudaSuccess) return true;
             for (auto &e : c->kev)
                 if (cudaEventCreate(&e) != cudaSuccess) return true;
+            for (auto &e : c->tune_ev)
+                if (cudaEventCreate(&e) != cudaSuccess) return true;
             return false;
         }()) {
         cudaGetLastError();
@@ -670,6 +672,8 @@ void capssa_ctx_destroy(capssa_ctx *ctx) {
     for (auto &e : c->pev)
         if (e) cudaEventDestroy(e);
     for (auto &e : c->kev)
+        if (e) cudaEventDestroy(e);
+    for (auto &e : c->tune_ev)
         if (e) cudaEventDestroy(e);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;

@@ -124,6 +124,10 @@ struct Ctx {
     cudaEvent_t pev[8] = {};        // phase boundaries of one suffix sort
     cudaEvent_t kev[2 * 16] = {};   // around each radix pass of the initial sort
     int sm_count = 0;
+    // radix autotuner: chosen records per thread by [packed records?][log2 n]
+    // (0 = not tuned yet), and its timing events
+    int radix_shape[2][33] = {};
+    cudaEvent_t tune_ev[2] = {};
     uint64_t launches = 0;
 };
 

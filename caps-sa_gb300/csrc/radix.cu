@@ -23,9 +23,6 @@
 namespace capssa {
 namespace radix {
 
-#ifndef CAPSSA_RADIX_ITEMS
-#define CAPSSA_RADIX_ITEMS 16
-#endif
 #ifndef CAPSSA_RADIX_MIN_BLOCKS
 #define CAPSSA_RADIX_MIN_BLOCKS 3
 #endif
@@ -35,13 +32,6 @@ namespace radix {
 
 constexpr int kRadix = 256;
 constexpr int kThreads = 256;
-#ifndef CAPSSA_RADIX_ITEMS_KEYS
-#define CAPSSA_RADIX_ITEMS_KEYS 24  // packed records: no value registers, a larger tile
-#endif
-constexpr int kItems = CAPSSA_RADIX_ITEMS;
-constexpr int kTile = kThreads * kItems;
-constexpr int kItemsKeys = CAPSSA_RADIX_ITEMS_KEYS;
-constexpr int kTileKeys = kThreads * kItemsKeys;
 constexpr int kWarps = kThreads / 32;
 constexpr unsigned long long kFlagA = 1ull << 62;
 constexpr unsigned long long kFlagP = 2ull << 62;
@@ -135,7 +125,9 @@ __device__ __forceinline__ uint64_t lookback(const unsigned long long *status, u
 // MODE: kPairs (values read), kGenVals (value = val_base + index), kKeysOnly.
 constexpr int kPairs = 0, kGenVals = 1, kKeysOnly = 2;
 
-template <int MODE>
+// IT records per thread (the tile is 256 * IT records): a template
+// parameter so that the tuner below can pick the shape per workload.
+template <int MODE, int IT>
 __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
     onesweep_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
                     uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out,
@@ -144,7 +136,6 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
                     int *__restrict__ err, uint32_t val_base) {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr bool kVals = MODE != kKeysOnly;
-    constexpr int IT = kVals ? kItems : kItemsKeys;  // records per thread
     constexpr int TILE = kThreads * IT;
     uint64_t *s_keys = reinterpret_cast<uint64_t *>(smem);
     uint32_t *s_vals = reinterpret_cast<uint32_t *>(s_keys + TILE);
@@ -275,10 +266,40 @@ __global__ void iota_kernel(uint32_t *out, uint32_t n, uint32_t base) {
         out[i] = base + i;
 }
 
-static size_t pass_smem(bool vals) {
-    const size_t tile = vals ? (size_t)kTile : (size_t)kTileKeys;
+static size_t pass_smem(bool vals, int items) {
+    const size_t tile = (size_t)kThreads * items;
     return tile * 8 + (vals ? tile * 4 : 0) + (size_t)kWarps * kRadix * 4 +
            (size_t)kRadix * 4 * 2 + (size_t)kWarps * 4;
+}
+
+// Tile shapes the tuner tries, per mode (records per thread).
+constexpr int kKeyShapes[3] = {16, 20, 24};
+constexpr int kPairShapes[2] = {12, 16};
+
+template <int MODE, int IT>
+void launch_shape(Ctx &c, const uint64_t *ki, const uint32_t *vi, uint64_t *ko, uint32_t *vo,
+                  uint32_t n, int shift, const uint32_t *offsets, unsigned long long *status,
+                  uint32_t *tile_counter, uint32_t val_base) {
+    const size_t sm = pass_smem(MODE != kKeysOnly, IT);
+    // function attributes are per device: set on the context's device each time
+    cudaFuncSetAttribute(onesweep_kernel<MODE, IT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sm);
+    const unsigned tiles = (n + kThreads * IT - 1) / (kThreads * IT);
+    onesweep_kernel<MODE, IT><<<tiles, kThreads, sm, c.stream>>>(
+        ki, vi, ko, vo, n, shift, offsets, status, tile_counter, c.d_flags, val_base);
+}
+
+void launch_pass(Ctx &c, int mode, int items, const uint64_t *ki, const uint32_t *vi,
+                 uint64_t *ko, uint32_t *vo, uint32_t n, int shift, const uint32_t *offsets,
+                 unsigned long long *status, uint32_t *tile_counter, uint32_t val_base) {
+#define CAPSSA_SHAPE(M, I)                                                                    \
+    if (mode == M && items == I)                                                              \
+        return launch_shape<M, I>(c, ki, vi, ko, vo, n, shift, offsets, status, tile_counter, \
+                                  val_base);
+    CAPSSA_SHAPE(kKeysOnly, 16) CAPSSA_SHAPE(kKeysOnly, 20) CAPSSA_SHAPE(kKeysOnly, 24)
+    CAPSSA_SHAPE(kPairs, 12) CAPSSA_SHAPE(kPairs, 16)
+    CAPSSA_SHAPE(kGenVals, 12) CAPSSA_SHAPE(kGenVals, 16)
+#undef CAPSSA_SHAPE
 }
 
 uint32_t *hist_buffer(Ctx &c) {
@@ -304,8 +325,9 @@ capssa_status sort_impl(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *ke
         return CAPSSA_OK;
     }
     uint32_t *counts = hist_buffer(c);
-    const uint32_t tile_sz = keys_only ? (uint32_t)kTileKeys : (uint32_t)kTile;
-    uint32_t n_tiles = (n + tile_sz - 1) / tile_sz;
+    // status words for the smallest tile any shape uses
+    const uint32_t min_tile = (uint32_t)kThreads * 12;
+    uint32_t n_tiles = (n + min_tile - 1) / min_tile;
     unsigned long long *status = (unsigned long long *)ws_get(
         c, WS_RADIX_STATUS, (size_t)n_tiles * kRadix * sizeof(unsigned long long));
     if (!counts || !status) return set_err(c, CAPSSA_ENOMEM, "radix workspace");
@@ -323,14 +345,6 @@ capssa_status sort_impl(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *ke
                                    c.stream));
     CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
 
-    // function attributes are per device: set them on the context's device
-    // (cheap, and correct when several devices share the process)
-    cudaFuncSetAttribute(onesweep_kernel<kPairs>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)pass_smem(true));
-    cudaFuncSetAttribute(onesweep_kernel<kGenVals>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)pass_smem(true));
-    cudaFuncSetAttribute(onesweep_kernel<kKeysOnly>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)pass_smem(false));
     // per-pass exclusive offsets live in the pinned scratch after the counts
     uint32_t *h_off = h + kMaxPasses * kRadix;
     bool in_b = false;
@@ -356,18 +370,44 @@ capssa_status sort_impl(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *ke
         const uint32_t *vi = in_b ? vals_b : vals_a;
         uint64_t *ko = in_b ? keys_a : keys_b;
         uint32_t *vo = in_b ? vals_a : vals_b;
-        if (keys_only)
-            onesweep_kernel<kKeysOnly><<<n_tiles, kThreads, pass_smem(false), c.stream>>>(
-                ki, nullptr, ko, nullptr, n, begin_bit + 8 * p, offsets, status, tile_counter,
-                c.d_flags, 0);
-        else if (vals_pending)
-            onesweep_kernel<kGenVals><<<n_tiles, kThreads, pass_smem(true), c.stream>>>(
-                ki, vi, ko, vo, n, begin_bit + 8 * p, offsets, status, tile_counter, c.d_flags,
-                val_base);
-        else
-            onesweep_kernel<kPairs><<<n_tiles, kThreads, pass_smem(true), c.stream>>>(
-                ki, vi, ko, vo, n, begin_bit + 8 * p, offsets, status, tile_counter, c.d_flags,
-                val_base);
+        const int mode = keys_only ? kKeysOnly : (vals_pending ? kGenVals : kPairs);
+        const int cls = mode == kKeysOnly ? 1 : 0;
+        int lg = 0;
+        while ((1u << (lg + 1)) <= n && lg < 31) lg++;
+        int &shape = c.radix_shape[cls][lg];
+        if (shape == 0) {
+            // autotuner: the first large pass of this kind and size class runs
+            // every candidate shape on the same input (each writes the same
+            // correct output) and keeps the fastest; small sorts take the
+            // default
+            const int *cand = cls ? kKeyShapes : kPairShapes;
+            const int nc = cls ? 3 : 2;
+            shape = cls ? 24 : 16;
+            if (n >= (1u << 22) && c.tune_ev[0]) {
+                float best = 1e30f;
+                for (int q = 0; q < nc; q++) {
+                    CAPSSA_CUDA(c, cudaMemsetAsync(status, 0, (size_t)n_tiles * kRadix * 8, c.stream));
+                    CAPSSA_CUDA(c, cudaMemsetAsync(tile_counter, 0, 4, c.stream));
+                    cudaEventRecord(c.tune_ev[0], c.stream);
+                    launch_pass(c, mode, cand[q], ki, vi, ko, vo, n, begin_bit + 8 * p, offsets,
+                                status, tile_counter, val_base);
+                    CAPSSA_LAUNCHED(c);
+                    cudaEventRecord(c.tune_ev[1], c.stream);
+                    CAPSSA_CUDA(c, cudaEventSynchronize(c.tune_ev[1]));
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, c.tune_ev[0], c.tune_ev[1]);
+                    if (ms < best) {
+                        best = ms;
+                        shape = cand[q];
+                    }
+                }
+                CAPSSA_CUDA(c, cudaMemsetAsync(status, 0, (size_t)n_tiles * kRadix * 8, c.stream));
+                CAPSSA_CUDA(c, cudaMemsetAsync(tile_counter, 0, 4, c.stream));
+            }
+        }
+        c.stats.radix_items = (uint32_t)shape;
+        launch_pass(c, mode, shape, ki, vi, ko, vo, n, begin_bit + 8 * p, offsets, status,
+                    tile_counter, val_base);
         CAPSSA_LAUNCHED(c);
         if (timed) cudaEventRecord(c.kev[2 * (*passes_run) + 1], c.stream);
         if (passes_run) (*passes_run)++;

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define CAPSSA_ABI_VERSION 2
+#define CAPSSA_ABI_VERSION 3
 
 typedef enum capssa_status {
     CAPSSA_OK = 0,
@@ -131,6 +131,9 @@ typedef struct capssa_stats {
     uint64_t partition_probes;  /* suffix-vs-splitter comparisons of the partition */
     uint32_t train_samples;     /* learned partition: samples the model trained on */
     float model_loss;           /* learned partition: final mean squared CDF error */
+    uint32_t radix_items;       /* records per thread of the radix passes (the context's
+                                   autotuner picks it on its first large sort of each kind) */
+    uint32_t reserved1;
 } capssa_stats;
 
 typedef struct capssa_ctx capssa_ctx;

@@ -61,7 +61,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_defaults(lib):
-    assert lib.capssa_abi_version() == 2
+    assert lib.capssa_abi_version() == 3
 
     class Opts(ctypes.Structure):
         _fields_ = [("max_context", ctypes.c_uint64), ("subproblem_count", ctypes.c_uint64),

@@ -463,3 +463,21 @@ def test_filter_source_matches_positions(ctx, index):
     assert np.array_equal(got2, orc.build_in_memory(t2, keep, index=index))
     # nothing kept
     assert len(ctx.build_in_memory_for_filter(t2, 900, 1000, index=index)) == 0
+
+
+def test_radix_autotuner_picks_a_shape_and_keeps_it():
+    """The context's autotuner times the candidate tile shapes on its first
+    large sort and reuses the choice; the output stays bit-exact."""
+    from capssa import workloads
+    c = capssa.Context(0)
+    try:
+        t = workloads.dna_with_repeats((1 << 22) + 5, seed=21)
+        want = orc.build_in_memory(t)
+        got1 = c.build_in_memory(t)
+        s1 = c.stats()["radix_items"]
+        got2 = c.build_in_memory(t)
+        s2 = c.stats()["radix_items"]
+        assert np.array_equal(got1, want) and np.array_equal(got2, want)
+        assert s1 in (16, 20, 24) and s1 == s2
+    finally:
+        c.close()
