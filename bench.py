@@ -302,7 +302,7 @@ def run_forms(ctx, t_dev, n):
                           "sample": "every 16th text (%d texts, %d symbols)"
                                     % (len(idx), sample_syms)}}
     del c_dev, o_dev
-    # ---- segmented filtered subset (config 3)
+    # ---- segmented, filtered subset: n = 2^29, lognormal segments, symbol < 4 kept
     text3, ends3, pos3 = workloads.segmented_filtered(1 << 29)
     t3 = torch.from_numpy(text3).to("cuda")
     p3 = torch.from_numpy(pos3.view(np.int64)).to("cuda")
