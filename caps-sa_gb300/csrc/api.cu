@@ -19,7 +19,6 @@
 
 namespace capssa {
 
-capssa_status widen_u32_u64(Ctx &c, const uint32_t *in, uint64_t *out, uint64_t n);
 capssa_status presence_u8(Ctx &c, const uint8_t *text, uint64_t n, uint32_t *present);
 
 void *ws_get(Ctx &c, int slot, size_t bytes) {
@@ -74,11 +73,12 @@ capssa_status check_dev_flags(Ctx &c) {
 // at n = 2^28: 17 symbols + a flag = 35 bits, 5 passes), with the position
 // packed below it when key and position fit 64 bits.  Otherwise the widest
 // key holds kmax symbols (kmax*b + bits(kmax) <= 64) and a length field.
-KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits) {
+KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits, int top_bits, uint64_t n_k) {
     KeyGeom g{};
     g.b = b < 1 ? 1 : b;
+    if (n_k == 0 || n_k > n) n_k = n;
     int logn = 0;
-    while (logn < 64 && (n >> logn) > 1) logn++;
+    while (logn < 64 && (n_k >> logn) > 1) logn++;
     // log2(n) / H + 3 symbols (H = symbol entropy in bits, <= b): random
     // suffixes then tie in about n / 2^(3H+1) pairs, which the refinement
     // resolves cheaply
@@ -89,7 +89,7 @@ KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits) {
     // length field (they are refined from depth 0)
     int vbits = 1;
     while (vbits < 32 && (1ull << vbits) < n) vbits++;
-    if (plain && kmin * g.b + 1 + vbits <= 64) {
+    if (plain && top_bits == 0 && kmin * g.b + 1 + vbits <= 64) {
         const int passes = (kmin * g.b + 1 + 7) / 8;
         int k = kmin;
         while ((k + 1) * g.b + 1 <= 8 * passes && (k + 1) * g.b + 1 + vbits <= 64) k++;
@@ -105,20 +105,21 @@ KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits) {
         while ((1 << lb) <= k) lb++;  // bits of 0..k
         return lb;
     };
+    // widest key below the top bits (at least one symbol)
     int kmax = 1;
     for (int k = 1; k * g.b <= 63; k++)
-        if (k * g.b + lbits_of(k) <= 64) kmax = k;
+        if (top_bits + k * g.b + lbits_of(k) <= 64) kmax = k;
     int k = kmax;
     if (kmin < kmax) {
-        int passes = (kmin * g.b + lbits_of(kmin) + 7) / 8;
+        int passes = (top_bits + kmin * g.b + lbits_of(kmin) + 7) / 8;
         k = kmin;
-        while (k + 1 <= kmax && (k + 1) * g.b + lbits_of(k + 1) <= 8 * passes) k++;
+        while (k + 1 <= kmax && top_bits + (k + 1) * g.b + lbits_of(k + 1) <= 8 * passes) k++;
     }
     g.k = k;
     g.lbits = lbits_of(k);
     g.total = g.k * g.b + g.lbits;
     g.flag_len = 0;
-    g.vbits = g.total + vbits <= 64 ? vbits : 0;
+    g.vbits = top_bits + g.total + vbits <= 64 ? vbits : 0;
     return g;
 }
 
@@ -287,7 +288,7 @@ template <typename ST>
 capssa_status build_common(Ctx &c, const ST *text, uint64_t n, const void *positions,
                            int pos_bytes, uint64_t m, const capssa_limits *lp,
                            const capssa_opts *opts, void *out_sa, int out_bytes, void *out_lcp,
-                           const PartRequest *part = nullptr) {
+                           const PartRequest *part = nullptr, uint64_t seg_major_len = 0) {
     if (!text && n) return set_err(c, CAPSSA_EINVAL, "null text");
     if (!out_sa && (positions ? m : n)) return set_err(c, CAPSSA_EINVAL, "null output");
     if (out_bytes == 4 && n > 0xFFFFFFFFull)
@@ -330,6 +331,8 @@ capssa_status build_common(Ctx &c, const ST *text, uint64_t n, const void *posit
     a.out_bytes = out_bytes;
     a.out_lcp = d_lcp;
     a.bucket_front = opts && (opts->flags & CAPSSA_FLAG_BUCKET_FRONT) ? 1 : 0;
+    a.seg_major = seg_major_len ? 1 : 0;
+    a.seg_max_len = seg_major_len;
     if (part) {
         a.part_p = part->p;
         a.part_mode = part->mode;
@@ -417,21 +420,23 @@ capssa_status sample_sort_common(Ctx &c, const ST *text, uint64_t n, const uint6
     return s;
 }
 
-__global__ void text_id_kernel(const uint32_t *__restrict__ sa, uint32_t n,
-                               const uint64_t *__restrict__ offs, uint64_t n_texts,
-                               uint64_t *__restrict__ keys, uint32_t *__restrict__ local) {
+// Segment-major global order -> per-text positions: slot i belongs to the
+// text t with offs[t] <= i < offs[t + 1] (empty texts own no slot), and so
+// does the position it holds.
+template <typename IT>
+__global__ void localize_kernel(const uint32_t *__restrict__ sa, uint32_t n,
+                                const uint64_t *__restrict__ offs, uint64_t n_texts,
+                                IT *__restrict__ out) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint64_t p = sa[i];
-        uint64_t lo = 0, hi = n_texts;  // last t with offs[t] <= p
+        uint64_t lo = 0, hi = n_texts;  // last t with offs[t] <= i
         while (hi - lo > 1) {
             uint64_t mid = (lo + hi) >> 1;
-            if (offs[mid] <= p)
+            if (__ldg(offs + mid) <= i)
                 lo = mid;
             else
                 hi = mid;
         }
-        keys[i] = lo;
-        local[i] = (uint32_t)(p - offs[lo]);
+        out[i] = (IT)(sa[i] - __ldg(offs + lo));
     }
 }
 
@@ -487,9 +492,11 @@ capssa_status filter_common(Ctx &c, const ST *text, uint64_t n, uint64_t lo, uin
                             nullptr);
 }
 
-// Many texts: one segmented sort of the concatenation, then a stable split
-// of the global order by text (within one text the segmented comparator is
-// exactly PlainText's).
+// Many texts: one segmented sort of the concatenation in segment-major
+// order (the text index above the key bits), so every text's suffixes come
+// out contiguous and in that text's own order (within one text the
+// segmented comparator is exactly PlainText's); positions are then made
+// local.
 template <typename ST>
 capssa_status batched_common(Ctx &c, const ST *texts, const uint64_t *offsets, uint64_t n_texts,
                              const capssa_opts *opts, void *out_sa, int out_bytes) {
@@ -509,8 +516,12 @@ capssa_status batched_common(Ctx &c, const ST *texts, const uint64_t *offsets, u
     if (n > 0xFFFFFFFEull) return set_err(c, CAPSSA_EUNSUPPORTED, "texts of 2^32-1 or more symbols");
     std::vector<uint64_t> ends;
     ends.reserve(n_texts);
+    uint64_t longest = 0;
     for (uint64_t t = 1; t <= n_texts; t++)
-        if (off[t] != off[t - 1]) ends.push_back(off[t]);
+        if (off[t] != off[t - 1]) {
+            ends.push_back(off[t]);
+            longest = std::max(longest, off[t] - off[t - 1]);
+        }
     capssa_limits lp{CAPSSA_LIMITS_SEGMENTED, CAPSSA_SHORTER_FIRST, ends.data(), ends.size()};
     uint32_t *d_sa = (uint32_t *)ws_get(c, WS_OUT2, n * 4 + 64);
     if (!d_sa) return set_err(c, CAPSSA_ENOMEM, "batched output");
@@ -518,35 +529,26 @@ capssa_status batched_common(Ctx &c, const ST *texts, const uint64_t *offsets, u
     capssa_opts_default(&o);
     if (opts) o = *opts;
     o.max_context = CAPSSA_UNBOUNDED;
-    capssa_status s = build_common<ST>(c, texts, n, nullptr, 4, 0, &lp, &o, d_sa, 4, nullptr);
+    capssa_status s =
+        build_common<ST>(c, texts, n, nullptr, 4, 0, &lp, &o, d_sa, 4, nullptr, nullptr, longest);
     if (s != CAPSSA_OK) return s;
     void *d_off = nullptr;
     s = stage_in(c, WS_MISC3, off.data(), off.size() * 8, 64, &d_off);
     if (s != CAPSSA_OK) return s;
-    uint64_t *ka = (uint64_t *)ws_get(c, WS_KEYS_A, n * 8);
-    uint64_t *kb = (uint64_t *)ws_get(c, WS_KEYS_B, n * 8);
-    uint32_t *va = (uint32_t *)ws_get(c, WS_VALS_A, n * 4);
-    uint32_t *vb = (uint32_t *)ws_get(c, WS_VALS_B, n * 4);
-    if (!ka || !kb || !va || !vb) return set_err(c, CAPSSA_ENOMEM, "batched split");
-    text_id_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(
-        d_sa, (uint32_t)n, (const uint64_t *)d_off, n_texts, ka, va);
+    // the text index and one symbol must share the 64-bit key
+    if (!c.seg_major_done)
+        return set_err(c, CAPSSA_EUNSUPPORTED, "too many texts for this alphabet width");
+    const bool out_dev = is_device_ptr(out_sa);
+    void *dst = out_dev ? out_sa : ws_get(c, WS_OUT, n * out_bytes + 64);
+    if (!dst) return set_err(c, CAPSSA_ENOMEM, "batched output");
+    if (out_bytes == 4)
+        localize_kernel<uint32_t><<<grid_for(n, 256), 256, 0, c.stream>>>(
+            d_sa, (uint32_t)n, (const uint64_t *)d_off, n_texts, (uint32_t *)dst);
+    else
+        localize_kernel<uint64_t><<<grid_for(n, 256), 256, 0, c.stream>>>(
+            d_sa, (uint32_t)n, (const uint64_t *)d_off, n_texts, (uint64_t *)dst);
     CAPSSA_LAUNCHED(c);
-    int tb = 1;
-    while ((1ull << tb) < n_texts) tb++;
-    bool in_b = false;
-    s = radix::sort_pairs(c, ka, va, kb, vb, (uint32_t)n, 0, tb, false, 0, &in_b);
-    if (s != CAPSSA_OK) return s;
-    const uint32_t *res = in_b ? vb : va;
-    bool out_dev = is_device_ptr(out_sa);
-    if (out_bytes == 4) {
-        return stage_out(c, out_sa, res, n * 4);
-    }
-    uint64_t *w = (uint64_t *)ws_get(c, WS_OUT, n * 8 + 64);
-    if (!w) return set_err(c, CAPSSA_ENOMEM, "batched widen");
-    uint64_t *dst = out_dev ? (uint64_t *)out_sa : w;
-    s = widen_u32_u64(c, res, dst, n);
-    if (s != CAPSSA_OK) return s;
-    if (!out_dev) return stage_out(c, out_sa, w, n * 8);
+    if (!out_dev) return stage_out(c, out_sa, dst, n * out_bytes);
     return CAPSSA_OK;
 }
 
@@ -562,19 +564,6 @@ __global__ void bounded_wait_kernel(const unsigned long long *word, uint32_t pol
         __nanosleep(64);
     }
     atomicCAS(err, DEV_OK, DEV_LOOKBACK_TIMEOUT);
-}
-
-__global__ void widen_u32_u64_kernel(const uint32_t *in, uint64_t *out, uint64_t n) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-         i += (uint64_t)gridDim.x * blockDim.x)
-        out[i] = in[i];
-}
-
-capssa_status widen_u32_u64(Ctx &c, const uint32_t *in, uint64_t *out, uint64_t n) {
-    widen_u32_u64_kernel<<<grid_for(n, 256), 256, 0,
-                           c.stream>>>(in, out, n);
-    CAPSSA_LAUNCHED(c);
-    return CAPSSA_OK;
 }
 
 __global__ void pack_keys_kernel(const uint8_t *__restrict__ text, uint64_t n,

@@ -54,6 +54,20 @@ __device__ __forceinline__ uint64_t first_end_after(const uint64_t *ends, uint64
     return lo;
 }
 
+// Index of the segment holding position p (p < n; PlainText: 0).
+__device__ __forceinline__ uint64_t dev_seg_at(const DevLimits &L, uint64_t p) {
+    if (!L.segmented) return 0;
+    if (L.dir) {
+        uint64_t block = p >> L.block_shift;
+        uint64_t lo = __ldg(L.dir + block);
+        uint64_t hi = __ldg(L.dir + block + 1);
+        if (hi < lo + 1) hi = lo + 1;
+        if (hi > L.n_ends) hi = L.n_ends;
+        return first_end_after(L.ends, lo, hi, p);
+    }
+    return first_end_after(L.ends, 0, L.n_ends, p);
+}
+
 // SegmentedText::lim_at / PlainText::lim_at (src/limits.rs:144-148, 305-328).
 __device__ __forceinline__ uint64_t dev_lim_at(const DevLimits &L, uint64_t p) {
     if (!L.segmented) return L.n - p;
@@ -128,6 +142,8 @@ struct Ctx {
     // (0 = not tuned yet), and its timing events
     int radix_shape[2][33] = {};
     cudaEvent_t tune_ev[2] = {};
+    // the last sort produced segment-major order (every segment contiguous)
+    bool seg_major_done = false;
     uint64_t launches = 0;
 };
 

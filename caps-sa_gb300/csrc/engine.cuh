@@ -41,6 +41,9 @@ struct EngineArgs {
     int out_bytes;         // 4 or 8
     void *out_lcp;         // device or nullptr
     int bucket_front;      // 1: bucket the keys by their top 16 bits first (bucket.cuh)
+    int seg_major;         // 1: sort by (segment, suffix): every segment's suffixes
+                           // contiguous, in their own order (many independent texts)
+    uint64_t seg_max_len;  // seg_major: the longest segment
     // sample-sort partition plan (build_in_memory_sample_sort's phases 1-3,
     // src/ext_mem.rs:1191-1428), computed after the sort when part_p > 0
     uint32_t part_p;         // subproblems
@@ -73,6 +76,9 @@ struct KeyGeom {
 };
 // plain: the limits are PlainText's (only the last k-1 suffixes end early);
 // hbits: entropy of the symbols in bits (<= b).
-KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits);
+// top_bits: bits the caller keeps above the key (a segment index), n_k: the
+// longest run of symbols a key has to tell apart (n when 0).
+KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits, int top_bits = 0,
+                 uint64_t n_k = 0);
 
 }  // namespace capssa

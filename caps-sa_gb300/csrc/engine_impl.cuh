@@ -144,7 +144,8 @@ template <typename S>
 __global__ void __launch_bounds__(kKeyThreads)
     key_kernel(const S *__restrict__ text, uint64_t n, DevLimits L, Coder<S> coder, int b,
                int k, int lbits, int flag_len, int vbits, int lf, int hist_shift,
-               int n_passes, uint64_t *__restrict__ keys, uint32_t *__restrict__ counts) {
+               int n_passes, int seg_shift, uint64_t *__restrict__ keys,
+               uint32_t *__restrict__ counts) {
     __shared__ uint32_t codes[kKeyTile + 64];
     __shared__ uint32_t hist[8 * 256];
     __shared__ uint16_t stab[256];  // u8 texts: the code table, staged
@@ -190,13 +191,18 @@ __global__ void __launch_bounds__(kKeyThreads)
         uint64_t w = 0;
         for (int j = 0; j < k; j++) w = (w << b) | codes[i0 + j];
         uint64_t end = p0 + dev_lim_at(L, p0);  // one past the last symbol of p0's suffix
+        // segment-major keys carry the segment index above the key bits
+        uint64_t seg = seg_shift ? dev_seg_at(L, p0) : 0;
         uint64_t out[kKeyPer];
 #pragma unroll
         for (int e = 0; e < kKeyPer; e++) {
             const uint64_t p = p0 + e;
             uint64_t key = 0;
             if (p < n) {
-                if (p >= end) end = p + dev_lim_at(L, p);
+                if (p >= end) {  // p == end: the next segment starts here
+                    end = p + dev_lim_at(L, p);
+                    seg++;
+                }
                 const uint64_t lim = end - p;
                 uint64_t content = w;
                 int take = k;
@@ -212,6 +218,7 @@ __global__ void __launch_bounds__(kKeyThreads)
                 const uint64_t field = flag_len ? (uint64_t)((take == k) != (lf != 0))
                                                 : (uint64_t)(lf ? k - take : take);
                 key = (content << lbits) | field;
+                if (seg_shift) key |= seg << seg_shift;
                 for (int ps = 0; ps < n_passes; ps++)
                     atomicAdd(&hist[ps * 256 + ((key >> (hist_shift + 8 * ps)) & 255)], 1u);
                 if (vbits) key = (key << vbits) | p;
@@ -1739,7 +1746,16 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
         // within 3% of the code width counts as full (sampling noise)
         hbits = hsum >= 0.97 * b ? (double)b : std::max<double>(hsum, 0.25);
     }
-    const KeyGeom geo = key_geom(b, n, !a.lim.segmented, hbits);
+    // segment-major order: the segment index sits above the key bits, and
+    // the key only has to tell apart the suffixes of one segment
+    int seg_bits =
+        a.seg_major && a.lim.segmented && a.lim.n_ends > 1 ? bits_for(a.lim.n_ends - 1) : 0;
+    if (seg_bits + b + 1 > 64) seg_bits = 0;  // no room: the caller splits by segment itself
+    // one segment is already in segment-major order
+    c.seg_major_done = a.seg_major && (seg_bits > 0 || a.lim.n_ends <= 1);
+    const KeyGeom geo = key_geom(b, n, !a.lim.segmented, hbits, seg_bits,
+                                 seg_bits ? a.seg_max_len : 0);
+    const int sort_bits = geo.total + seg_bits;
     c.stats.key_symbols = geo.k;
     c.stats.key_bits_per_symbol = geo.b;
 
@@ -1757,18 +1773,18 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     // large texts: two passes on the top 16 key bits make 65536 buckets
     // contiguous, then each bucket is sorted on chip (bucket.cuh)
     const int bb = bucket::kBucketBits;
-    const bool msd = a.bucket_front && n >= (1ull << 22) && geo.total > bb + 8;
+    const bool msd = a.bucket_front && !seg_bits && n >= (1ull << 22) && geo.total > bb + 8;
     // otherwise, when key and position fit one word, the sort moves 8 B per
     // suffix and pass instead of 12
     const int vbits = msd ? 0 : geo.vbits;
     const int hist_shift = msd ? geo.total - bb : 0;
-    const int key_passes = msd ? (bb + 7) / 8 : (geo.total + 7) / 8;
+    const int key_passes = msd ? (bb + 7) / 8 : (sort_bits + 7) / 8;
     uint32_t *counts = radix::hist_buffer(c);
     if (!counts) return set_err(c, CAPSSA_ENOMEM, "radix histograms");
     CAPSSA_CUDA(c, cudaMemsetAsync(counts, 0, radix::kMaxPasses * 256 * 4, c.stream));
     key_kernel<S><<<grid_for(n, kKeyTile), kKeyThreads, 0, c.stream>>>(
         text, n, a.lim, coder, geo.b, geo.k, geo.lbits, geo.flag_len, vbits, lf, hist_shift,
-        key_passes, keys_a, counts);
+        key_passes, seg_bits ? geo.total : 0, keys_a, counts);
     CAPSSA_LAUNCHED(c);
     // bit-packed copy of the text for direct comparisons of small groups
     const uint64_t nwords = (n * (uint64_t)geo.b + 63) / 64 + 4;
@@ -1786,9 +1802,9 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     bool in_b = false;
     int passes = 0;
     capssa_status s =
-        vbits ? radix::sort_keys(c, keys_a, keys_b, nn, vbits, vbits + geo.total, &in_b, &passes,
+        vbits ? radix::sort_keys(c, keys_a, keys_b, nn, vbits, vbits + sort_bits, &in_b, &passes,
                                  /*hist_ready=*/true)
-              : radix::sort_pairs(c, keys_a, vals_a, keys_b, vals_b, nn, hist_shift, geo.total,
+              : radix::sort_pairs(c, keys_a, vals_a, keys_b, vals_b, nn, hist_shift, sort_bits,
                                   true, 0, &in_b, &passes, /*hist_ready=*/true);
     if (s != CAPSSA_OK) return s;
     c.stats.sort_passes = (uint32_t)passes;

@@ -53,13 +53,15 @@ def limits_pair(n, ends=None, longer_first=False):
 
 
 def check_against_oracle(ctx, text, positions=None, ends=None, longer_first=False,
-                         max_ctx=orc.UNBOUNDED, index=np.uint32, partition=None):
+                         max_ctx=orc.UNBOUNDED, index=np.uint32, partition=None,
+                         bucket_front=False):
     n = len(text)
     lp, lo = limits_pair(n, ends, longer_first)
     if partition is None:
-        opts = capssa.Opts(max_context=max_ctx)
+        opts = capssa.Opts(max_context=max_ctx, bucket_front=bucket_front)
     else:
-        opts = capssa.ExtMemOpts(max_context=max_ctx, partition=partition)
+        opts = capssa.ExtMemOpts(max_context=max_ctx, partition=partition,
+                                 bucket_front=bucket_front)
     if positions is None:
         got = ctx.build_in_memory(text, lp, opts, index=index)
         want = orc.build_in_memory(text, None, lo, max_ctx, index=index)
@@ -345,6 +347,39 @@ def test_batched_matches_per_text(ctx, index):
         assert got[offs[i]:offs[i + 1]].tolist() == orc.build_in_memory(tx).tolist(), i
 
 
+@pytest.mark.parametrize("dtype,span", [(np.uint8, 256), (np.uint16, 40000),
+                                        (np.uint32, 1 << 31)])
+def test_batched_many_small_texts(ctx, dtype, span):
+    # thousands of texts of 0..6 symbols (empty and one-symbol texts among
+    # them), equal texts repeated, wide alphabets
+    rng = np.random.default_rng(11)
+    lens = rng.integers(0, 7, 3000)
+    texts = [rng.integers(0, 3, L).astype(dtype) * (span // 3) for L in lens]
+    for i in range(0, 3000, 5):
+        texts[i] = texts[0].copy()
+        lens[i] = len(texts[0])
+    cat = np.concatenate(texts).astype(dtype)
+    offs = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+    got = ctx.build_batched(cat, offs, index=np.uint64)
+    for i, tx in enumerate(texts):
+        assert got[offs[i]:offs[i + 1]].tolist() == orc.build_in_memory(tx).tolist(), i
+
+
+def test_batched_device_output_and_long_texts(ctx):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(12)
+    lens = np.array([70000, 1, 0, 120000, 3, 90000])
+    texts = [rng.integers(0, 2, L).astype(np.uint8) for L in lens]
+    texts[3][50000:90000] = texts[0][10000:50000]  # a long repeat across texts
+    cat = np.concatenate(texts)
+    offs = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+    out = torch.empty(int(offs[-1]), dtype=torch.int32, device="cuda")
+    ctx.build_batched(cat, offs, index=np.uint32, out=out)
+    got = out.cpu().numpy().view(np.uint32)
+    for i, tx in enumerate(texts):
+        assert np.array_equal(got[offs[i]:offs[i + 1]], orc.build_in_memory(tx)), i
+
+
 # ---------------------------------------------------------------- packed keys
 
 def test_pack_params_and_keys(ctx, golden):
@@ -411,17 +446,17 @@ def test_bucket_front_end_plain(ctx, dtype):
     the top 16 key bits, on-chip sort of each bucket, oversize buckets by the
     global sort): bit-exact against the oracle."""
     t = _bucket_text((1 << 22) + 12345, seed=11).astype(dtype)
-    opts = capssa.ExtMemOpts(partition=capssa.Partition.SPLITTERS)
-    got = ctx.build_in_memory(t, None, opts)
+    got = ctx.build_in_memory(t, None, capssa.Opts(bucket_front=True))
     assert np.array_equal(got, orc.build_in_memory(t))
+    assert ctx.stats()["partitions"] == 65536  # the front end ran
 
 
 def test_bucket_front_end_star_segments(ctx):
     t = _bucket_text((1 << 22) + 777, seed=12).astype(np.uint8)
     rng = np.random.default_rng(5)
     ends = np.unique(np.concatenate([rng.integers(1, len(t), 300), [len(t)]])).tolist()
-    check_against_oracle(ctx, t, ends=ends, longer_first=True,
-                         partition=capssa.Partition.SPLITTERS)
+    check_against_oracle(ctx, t, ends=ends, longer_first=True, bucket_front=True)
+    assert ctx.stats()["partitions"] == 65536
 
 
 def test_bucket_front_end_text_alphabet(ctx):
@@ -429,7 +464,8 @@ def test_bucket_front_end_text_alphabet(ctx):
     rng = np.random.default_rng(13)
     t = rng.integers(0, 20, (1 << 22) + 99).astype(np.uint8)
     t[5000:25000] = 7
-    check_against_oracle(ctx, t, partition=capssa.Partition.SPLITTERS)
+    check_against_oracle(ctx, t, bucket_front=True)
+    assert ctx.stats()["partitions"] == 65536
 
 
 def test_bounded_wait_times_out_and_context_survives(ctx):
