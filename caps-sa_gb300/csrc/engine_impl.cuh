@@ -133,63 +133,46 @@ struct Coder {
     }
 };
 
+struct Packed {
+    const uint64_t *w;  // MSB-first b-bit codes, zero padded
+    int b;              // bits per symbol
+    int spw;            // whole symbols per 64-bit window
+    uint64_t mask;      // the spw*b leading bits
+};
+
+// 64-bit window of the packed text starting at symbol p.
+__device__ __forceinline__ uint64_t window_at(const Packed &P, uint64_t p) {
+    uint64_t s = p * (uint64_t)P.b;
+    uint64_t wi = s >> 6;
+    uint32_t sh = (uint32_t)(s & 63);
+    uint64_t v = __ldg(P.w + wi);
+    if (sh) v = (v << sh) | (__ldg(P.w + wi + 1) >> (64 - sh));
+    return v & P.mask;
+}
+
 // Composite key of every text position (engine.cuh step 2), with the digit
 // histograms of every radix pass accumulated on the way (so the sort needs
-// no separate histogram read of the keys).  Each thread owns kKeyPer
-// consecutive positions: the k-symbol window slides one symbol per
-// position over codes staged in shared memory, and only suffixes that end
-// inside the window (lim < k) are masked and padded.  With vbits > 0 the
-// position is packed below the key (one 64-bit word per suffix).
-template <typename S>
+// no separate histogram read of the keys).  The k-symbol content of each
+// suffix is read straight from the packed text (two 64-bit loads, shared by
+// the neighbouring threads' positions); only suffixes that end inside the
+// window (lim < k) are masked and padded.  Each thread owns kKeyPer
+// consecutive positions of a tile (the segment end is tracked across
+// them); blocks stride over the tiles and add their histograms to the
+// global counts once.  With vbits > 0 the position is packed below the key
+// (one 64-bit word per suffix).
 __global__ void __launch_bounds__(kKeyThreads)
-    key_kernel(const S *__restrict__ text, uint64_t n, DevLimits L, Coder<S> coder, int b,
-               int k, int lbits, int flag_len, int vbits, int lf, int hist_shift,
-               int n_passes, int seg_shift, uint64_t *__restrict__ keys,
+    key_kernel(Packed P, uint64_t n, DevLimits L, int k, int lbits, int flag_len, int vbits,
+               int lf, int hist_shift, int n_passes, int seg_shift, uint64_t *__restrict__ keys,
                uint32_t *__restrict__ counts) {
-    __shared__ uint32_t codes[kKeyTile + 64];
     __shared__ uint32_t hist[8 * 256];
-    __shared__ uint16_t stab[256];  // u8 texts: the code table, staged
-    const uint64_t t0 = (uint64_t)blockIdx.x * kKeyTile;
     for (int i = threadIdx.x; i < n_passes * 256; i += kKeyThreads) hist[i] = 0;
-    if (sizeof(S) == 1 && coder.table && ((uintptr_t)text & 15) == 0) {
-        // u8: 16 symbols per thread in one 16-byte load (the tile starts on a
-        // 2048-byte boundary of the padded staging buffer), codes from the
-        // shared table
-        for (int i = threadIdx.x; i < 256; i += kKeyThreads) stab[i] = coder.table[i];
-        __syncthreads();
-        const uint8_t *t8 = reinterpret_cast<const uint8_t *>(text);
-        for (int q = threadIdx.x; q * 16 < kKeyTile + k; q += kKeyThreads) {
-            const uint64_t p = t0 + (uint64_t)q * 16;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (p + 16 <= n) {
-                v = *reinterpret_cast<const uint4 *>(t8 + p);
-            } else {
-                uint32_t wv[4] = {0, 0, 0, 0};
-                for (int e = 0; e < 16 && p + e < n; e++) wv[e >> 2] |= (uint32_t)t8[p + e] << (8 * (e & 3));
-                v = make_uint4(wv[0], wv[1], wv[2], wv[3]);
-            }
-            const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-            for (int e = 0; e < 16; e++) {
-                const int i = q * 16 + e;
-                if (i < kKeyTile + 64)
-                    codes[i] = p + e < n ? (uint32_t)stab[(wv[e >> 2] >> (8 * (e & 3))) & 255u] : 0u;
-            }
-        }
-    } else {
-        for (int i = threadIdx.x; i < kKeyTile + k; i += kKeyThreads) {
-            uint64_t p = t0 + i;
-            codes[i] = p < n ? coder(text[p]) : 0u;
-        }
-    }
     __syncthreads();
-    const int i0 = threadIdx.x * kKeyPer;
-    const uint64_t p0 = t0 + i0;
-    const uint64_t kbits = (uint64_t)k * b;
-    const uint64_t kmask = (1ull << kbits) - 1;
-    if (p0 < n) {
-        uint64_t w = 0;
-        for (int j = 0; j < k; j++) w = (w << b) | codes[i0 + j];
+    const int b = P.b;
+    const int kbits = k * b;  // 1..63
+    for (uint64_t t0 = (uint64_t)blockIdx.x * kKeyTile; t0 < n;
+         t0 += (uint64_t)gridDim.x * kKeyTile) {
+        const uint64_t p0 = t0 + (uint64_t)threadIdx.x * kKeyPer;
+        if (p0 >= n) continue;
         uint64_t end = p0 + dev_lim_at(L, p0);  // one past the last symbol of p0's suffix
         // segment-major keys carry the segment index above the key bits
         uint64_t seg = seg_shift ? dev_seg_at(L, p0) : 0;
@@ -203,14 +186,17 @@ __global__ void __launch_bounds__(kKeyThreads)
                     end = p + dev_lim_at(L, p);
                     seg++;
                 }
+                const uint64_t bit = p * (uint64_t)b;
+                const uint64_t wi = bit >> 6;
+                const uint32_t sh = (uint32_t)(bit & 63);
+                const uint64_t w0 = __ldg(P.w + wi), w1 = __ldg(P.w + wi + 1);
+                uint64_t content = ((w0 << sh) | ((w1 >> 1) >> (63 - sh))) >> (64 - kbits);
                 const uint64_t lim = end - p;
-                uint64_t content = w;
                 int take = k;
                 if (lim < (uint64_t)k) {
                     take = (int)lim;
-                    uint64_t low = (uint64_t)(k - take) * b;
-                    uint64_t lowmask = (1ull << low) - 1;
-                    content = lf ? (w | lowmask) : (w & ~lowmask);
+                    const uint64_t lowmask = (1ull << ((k - take) * b)) - 1;
+                    content = lf ? (content | lowmask) : (content & ~lowmask);
                 }
                 // length field: symbols taken (ShorterFirst) or missing
                 // (LongerFirst); or one flag that orders an early end first
@@ -219,12 +205,16 @@ __global__ void __launch_bounds__(kKeyThreads)
                                                 : (uint64_t)(lf ? k - take : take);
                 key = (content << lbits) | field;
                 if (seg_shift) key |= seg << seg_shift;
-                for (int ps = 0; ps < n_passes; ps++)
-                    atomicAdd(&hist[ps * 256 + ((key >> (hist_shift + 8 * ps)) & 255)], 1u);
+                const uint64_t hk = key >> hist_shift;
+                const uint32_t lo = (uint32_t)hk, hi = (uint32_t)(hk >> 32);
+#pragma unroll
+                for (int ps = 0; ps < 8; ps++)
+                    if (ps < n_passes)
+                        atomicAdd(&hist[ps * 256 + (((ps < 4 ? lo : hi) >> (8 * (ps & 3))) & 255u)],
+                                  1u);
                 if (vbits) key = (key << vbits) | p;
             }
             out[e] = key;
-            w = ((w << b) | codes[i0 + e + k]) & kmask;
         }
         if (p0 + kKeyPer <= n) {
             uint4 *dst = reinterpret_cast<uint4 *>(keys + p0);
@@ -636,23 +626,6 @@ __global__ void sort_small_kernel(const uint4 *__restrict__ groups, uint32_t cou
 // but on a bit-packed copy of the text: one 64-bit window holds 64/b
 // symbols (32 for DNA), so a suffix pair that differs within ~100 symbols
 // costs a few sector reads instead of several rank-doubling rounds.
-struct Packed {
-    const uint64_t *w;  // MSB-first b-bit codes, zero padded
-    int b;              // bits per symbol
-    int spw;            // whole symbols per 64-bit window
-    uint64_t mask;      // the spw*b leading bits
-};
-
-// 64-bit window of the packed text starting at symbol p.
-__device__ __forceinline__ uint64_t window_at(const Packed &P, uint64_t p) {
-    uint64_t s = p * (uint64_t)P.b;
-    uint64_t wi = s >> 6;
-    uint32_t sh = (uint32_t)(s & 63);
-    uint64_t v = __ldg(P.w + wi);
-    if (sh) v = (v << sh) | (__ldg(P.w + wi + 1) >> (64 - sh));
-    return v & P.mask;
-}
-
 // Sequential reader of b-bit symbols from the packed text: one 64-bit
 // load per window after the first.
 struct PackedStream {
@@ -780,6 +753,49 @@ __global__ void pack_text_kernel(const S *__restrict__ text, uint64_t n, Coder<S
                 v |= shift < 64 ? (c << shift) : 0ull;
             else
                 v |= c >> (-shift);
+        }
+        words[w] = v;
+    }
+}
+
+// pack_text_kernel for u8 text (16-byte aligned) whose code width b divides
+// 64: word w holds exactly the 64 / b symbols from w * 64 / b, read with
+// vector loads and coded through a shared copy of the code table.
+__global__ void __launch_bounds__(256)
+    pack_u8_kernel(const uint8_t *__restrict__ text, uint64_t n, const uint16_t *__restrict__ table,
+                   int b, uint64_t *__restrict__ words, uint64_t nwords) {
+    __shared__ uint16_t stab[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) stab[i] = table[i];
+    __syncthreads();
+    const int spw = 64 / b;  // 64, 32, 16 or 8 symbols
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwords;
+         w += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t s0 = w * (uint64_t)spw;
+        uint64_t v = 0;
+        for (int q = 0; q < spw; q += 16) {
+            const int cnt = spw < 16 ? spw : 16;
+            const uint64_t p = s0 + q;
+            uint32_t wv[4] = {0, 0, 0, 0};
+            if (p + cnt <= n) {
+                if (cnt == 16) {
+                    const uint4 x = *reinterpret_cast<const uint4 *>(text + p);
+                    wv[0] = x.x; wv[1] = x.y; wv[2] = x.z; wv[3] = x.w;
+                } else {
+                    const uint2 x = *reinterpret_cast<const uint2 *>(text + p);
+                    wv[0] = x.x; wv[1] = x.y;
+                }
+            } else {
+                for (int e = 0; e < cnt && p + e < n; e++)
+                    wv[e >> 2] |= (uint32_t)text[p + e] << (8 * (e & 3));
+            }
+#pragma unroll
+            for (int e = 0; e < 16; e++) {
+                if (e < cnt) {
+                    const uint32_t c =
+                        p + e < n ? (uint32_t)stab[(wv[e >> 2] >> (8 * (e & 3))) & 255u] : 0u;
+                    v = (v << b) | c;
+                }
+            }
         }
         words[w] = v;
     }
@@ -1782,22 +1798,27 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     uint32_t *counts = radix::hist_buffer(c);
     if (!counts) return set_err(c, CAPSSA_ENOMEM, "radix histograms");
     CAPSSA_CUDA(c, cudaMemsetAsync(counts, 0, radix::kMaxPasses * 256 * 4, c.stream));
-    key_kernel<S><<<grid_for(n, kKeyTile), kKeyThreads, 0, c.stream>>>(
-        text, n, a.lim, coder, geo.b, geo.k, geo.lbits, geo.flag_len, vbits, lf, hist_shift,
-        key_passes, seg_bits ? geo.total : 0, keys_a, counts);
-    CAPSSA_LAUNCHED(c);
-    // bit-packed copy of the text for direct comparisons of small groups
+    // bit-packed copy of the text: the key windows, and the direct
+    // comparisons of small groups
     const uint64_t nwords = (n * (uint64_t)geo.b + 63) / 64 + 4;
     uint64_t *packed = (uint64_t *)ws_get(c, WS_PACKED, nwords * 8);
     if (!packed) return set_err(c, CAPSSA_ENOMEM, "packed text");
-    pack_text_kernel<S><<<grid_for(nwords, 256), 256, 0, c.stream>>>(text, n, coder, geo.b,
-                                                                     packed, nwords);
+    if (sizeof(S) == 1 && table && 64 % geo.b == 0 && ((uintptr_t)text & 15) == 0)
+        pack_u8_kernel<<<grid_for(nwords, 256), 256, 0, c.stream>>>(
+            (const uint8_t *)text, n, table, geo.b, packed, nwords);
+    else
+        pack_text_kernel<S><<<grid_for(nwords, 256), 256, 0, c.stream>>>(text, n, coder, geo.b,
+                                                                         packed, nwords);
     CAPSSA_LAUNCHED(c);
     Packed P;
     P.w = packed;
     P.b = geo.b;
     P.spw = 64 / geo.b;
     P.mask = P.spw * P.b >= 64 ? ~0ull : (~0ull << (64 - P.spw * P.b));
+    key_kernel<<<std::min<unsigned>(grid_for(n, kKeyTile), c.sm_count * 8), kKeyThreads, 0,
+                 c.stream>>>(P, n, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf, hist_shift,
+                             key_passes, seg_bits ? geo.total : 0, keys_a, counts);
+    CAPSSA_LAUNCHED(c);
     cudaEventRecord(c.pev[1], c.stream);
     bool in_b = false;
     int passes = 0;

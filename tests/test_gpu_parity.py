@@ -117,7 +117,8 @@ def test_empty_and_single(ctx):
 # ---------------------------------------------------------------- random vs oracle
 
 @pytest.mark.parametrize("dtype,sigma", [(np.uint8, 2), (np.uint8, 4), (np.uint8, 6),
-                                         (np.uint8, 255), (np.uint16, 16), (np.uint16, 4000),
+                                         (np.uint8, 16), (np.uint8, 100), (np.uint8, 255),
+                                         (np.uint16, 16), (np.uint16, 4000),
                                          (np.uint32, 32), (np.uint32, 1 << 31)])
 def test_random_plain(ctx, dtype, sigma):
     rng = np.random.default_rng(0xC0FFEE + sigma)
