@@ -313,11 +313,31 @@ def run_forms(ctx, t_dev, n):
     # the same through the GPU filter source (positions selected on the device)
     ctx.build_in_memory_for_filter(t3, 0, 4, lp3, out=o3)
     f_ms = _timed(lambda: ctx.build_in_memory_for_filter(t3, 0, 4, lp3, out=o3), 2)
+    # build_ext_mem_for_filter: host text in, suffix order streamed to a host
+    # callback in 32 MiB batches (host clock around the whole call)
+    sent = [0]
+
+    def sink(batch):
+        sent[0] += len(batch)
+
+    ctx.try_build_ext_mem(text3, None, sink, lp3, keep=(0, 4))  # warm
+    sent[0] = 0
+    t0 = time.perf_counter()
+    ctx.try_build_ext_mem(text3, None, sink, lp3, keep=(0, 4))
+    e_ms = (time.perf_counter() - t0) * 1e3
+    assert sent[0] == len(pos3)
     out["segmented_filtered_2p29"] = {"value": len(pos3) / (s_ms / 1e3) / 1e6,
                                       "unit": "Msuffixes/s", "ms": s_ms,
                                       "positions": int(len(pos3)), "segments": int(len(ends3)),
                                       "filter_source": {"value": len(pos3) / (f_ms / 1e3) / 1e6,
-                                                        "unit": "Msuffixes/s", "ms": f_ms}}
+                                                        "unit": "Msuffixes/s", "ms": f_ms},
+                                      "ext_mem_for_filter": {
+                                          "value": len(pos3) / (e_ms / 1e3) / 1e6,
+                                          "unit": "Msuffixes/s", "ms": e_ms,
+                                          "h2d_bytes": int(text3.nbytes),
+                                          "d2h_bytes": int(8 * len(pos3)),
+                                          "clock": "host, whole call (text upload, build, "
+                                                   "streamed emit)"}}
     del t3, p3, o3
     torch.cuda.synchronize()
     return out

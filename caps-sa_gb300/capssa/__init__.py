@@ -119,6 +119,10 @@ class _Packer(C.Structure):
 
 EMIT_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_uint64), C.c_uint64)
 
+
+class _Checksum128(C.Structure):
+    _fields_ = [("count", C.c_uint64), ("lo", C.c_uint64), ("hi", C.c_uint64)]
+
 _SYM = {np.dtype(np.uint8): "u8", np.dtype(np.uint16): "u16", np.dtype(np.uint32): "u32"}
 _IDX = {np.dtype(np.uint32): "u32", np.dtype(np.uint64): "u64"}
 
@@ -160,11 +164,21 @@ def _load():
             vp, vp, u64, C.POINTER(_Limits), C.POINTER(_Opts), EMIT_FN, vp]
         getattr(L, "capssa_build_in_memory_sample_sort_for_positions_%s" % s).argtypes = [
             vp, vp, u64, vp, u64, C.POINTER(_Limits), C.POINTER(_Opts), EMIT_FN, vp]
+        getattr(L, "capssa_build_ext_mem_%s" % s).argtypes = [
+            vp, vp, u64, C.POINTER(_Limits), C.POINTER(_Opts), EMIT_FN, vp]
+        getattr(L, "capssa_build_ext_mem_for_positions_%s" % s).argtypes = [
+            vp, vp, u64, vp, u64, C.POINTER(_Limits), C.POINTER(_Opts), EMIT_FN, vp]
+        getattr(L, "capssa_build_ext_mem_for_filter_%s" % s).argtypes = [
+            vp, vp, u64, u64, u64, C.POINTER(_Limits), C.POINTER(_Opts), EMIT_FN, vp, vp]
         getattr(L, "capssa_lcp_%s" % s).argtypes = [vp, vp, u64, vp, vp, u64, u64, vp]
         getattr(L, "capssa_sample_sort_plan_%s" % s).argtypes = [
             vp, vp, u64, vp, u64, C.POINTER(_Limits), C.POINTER(_Opts), vp, vp, vp]
         getattr(L, "capssa_suffix_cmp_%s" % s).argtypes = [
             vp, vp, u64, C.POINTER(_Limits), vp, vp, u64, u64, vp]
+    L.capssa_checksum128_init.argtypes = [C.POINTER(_Checksum128)]
+    L.capssa_checksum128_update.argtypes = [C.POINTER(_Checksum128), vp, u64]
+    L.capssa_sa_lcp_records_u32.argtypes = [vp, vp, vp, u64, vp]
+    L.capssa_sa_lcp_records_u64.argtypes = [vp, vp, vp, u64, vp]
     L.capssa_pack_params_u8.argtypes = [vp, vp, u64, i32, u64, C.POINTER(_Packer),
                                         C.POINTER(i32)]
     L.capssa_pack_keys_u8.argtypes = [vp, vp, u64, C.POINTER(_Packer), C.POINTER(_Limits), vp,
@@ -441,6 +455,118 @@ class Context:
         self.try_build_in_memory_sample_sort(text, opts, emit, lp, positions)
         return None
 
+    def try_build_ext_mem(self, text, opts=None, emit=None, lp=None, positions=None, keep=None):
+        """try_build_ext_mem[_with], _for_positions[_with], _for_filter[_with]
+        (src/ext_mem.rs:279-553).  `keep = (lo, hi)` selects the positions p
+        with lo <= text[p] < hi (the filter source; a Python predicate cannot
+        run on the device).  `emit(batch: np.ndarray[u64])` is called in
+        suffix order; raising from it aborts with BuildError.  Returns the
+        number of positions emitted."""
+        err = {}
+
+        def cb(user, ptr, length):
+            try:
+                arr = np.ctypeslib.as_array(ptr, shape=(length,))
+                r = emit(arr)
+                return 0 if r is None or r == 0 or r is True else 1
+            except BaseException as e:  # the callback must not unwind through C
+                err["e"] = e
+                return 1
+
+        cfn = EMIT_FN(cb)
+        st, count = self._ext_mem_call(text, opts, lp, positions, keep, cfn, None)
+        self._check(st, err.get("e"))
+        return count
+
+    def _ext_mem_call(self, text, opts, lp, positions, keep, cfn, user):
+        """One capssa_build_ext_mem* call with a C emit callback: (status, count)."""
+        if callable(keep):
+            raise TypeError("keep must be a (lo, hi) symbol range: predicates run on the GPU")
+        text, tp, n, s = _text(text)
+        lim = (lp or PlainText(n))._c()
+        o = _copts(opts)
+        if keep is not None:
+            if positions is not None:
+                raise ValueError("give positions or keep, not both")
+            lo, hi = keep
+            m = C.c_uint64(0)
+            st = getattr(lib, "capssa_build_ext_mem_for_filter_%s" % s)(
+                self._h, tp, n, int(lo), int(hi), C.byref(lim), C.byref(o), cfn, user,
+                C.byref(m))
+            return st, int(m.value)
+        if positions is None:
+            return getattr(lib, "capssa_build_ext_mem_%s" % s)(
+                self._h, tp, n, C.byref(lim), C.byref(o), cfn, user), n
+        pos = np.ascontiguousarray(positions, dtype=np.uint64)
+        st = getattr(lib, "capssa_build_ext_mem_for_positions_%s" % s)(
+            self._h, tp, n, pos.ctypes.data, len(pos), C.byref(lim), C.byref(o), cfn, user)
+        return st, len(pos)
+
+    def build_ext_mem_to_file(self, path, text, opts=None, lp=None, positions=None, keep=None,
+                              width=8):
+        """The SA file of examples/caps_sa.rs:131-172: the emitted positions
+        appended to `path` as little-endian u64 (width 8) or u32 (width 4)
+        by the library's own C sink (no Python call per batch).  Returns the
+        number of positions written."""
+        if width not in (4, 8):
+            raise ValueError("width must be 4 or 8")
+        libc = C.CDLL(None)
+        libc.fopen.restype = C.c_void_p
+        libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
+        libc.fclose.argtypes = [C.c_void_p]
+        f = libc.fopen(os.fsencode(path), b"wb")
+        if not f:
+            raise OSError("cannot open %s for writing" % path)
+        sink = C.cast(lib.capssa_emit_file_u64 if width == 8 else lib.capssa_emit_file_u32,
+                      EMIT_FN)
+        try:
+            st, count = self._ext_mem_call(text, opts, lp, positions, keep, sink, C.c_void_p(f))
+        finally:
+            closed = libc.fclose(f)
+        if st == Status.EEMIT:
+            raise OSError("writing %s failed (disk full, or a position >= 2^32 for width 4)"
+                          % path)
+        self._check(st)
+        if closed != 0:
+            raise OSError("closing %s failed" % path)
+        return count
+
+    def ext_mem_checksum128(self, text, opts=None, lp=None, positions=None, keep=None):
+        """(count, 128-bit checksum) of the emitted stream, computed by the
+        library's C sink: the ruSTAR replay's regression signal
+        (examples/rustar_segmented_bench.rs:236-245)."""
+        ck = Checksum128()
+        st, _ = self._ext_mem_call(text, opts, lp, positions, keep,
+                                   C.cast(lib.capssa_emit_checksum128, EMIT_FN), C.byref(ck._c))
+        self._check(st)
+        return ck.count, ck.value
+
+    def sa_lcp_records(self, sa, lcp):
+        """SaLcp<I> bucket records (src/ext_bucket.rs:65-108) of an SA and its
+        LCP array, interleaved on the GPU: a structured array with fields
+        pos, lcp (little-endian u32 or u64, 8 or 16 bytes a record)."""
+        sa = np.ascontiguousarray(sa)
+        lcp = np.ascontiguousarray(lcp, dtype=sa.dtype)
+        if sa.dtype not in (np.uint32, np.uint64) or len(lcp) != len(sa):
+            raise ValueError("sa and lcp: equal-length u32 or u64 arrays")
+        w = "<u4" if sa.dtype == np.uint32 else "<u8"
+        out = np.empty(len(sa), dtype=[("pos", w), ("lcp", w)])
+        fn = lib.capssa_sa_lcp_records_u32 if sa.dtype == np.uint32 else lib.capssa_sa_lcp_records_u64
+        self._check(fn(self._h, sa.ctypes.data, lcp.ctypes.data, len(sa), out.ctypes.data))
+        return out
+
+    def build_ext_mem(self, text, opts=None, emit=None, lp=None, positions=None, keep=None):
+        """build_ext_mem[_with|_for_positions[_with]|_for_filter[_with]]
+        (src/ext_mem.rs:289, 315, 370, 399, 472, 503); without `emit` the
+        emitted positions are collected and returned."""
+        if emit is None:
+            chunks = []
+            self.try_build_ext_mem(text, opts, lambda b: chunks.append(b.copy()), lp, positions,
+                                   keep)
+            return np.concatenate(chunks) if chunks else np.zeros(0, dtype=np.uint64)
+        self.try_build_ext_mem(text, opts, emit, lp, positions, keep)
+        return None
+
     def build_in_memory_for_filter(self, text, lo, hi, lp=None, opts=None, index=np.uint64,
                                    out=None):
         """The positions p with lo <= text[p] < hi in suffix order: the filter
@@ -607,6 +733,28 @@ class Context:
 _default = threading.local()
 
 
+class Checksum128:
+    """The order-sensitive 128-bit checksum of an emitted position stream
+    (examples/rustar_segmented_bench.rs:236-245), kept by the library."""
+
+    def __init__(self):
+        self._c = _Checksum128()
+        lib.capssa_checksum128_init(C.byref(self._c))
+
+    def update(self, positions):
+        p = np.ascontiguousarray(positions, dtype=np.uint64)
+        lib.capssa_checksum128_update(C.byref(self._c), p.ctypes.data, len(p))
+        return self
+
+    @property
+    def count(self) -> int:
+        return int(self._c.count)
+
+    @property
+    def value(self) -> int:
+        return (int(self._c.hi) << 64) | int(self._c.lo)
+
+
 def default_context() -> Context:
     if getattr(_default, "ctx", None) is None:
         _default.ctx = Context(0)
@@ -655,6 +803,34 @@ def build_in_memory_sample_sort_for_positions(text, positions, opts=None, emit=N
 
 def build_in_memory_sample_sort_for_positions_with(text, positions, lp, opts=None, emit=None):
     return default_context().build_in_memory_sample_sort(text, opts, emit, lp, positions)
+
+
+def build_ext_mem(text, opts=None, emit=None):
+    return default_context().build_ext_mem(text, opts, emit)
+
+
+def try_build_ext_mem(text, opts, emit):
+    return default_context().try_build_ext_mem(text, opts, emit)
+
+
+def build_ext_mem_with(text, lp, opts=None, emit=None):
+    return default_context().build_ext_mem(text, opts, emit, lp)
+
+
+def build_ext_mem_for_positions(text, positions, opts=None, emit=None):
+    return default_context().build_ext_mem(text, opts, emit, None, positions)
+
+
+def build_ext_mem_for_positions_with(text, positions, lp, opts=None, emit=None):
+    return default_context().build_ext_mem(text, opts, emit, lp, positions)
+
+
+def build_ext_mem_for_filter(text, keep, opts=None, emit=None):
+    return default_context().build_ext_mem(text, opts, emit, None, None, keep)
+
+
+def build_ext_mem_for_filter_with(text, keep, lp, opts=None, emit=None):
+    return default_context().build_ext_mem(text, opts, emit, lp, None, keep)
 
 
 def lcp(text, p, q, max_ctx=UNBOUNDED):

@@ -370,29 +370,14 @@ uint64_t effective_p(uint64_t n, uint64_t requested, int threads) {
     return std::min<uint64_t>(std::max<uint64_t>(raw, 1), n);
 }
 
-// Sample-sort builders: the suffix order on the device, delivered to the
-// caller's emit callback in batches, each batch copied while the previous
-// one is being consumed.
-template <typename ST>
-capssa_status sample_sort_common(Ctx &c, const ST *text, uint64_t n, const uint64_t *positions,
-                                 uint64_t m, const capssa_limits *lp, const capssa_opts *opts,
-                                 capssa_emit_fn emit, void *user) {
-    if (!emit) return set_err(c, CAPSSA_EINVAL, "null emit callback");
-    const uint64_t count = positions ? m : n;
-    if (count == 0) return CAPSSA_OK;
-    uint64_t *d_sa = (uint64_t *)ws_get(c, WS_OUT, count * 8 + 64);
-    if (!d_sa) return set_err(c, CAPSSA_ENOMEM, "output buffer");
-    PartRequest pr{(uint32_t)effective_p(count, opts ? opts->subproblem_count : 0,
-                                         opts ? opts->host_threads : 0),
-                   opts && opts->partition == CAPSSA_PARTITION_LEARNED ? CAPSSA_PARTITION_LEARNED
-                                                                       : CAPSSA_PARTITION_SPLITTERS,
-                   nullptr, nullptr};
-    capssa_status s =
-        build_common<ST>(c, text, n, positions, 8, m, lp, opts, d_sa, 8, nullptr, &pr);
-    if (s != CAPSSA_OK) return s;
-    const uint64_t batch = 1u << 22;  // 4 Mi positions (32 MiB) per emit
-    uint64_t *h = nullptr;
-    CAPSSA_CUDA(c, cudaMallocHost(&h, 2 * batch * 8));
+// Streams `count` device positions to `emit` in batches of 4 Mi (32 MiB),
+// each batch copied to pinned memory while the previous one is consumed.
+capssa_status emit_stream(Ctx &c, const uint64_t *d_sa, uint64_t count, capssa_emit_fn emit,
+                          void *user) {
+    capssa_status s = CAPSSA_OK;
+    const uint64_t batch = 1u << 22;
+    if (!c.h_emit) CAPSSA_CUDA(c, cudaMallocHost(&c.h_emit, 2 * batch * 8));
+    uint64_t *h = c.h_emit;
     cudaEvent_t done[2];
     cudaEventCreateWithFlags(&done[0], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&done[1], cudaEventDisableTiming);
@@ -416,8 +401,51 @@ capssa_status sample_sort_common(Ctx &c, const ST *text, uint64_t n, const uint6
     c.stats.d2h_ms += ms_since(t0);
     cudaEventDestroy(done[0]);
     cudaEventDestroy(done[1]);
-    cudaFreeHost(h);
     return s;
+}
+
+// Sample-sort builders: the suffix order on the device, delivered to the
+// caller's emit callback in batches, each batch copied while the previous
+// one is being consumed.
+template <typename ST>
+capssa_status sample_sort_common(Ctx &c, const ST *text, uint64_t n, const uint64_t *positions,
+                                 uint64_t m, const capssa_limits *lp, const capssa_opts *opts,
+                                 capssa_emit_fn emit, void *user) {
+    if (!emit) return set_err(c, CAPSSA_EINVAL, "null emit callback");
+    const uint64_t count = positions ? m : n;
+    if (count == 0) return CAPSSA_OK;
+    uint64_t *d_sa = (uint64_t *)ws_get(c, WS_OUT, count * 8 + 64);
+    if (!d_sa) return set_err(c, CAPSSA_ENOMEM, "output buffer");
+    PartRequest pr{(uint32_t)effective_p(count, opts ? opts->subproblem_count : 0,
+                                         opts ? opts->host_threads : 0),
+                   opts && opts->partition == CAPSSA_PARTITION_LEARNED ? CAPSSA_PARTITION_LEARNED
+                                                                       : CAPSSA_PARTITION_SPLITTERS,
+                   nullptr, nullptr};
+    capssa_status s =
+        build_common<ST>(c, text, n, positions, 8, m, lp, opts, d_sa, 8, nullptr, &pr);
+    if (s != CAPSSA_OK) return s;
+    return emit_stream(c, d_sa, count, emit, user);
+}
+
+// build_ext_mem* (src/ext_mem.rs:279-553): the same suffix order streamed
+// to `emit`.  The reference spills partition buckets to temp files to bound
+// host RAM; here the whole working set (under 50 bytes per suffix, so under
+// 200 GB for the largest supported text) lives in device memory and the
+// host holds only the text and the two emit batches, so there is nothing
+// to spill and no partition plan to compute.
+template <typename ST>
+capssa_status ext_mem_common(Ctx &c, const ST *text, uint64_t n, const void *positions,
+                             int pos_bytes, uint64_t m, const capssa_limits *lp,
+                             const capssa_opts *opts, capssa_emit_fn emit, void *user) {
+    if (!emit) return set_err(c, CAPSSA_EINVAL, "null emit callback");
+    const uint64_t count = positions ? m : n;
+    if (count == 0) return CAPSSA_OK;
+    uint64_t *d_sa = (uint64_t *)ws_get(c, WS_OUT, count * 8 + 64);
+    if (!d_sa) return set_err(c, CAPSSA_ENOMEM, "output buffer");
+    capssa_status s =
+        build_common<ST>(c, text, n, positions, pos_bytes, m, lp, opts, d_sa, 8, nullptr);
+    if (s != CAPSSA_OK) return s;
+    return emit_stream(c, d_sa, count, emit, user);
 }
 
 // Segment-major global order -> per-text positions: slot i belongs to the
@@ -464,7 +492,8 @@ __global__ void filter_scatter_kernel(const uint32_t *__restrict__ incl, uint64_
 template <typename ST>
 capssa_status filter_common(Ctx &c, const ST *text, uint64_t n, uint64_t lo, uint64_t hi,
                             const capssa_limits *lp, const capssa_opts *opts, void *out_sa,
-                            int out_bytes, uint64_t *m_out) {
+                            int out_bytes, uint64_t *m_out, capssa_emit_fn emit = nullptr,
+                            void *user = nullptr) {
     if (!m_out) return set_err(c, CAPSSA_EINVAL, "null count output");
     *m_out = 0;
     if (n == 0) return CAPSSA_OK;
@@ -485,9 +514,11 @@ capssa_status filter_common(Ctx &c, const ST *text, uint64_t n, uint64_t lo, uin
     CAPSSA_CUDA(c, cudaMemcpyAsync(&m32, flag + (n - 1), 4, cudaMemcpyDeviceToHost, c.stream));
     CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
     *m_out = m32;
-    if (!out_sa || m32 == 0) return CAPSSA_OK;
+    if ((!out_sa && !emit) || m32 == 0) return CAPSSA_OK;
     filter_scatter_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(flag, n, pos);
     CAPSSA_LAUNCHED(c);
+    if (emit)
+        return ext_mem_common<ST>(c, (const ST *)d_text, n, pos, 4, m32, lp, opts, emit, user);
     return build_common<ST>(c, (const ST *)d_text, n, pos, 4, m32, lp, opts, out_sa, out_bytes,
                             nullptr);
 }
@@ -648,6 +679,8 @@ void capssa_ctx_trim(capssa_ctx *ctx) {
         c->bufs[i] = nullptr;
         c->sizes[i] = 0;
     }
+    if (c->h_emit) cudaFreeHost(c->h_emit);
+    c->h_emit = nullptr;
 }
 
 void capssa_ctx_destroy(capssa_ctx *ctx) {
@@ -768,6 +801,34 @@ uint64_t capssa_ctx_workspace_bytes(const capssa_ctx *ctx) {
         if (positions == nullptr && m) return scope.finish(set_err(c, CAPSSA_EINVAL, "null positions")); \
         return scope.finish(plan_common<ST>(c, text, n, positions, m, lp, opts, p_out, pivots, \
                                             sizes));                                          \
+    }                                                                                         \
+    capssa_status capssa_build_ext_mem_##S(capssa_ctx *ctx, const ST *text, uint64_t n,       \
+                                           const capssa_limits *lp, const capssa_opts *opts,  \
+                                           capssa_emit_fn emit, void *user) {                 \
+        CTX_OR_EINVAL(ctx);                                                                   \
+        return scope.finish(                                                                  \
+            ext_mem_common<ST>(c, text, n, nullptr, 8, 0, lp, opts, emit, user));             \
+    }                                                                                         \
+    capssa_status capssa_build_ext_mem_for_positions_##S(                                     \
+        capssa_ctx *ctx, const ST *text, uint64_t n, const uint64_t *positions, uint64_t m,   \
+        const capssa_limits *lp, const capssa_opts *opts, capssa_emit_fn emit, void *user) {  \
+        CTX_OR_EINVAL(ctx);                                                                   \
+        if (!positions && m) return scope.finish(set_err(c, CAPSSA_EINVAL, "null positions")); \
+        if (m == 0) return scope.finish(emit ? CAPSSA_OK : set_err(c, CAPSSA_EINVAL, "null emit callback")); \
+        return scope.finish(                                                                  \
+            ext_mem_common<ST>(c, text, n, positions, 8, m, lp, opts, emit, user));           \
+    }                                                                                         \
+    capssa_status capssa_build_ext_mem_for_filter_##S(                                        \
+        capssa_ctx *ctx, const ST *text, uint64_t n, uint64_t lo, uint64_t hi,                \
+        const capssa_limits *lp, const capssa_opts *opts, capssa_emit_fn emit, void *user,    \
+        uint64_t *m_out) {                                                                    \
+        CTX_OR_EINVAL(ctx);                                                                   \
+        if (!emit) return scope.finish(set_err(c, CAPSSA_EINVAL, "null emit callback"));     \
+        uint64_t m_local = 0;                                                                 \
+        capssa_status st = filter_common<ST>(c, text, n, lo, hi, lp, opts, nullptr, 8,        \
+                                             &m_local, emit, user);                           \
+        if (m_out) *m_out = m_local;                                                          \
+        return scope.finish(st);                                                              \
     }                                                                                         \
     capssa_status capssa_build_in_memory_sample_sort_##S(                                     \
         capssa_ctx *ctx, const ST *text, uint64_t n, const capssa_limits *lp,                 \
@@ -1108,3 +1169,114 @@ capssa_status presence_u8(Ctx &c, const uint8_t *text, uint64_t n, uint32_t *pre
     return CAPSSA_OK;
 }
 }  // namespace capssa
+
+// ------------------------------------------------------------ on-disk formats
+
+namespace capssa {
+namespace {
+
+// SaLcp<I> bucket records (src/ext_bucket.rs:65-108): (pos, lcp) pairs, the
+// device's little-endian words being the record's byte order.
+template <typename IT>
+__global__ void sa_lcp_records_kernel(const IT *__restrict__ sa, const IT *__restrict__ lcp,
+                                      uint64_t n, IT *__restrict__ rec) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        rec[2 * i] = sa[i];
+        rec[2 * i + 1] = lcp[i];
+    }
+}
+
+template <typename IT>
+capssa_status sa_lcp_records(Ctx &c, const IT *sa, const IT *lcp, uint64_t n, void *out) {
+    if (n == 0) return CAPSSA_OK;
+    if (!sa || !lcp || !out) return set_err(c, CAPSSA_EINVAL, "null buffer");
+    void *d_sa = nullptr, *d_lcp = nullptr;
+    capssa_status s = stage_in(c, WS_MISC, sa, n * sizeof(IT), 64, &d_sa);
+    if (s == CAPSSA_OK) s = stage_in(c, WS_MISC2, lcp, n * sizeof(IT), 64, &d_lcp);
+    if (s != CAPSSA_OK) return s;
+    const bool out_dev = is_device_ptr(out);
+    void *d_rec = out_dev ? out : ws_get(c, WS_OUT, 2 * n * sizeof(IT) + 64);
+    if (!d_rec) return set_err(c, CAPSSA_ENOMEM, "record buffer");
+    sa_lcp_records_kernel<IT><<<grid_for(n, 256, 152 * 64), 256, 0, c.stream>>>(
+        (const IT *)d_sa, (const IT *)d_lcp, n, (IT *)d_rec);
+    CAPSSA_LAUNCHED(c);
+    if (!out_dev) return stage_out(c, out, d_rec, 2 * n * sizeof(IT));
+    return CAPSSA_OK;
+}
+
+// Little-endian bytes of `len` values, `width` bytes each, appended to f.
+int write_le(FILE *f, const uint64_t *v, uint64_t len, int width) {
+    unsigned char buf[8 * 4096];
+    while (len) {
+        const uint64_t take = len < 4096 ? len : 4096;
+        for (uint64_t i = 0; i < take; i++) {
+            if (width == 4 && v[i] > 0xFFFFFFFFull) return 1;
+            for (int b = 0; b < width; b++) buf[i * width + b] = (unsigned char)(v[i] >> (8 * b));
+        }
+        if (std::fwrite(buf, (size_t)width, (size_t)take, f) != take) return 1;
+        v += take;
+        len -= take;
+    }
+    return 0;
+}
+
+}  // namespace
+}  // namespace capssa
+
+extern "C" {
+
+// examples/rustar_segmented_bench.rs:236-245: state = 0x6c62272e07bb0142_
+// 62b821756295c58d; per position p: state ^= p, state *= 2^88 + 0x13b
+// (mod 2^128), state ^= p << 64.
+void capssa_checksum128_init(capssa_checksum128 *c) {
+    if (!c) return;
+    c->count = 0;
+    c->hi = 0x6c62272e07bb0142ull;
+    c->lo = 0x62b821756295c58dull;
+}
+
+void capssa_checksum128_update(capssa_checksum128 *c, const uint64_t *positions, uint64_t len) {
+    if (!c || (!positions && len)) return;
+    unsigned __int128 x = ((unsigned __int128)c->hi << 64) | c->lo;
+    const unsigned __int128 prime = ((unsigned __int128)1 << 88) | 0x13b;
+    for (uint64_t i = 0; i < len; i++) {
+        const uint64_t p = positions[i];
+        x ^= p;
+        x *= prime;
+        x ^= (unsigned __int128)p << 64;
+    }
+    c->count += len;
+    c->lo = (uint64_t)x;
+    c->hi = (uint64_t)(x >> 64);
+}
+
+int capssa_emit_checksum128(void *user, const uint64_t *positions, uint64_t len) {
+    if (!user) return 1;
+    capssa_checksum128_update((capssa_checksum128 *)user, positions, len);
+    return 0;
+}
+
+int capssa_emit_file_u64(void *user, const uint64_t *positions, uint64_t len) {
+    if (!user || (!positions && len)) return 1;
+    return write_le((FILE *)user, positions, len, 8);
+}
+
+int capssa_emit_file_u32(void *user, const uint64_t *positions, uint64_t len) {
+    if (!user || (!positions && len)) return 1;
+    return write_le((FILE *)user, positions, len, 4);
+}
+
+capssa_status capssa_sa_lcp_records_u32(capssa_ctx *ctx, const uint32_t *sa, const uint32_t *lcp,
+                                        uint64_t n, void *out_records) {
+    CTX_OR_EINVAL(ctx);
+    return scope.finish(sa_lcp_records<uint32_t>(c, sa, lcp, n, out_records));
+}
+
+capssa_status capssa_sa_lcp_records_u64(capssa_ctx *ctx, const uint64_t *sa, const uint64_t *lcp,
+                                        uint64_t n, void *out_records) {
+    CTX_OR_EINVAL(ctx);
+    return scope.finish(sa_lcp_records<uint64_t>(c, sa, lcp, n, out_records));
+}
+
+}  // extern "C"

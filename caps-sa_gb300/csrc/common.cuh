@@ -144,6 +144,7 @@ struct Ctx {
     cudaEvent_t tune_ev[2] = {};
     // the last sort produced segment-major order (every segment contiguous)
     bool seg_major_done = false;
+    uint64_t *h_emit = nullptr;     // pinned double buffer of the emit stream
     uint64_t launches = 0;
 };
 

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define CAPSSA_ABI_VERSION 3
+#define CAPSSA_ABI_VERSION 4
 
 typedef enum capssa_status {
     CAPSSA_OK = 0,
@@ -239,6 +239,28 @@ typedef int (*capssa_emit_fn)(void *user, const uint64_t *positions, uint64_t le
         capssa_ctx *ctx, const ST *text, uint64_t n, uint64_t lo, uint64_t hi,            \
         const capssa_limits *lp, const capssa_opts *opts, IT *out_sa, uint64_t *m_out);
 
+/* build_ext_mem[_with] / try_* (src/ext_mem.rs:279-338), and the
+ * _for_positions (src/ext_mem.rs:370-453) and _for_filter (keep =
+ * lo <= text[p] < hi, src/ext_mem.rs:472-553) variants: every suffix (or
+ * the given / kept positions) streamed to `emit` in suffix order, host
+ * memory bounded by the text and two 32 MiB emit batches.  The working set
+ * stays in device memory, so nothing is spilled to temp files (the
+ * reference's work_dir / physical_file_count have no counterpart).
+ * _for_filter reports the kept count in *m_out when m_out is not null. */
+#define CAPSSA_DECL_EXTMEM(S, ST)                                                         \
+    capssa_status capssa_build_ext_mem_##S(capssa_ctx *ctx, const ST *text, uint64_t n,   \
+                                           const capssa_limits *lp,                       \
+                                           const capssa_opts *opts, capssa_emit_fn emit,  \
+                                           void *user);                                   \
+    capssa_status capssa_build_ext_mem_for_positions_##S(                                 \
+        capssa_ctx *ctx, const ST *text, uint64_t n, const uint64_t *positions,           \
+        uint64_t m, const capssa_limits *lp, const capssa_opts *opts, capssa_emit_fn emit, \
+        void *user);                                                                      \
+    capssa_status capssa_build_ext_mem_for_filter_##S(                                    \
+        capssa_ctx *ctx, const ST *text, uint64_t n, uint64_t lo, uint64_t hi,            \
+        const capssa_limits *lp, const capssa_opts *opts, capssa_emit_fn emit, void *user, \
+        uint64_t *m_out);
+
 #define CAPSSA_DECL_ALL_I(S, ST)                                                          \
     CAPSSA_DECL_BUILD(S, ST, u32, uint32_t)                                               \
     CAPSSA_DECL_BUILD(S, ST, u64, uint64_t)                                               \
@@ -252,7 +274,8 @@ typedef int (*capssa_emit_fn)(void *user, const uint64_t *positions, uint64_t le
     CAPSSA_DECL_BATCHED(S, ST, u64, uint64_t)                                             \
     CAPSSA_DECL_FILTER(S, ST, u32, uint32_t)                                              \
     CAPSSA_DECL_FILTER(S, ST, u64, uint64_t)                                              \
-    CAPSSA_DECL_SS(S, ST)
+    CAPSSA_DECL_SS(S, ST)                                                                 \
+    CAPSSA_DECL_EXTMEM(S, ST)
 
 CAPSSA_DECL_ALL_I(u8, uint8_t)
 CAPSSA_DECL_ALL_I(u16, uint16_t)
@@ -382,6 +405,39 @@ capssa_status capssa_cdf_grad(capssa_ctx *ctx, const float *params, const uint64
                               const float *targets, uint64_t n, float *grad, float *loss);
 capssa_status capssa_cdf_train(capssa_ctx *ctx, const uint64_t *prefixes, const float *targets,
                                uint64_t n, int32_t steps, float *params, float *loss);
+
+/* ---------------------------------------------------------------------
+ * On-disk formats and emit sinks.
+ *
+ * capssa_emit_file_u64 / capssa_emit_file_u32: capssa_emit_fn sinks that
+ * append each batch to the FILE* passed as `user` as little-endian u64 or
+ * u32 values, the SA files of examples/caps_sa.rs:131-139 (u32) and
+ * :147-172 (u64 stream).  They return nonzero (abort) on a write error, and
+ * _u32 also on a position >= 2^32.
+ *
+ * capssa_checksum128: the order-sensitive 128-bit checksum the ruSTAR
+ * replay prints over an emitted stream (examples/rustar_segmented_bench.rs:
+ * 236-245).  Start from capssa_checksum128_init, feed the positions in
+ * order; capssa_emit_checksum128 is the same as an emit sink
+ * (user = capssa_checksum128 *).
+ *
+ * capssa_sa_lcp_records_{I}: SA and LCP arrays interleaved into SaLcp<I>
+ * bucket records (pos, lcp), little-endian, 8 or 16 bytes each
+ * (src/ext_bucket.rs:65-108), on the GPU; host or device buffers.
+ * ------------------------------------------------------------------- */
+typedef struct capssa_checksum128 {
+    uint64_t count;
+    uint64_t lo, hi; /* the 128-bit state */
+} capssa_checksum128;
+void capssa_checksum128_init(capssa_checksum128 *c);
+void capssa_checksum128_update(capssa_checksum128 *c, const uint64_t *positions, uint64_t len);
+int capssa_emit_checksum128(void *user, const uint64_t *positions, uint64_t len);
+int capssa_emit_file_u64(void *user, const uint64_t *positions, uint64_t len);
+int capssa_emit_file_u32(void *user, const uint64_t *positions, uint64_t len);
+capssa_status capssa_sa_lcp_records_u32(capssa_ctx *ctx, const uint32_t *sa, const uint32_t *lcp,
+                                        uint64_t n, void *out_records);
+capssa_status capssa_sa_lcp_records_u64(capssa_ctx *ctx, const uint64_t *sa, const uint64_t *lcp,
+                                        uint64_t n, void *out_records);
 
 #ifdef __cplusplus
 }

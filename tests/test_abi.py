@@ -24,7 +24,8 @@ def declared_symbols():
               "capssa_build_batched_%s_%s", "capssa_build_in_memory_for_filter_%s_%s"]
     fam_s = ["capssa_build_in_memory_sample_sort_%s",
              "capssa_build_in_memory_sample_sort_for_positions_%s", "capssa_lcp_%s",
-             "capssa_suffix_cmp_%s", "capssa_sample_sort_plan_%s"]
+             "capssa_suffix_cmp_%s", "capssa_sample_sort_plan_%s", "capssa_build_ext_mem_%s",
+             "capssa_build_ext_mem_for_positions_%s", "capssa_build_ext_mem_for_filter_%s"]
     for f in fam_si:
         for s in sym:
             for i in idx:
@@ -61,7 +62,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_defaults(lib):
-    assert lib.capssa_abi_version() == 3
+    assert lib.capssa_abi_version() == 4
 
     class Opts(ctypes.Structure):
         _fields_ = [("max_context", ctypes.c_uint64), ("subproblem_count", ctypes.c_uint64),
