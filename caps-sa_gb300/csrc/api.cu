@@ -73,7 +73,8 @@ capssa_status check_dev_flags(Ctx &c) {
 // at n = 2^28: 17 symbols + a flag = 35 bits, 5 passes), with the position
 // packed below it when key and position fit 64 bits.  Otherwise the widest
 // key holds kmax symbols (kmax*b + bits(kmax) <= 64) and a length field.
-KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits, int top_bits, uint64_t n_k) {
+KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits, int top_bits, uint64_t n_k,
+                 bool allow_flagless) {
     KeyGeom g{};
     g.b = b < 1 ? 1 : b;
     if (n_k == 0 || n_k > n) n_k = n;
@@ -91,6 +92,24 @@ KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits, int top_bits, uint
     while (vbits < 32 && (1ull << vbits) < n) vbits++;
     if (plain && top_bits == 0 && kmin * g.b + 1 + vbits <= 64) {
         const int passes = (kmin * g.b + 1 + 7) / 8;
+        // without the flag, one symbol less than kmin (random ties 2^H times
+        // likelier, still a few percent) when that saves a whole pass
+        const int k2 = kmin - 1;
+        const int passes2 = (k2 * g.b + 7) / 8;
+        if (allow_flagless && k2 >= 2 && passes2 < passes && k2 * g.b + vbits <= 64 &&
+            n >= (1ull << 16)) {
+            int k = k2;
+            while ((k + 1) * g.b <= 8 * passes2 && (k + 1) * g.b <= 63 &&
+                   (k + 1) * g.b + vbits <= 64)
+                k++;
+            g.k = k;
+            g.lbits = 0;
+            g.flag_len = 2;
+            g.total = k * g.b;
+            g.vbits = vbits;
+            g.flagless = 1;
+            return g;
+        }
         int k = kmin;
         while ((k + 1) * g.b + 1 <= 8 * passes && (k + 1) * g.b + 1 + vbits <= 64) k++;
         g.k = k;

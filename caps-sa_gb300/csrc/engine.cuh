@@ -73,12 +73,19 @@ struct KeyGeom {
     int total;     // k*b + lbits
     int flag_len;  // 1: the length field is one "ended early" flag (plain texts)
     int vbits;     // > 0: the position is packed below the key in vbits bits
+    // 1: no length field at all (lbits 0, flag_len 2).  Only for ShorterFirst
+    // plain texts, when the flag bit alone would cost a radix pass: the k - 1
+    // suffixes that end inside the key are left out of the sort and placed
+    // afterwards (a short suffix precedes exactly the full suffixes whose
+    // key is >= its zero-padded key).
+    int flagless;
 };
 // plain: the limits are PlainText's (only the last k-1 suffixes end early);
 // hbits: entropy of the symbols in bits (<= b).
 // top_bits: bits the caller keeps above the key (a segment index), n_k: the
-// longest run of symbols a key has to tell apart (n when 0).
+// longest run of symbols a key has to tell apart (n when 0), allow_flagless:
+// a ShorterFirst plain text may drop the early-end flag (see KeyGeom).
 KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits, int top_bits = 0,
-                 uint64_t n_k = 0);
+                 uint64_t n_k = 0, bool allow_flagless = false);
 
 }  // namespace capssa

@@ -161,18 +161,18 @@ __device__ __forceinline__ uint64_t window_at(const Packed &P, uint64_t p) {
 // global counts once.  With vbits > 0 the position is packed below the key
 // (one 64-bit word per suffix).
 __global__ void __launch_bounds__(kKeyThreads)
-    key_kernel(Packed P, uint64_t n, DevLimits L, int k, int lbits, int flag_len, int vbits,
-               int lf, int hist_shift, int n_passes, int seg_shift, uint64_t *__restrict__ keys,
-               uint32_t *__restrict__ counts) {
+    key_kernel(Packed P, uint64_t n, uint64_t n_rec, DevLimits L, int k, int lbits, int flag_len,
+               int vbits, int lf, int hist_shift, int n_passes, int seg_shift,
+               uint64_t *__restrict__ keys, uint32_t *__restrict__ counts) {
     __shared__ uint32_t hist[8 * 256];
     for (int i = threadIdx.x; i < n_passes * 256; i += kKeyThreads) hist[i] = 0;
     __syncthreads();
     const int b = P.b;
     const int kbits = k * b;  // 1..63
-    for (uint64_t t0 = (uint64_t)blockIdx.x * kKeyTile; t0 < n;
+    for (uint64_t t0 = (uint64_t)blockIdx.x * kKeyTile; t0 < n_rec;
          t0 += (uint64_t)gridDim.x * kKeyTile) {
         const uint64_t p0 = t0 + (uint64_t)threadIdx.x * kKeyPer;
-        if (p0 >= n) continue;
+        if (p0 >= n_rec) continue;
         uint64_t end = p0 + dev_lim_at(L, p0);  // one past the last symbol of p0's suffix
         // segment-major keys carry the segment index above the key bits
         uint64_t seg = seg_shift ? dev_seg_at(L, p0) : 0;
@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(kKeyThreads)
         for (int e = 0; e < kKeyPer; e++) {
             const uint64_t p = p0 + e;
             uint64_t key = 0;
-            if (p < n) {
+            if (p < n_rec) {
                 if (p >= end) {  // p == end: the next segment starts here
                     end = p + dev_lim_at(L, p);
                     seg++;
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(kKeyThreads)
                 // (ShorterFirst) or last (LongerFirst) among equal contents
                 const uint64_t field = flag_len ? (uint64_t)((take == k) != (lf != 0))
                                                 : (uint64_t)(lf ? k - take : take);
-                key = (content << lbits) | field;
+                key = lbits ? (content << lbits) | field : content;
                 if (seg_shift) key |= seg << seg_shift;
                 const uint64_t hk = key >> hist_shift;
                 const uint32_t lo = (uint32_t)hk, hi = (uint32_t)(hk >> 32);
@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(kKeyThreads)
             }
             out[e] = key;
         }
-        if (p0 + kKeyPer <= n) {
+        if (p0 + kKeyPer <= n_rec) {
             uint4 *dst = reinterpret_cast<uint4 *>(keys + p0);
 #pragma unroll
             for (int e = 0; e < kKeyPer; e += 2)
@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(kKeyThreads)
                                         (uint32_t)out[e + 1], (uint32_t)(out[e + 1] >> 32));
         } else {
             for (int e = 0; e < kKeyPer; e++)
-                if (p0 + e < n) keys[p0 + e] = out[e];
+                if (p0 + e < n_rec) keys[p0 + e] = out[e];
         }
     }
     __syncthreads();
@@ -392,6 +392,61 @@ __device__ __forceinline__ uint64_t block_excl_scan64(uint64_t v, uint64_t *excl
     return total;
 }
 
+// The short suffixes of a flagless sort (KeyGeom::flagless), by value: the
+// SA index each sorted record moves up by is the number of short suffixes
+// inserted at or before it (ip[] ascending, one entry per short suffix).
+struct ShortList {
+    uint32_t n;
+    uint32_t ip[63];
+};
+
+__device__ __forceinline__ uint32_t short_shift(const ShortList &S, uint32_t i) {
+    uint32_t c = 0;
+    for (uint32_t j = 0; j < S.n; j++) c += S.ip[j] <= i ? 1u : 0u;
+    return c;
+}
+
+// Key (first lim symbols, zero padded) and insertion point of each short
+// suffix n_rec + j of a flagless sort: the number of sorted records whose
+// key is smaller (a short suffix precedes every full suffix whose key is at
+// least its padded key, ShorterFirst).
+__global__ void short_place_kernel(Packed P, uint64_t n, uint32_t n_rec, int k,
+                                   const uint64_t *__restrict__ recs, int vbits,
+                                   uint32_t *__restrict__ ip_out, uint64_t *__restrict__ key_out) {
+    const uint32_t j = threadIdx.x;
+    if (n_rec + (uint64_t)j >= n) return;
+    const uint64_t sp = n_rec + (uint64_t)j;
+    const int take = (int)(n - sp);  // < k
+    const int kbits = k * P.b;
+    uint64_t key = window_at(P, sp) >> (64 - kbits);
+    key &= ~((1ull << ((k - take) * P.b)) - 1);
+    uint32_t lo = 0, hi = n_rec;
+    while (lo < hi) {
+        const uint32_t mid = lo + ((hi - lo) >> 1);
+        if ((recs[mid] >> vbits) < key)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    ip_out[j] = lo;
+    key_out[j] = key;
+}
+
+// The short suffixes' own SA slots (singleton groups).
+struct ShortSlots {
+    uint32_t n;
+    uint32_t slot[63];
+    uint32_t pos[63];
+};
+
+__global__ void short_write_kernel(ShortSlots W, uint32_t *__restrict__ sa,
+                                   uint32_t *__restrict__ hd) {
+    const uint32_t j = threadIdx.x;
+    if (j >= W.n) return;
+    sa[W.slot[j]] = W.pos[j];
+    hd[W.slot[j]] = W.slot[j];
+}
+
 constexpr int kInitPer = 16;  // sorted keys per thread in init_groups_kernel
 constexpr int kInitTile = 256 * kInitPer;
 
@@ -405,17 +460,22 @@ constexpr int kInitTile = 256 * kInitPer;
 __global__ void __launch_bounds__(256)
     init_groups_kernel(const uint64_t *__restrict__ keys, uint32_t n, int k, uint64_t lmask,
                        int lf, int flag_len, int vshift, uint32_t *__restrict__ hd,
-                       uint32_t *__restrict__ sa_out, GroupLists G) {
+                       uint32_t *__restrict__ sa_out, GroupLists G, ShortList S) {
     static_assert(kLists <= 8, "two packed words of four 16-bit counters");
     __shared__ uint64_t sk[kInitTile + 2];  // sk[l + 1] = key of sorted index base + l
     __shared__ uint32_t s_base[kLists];
     const uint32_t base = blockIdx.x * (uint32_t)kInitTile;
     const uint32_t valid = n - base < (uint32_t)kInitTile ? n - base : (uint32_t)kInitTile;
     const uint64_t vmask = (1ull << vshift) - 1;
+    // SA index of sorted record i: i + (short suffixes inserted at or before
+    // it), one shift for the whole block unless an insertion falls inside
+    const uint32_t sh_lo = S.n ? short_shift(S, base) : 0u;
+    const bool sh_flat = !S.n || short_shift(S, base + valid - 1) == sh_lo;
+    auto shift_of = [&](uint32_t i) { return sh_flat ? sh_lo : short_shift(S, i); };
     for (uint32_t l = threadIdx.x; l < valid; l += 256) {
         const uint64_t item = keys[base + l];
         sk[l + 1] = item >> vshift;
-        if (sa_out) sa_out[base + l] = (uint32_t)(item & vmask);
+        if (sa_out) sa_out[base + l + shift_of(base + l)] = (uint32_t)(item & vmask);
     }
     if (threadIdx.x == 0) sk[0] = base > 0 ? keys[base - 1] >> vshift : 0ull;
     if (threadIdx.x == 32) sk[valid + 1] = base + valid < n ? keys[base + valid] >> vshift : 0ull;
@@ -425,7 +485,10 @@ __global__ void __launch_bounds__(256)
     // (0 for the early-ended suffixes of a flagged plain text)
     auto state = [&](uint64_t key, bool &complete, uint64_t &depth) {
         const uint32_t lenf = (uint32_t)(key & lmask);
-        if (flag_len) {
+        if (flag_len == 2) {  // no length field: every record is a full suffix
+            complete = false;
+            depth = (uint64_t)k;
+        } else if (flag_len) {
             complete = false;
             depth = lenf == (lf ? 0u : 1u) ? (uint64_t)k : 0ull;
         } else {
@@ -459,19 +522,22 @@ __global__ void __launch_bounds__(256)
         const uint64_t key = sk[l + 1];
         const bool head = (i == 0) || sk[l] != key;
         const bool last = (i == n - 1) || sk[l + 2] != key;
+        // an insertion point only ever falls on a group head, so a group
+        // moves by one shift
+        const uint32_t sh = shift_of(i);
         if (head && last) {
-            hd[i] = i;
+            hd[i + sh] = i + sh;
             continue;
         }
         const uint32_t g = head ? i : head_of(l, key);
         bool complete = false;
         uint64_t depth = (uint64_t)k;
         if (lf_field || (last && !head)) state(key, complete, depth);
-        hd[i] = (complete && lf) ? i : g;
+        hd[i + sh] = ((complete && lf) ? i : g) + sh;
         if (!complete && last && !head) {
             const int li = list_of(i - g + 1, depth);
             if (li == kLists) {
-                append_big(G, 0, g, i - g + 1);
+                append_big(G, 0, g + sh, i - g + 1);
             } else {
                 if (li < 4)
                     cnt_lo += 1ull << (16 * li);
@@ -512,7 +578,7 @@ __global__ void __launch_bounds__(256)
                 off += 1ull << sh;
             }
         }
-        list_ptr(G, li, 0)[slot] = group_entry(g, i - g + 1, depth);
+        list_ptr(G, li, 0)[slot] = group_entry(g + shift_of(i), i - g + 1, depth);
     }
 }
 
@@ -1769,8 +1835,14 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     if (seg_bits + b + 1 > 64) seg_bits = 0;  // no room: the caller splits by segment itself
     // one segment is already in segment-major order
     c.seg_major_done = a.seg_major && (seg_bits > 0 || a.lim.n_ends <= 1);
+    // a ShorterFirst plain text may drop the early-end flag when that saves a
+    // radix pass (not with the bucket front end, which sorts key + value)
+    const bool allow_flagless = !a.lim.segmented && !lf && !a.bucket_front && n <= 0xFFFFFFFEull;
     const KeyGeom geo = key_geom(b, n, !a.lim.segmented, hbits, seg_bits,
-                                 seg_bits ? a.seg_max_len : 0);
+                                 seg_bits ? a.seg_max_len : 0, allow_flagless);
+    // records the radix sort orders: every suffix, or the full ones only
+    const uint64_t n_short = geo.flagless ? (uint64_t)geo.k - 1 : 0;
+    const uint64_t n_rec = n - n_short;
     const int sort_bits = geo.total + seg_bits;
     c.stats.key_symbols = geo.k;
     c.stats.key_bits_per_symbol = geo.b;
@@ -1815,16 +1887,16 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     P.b = geo.b;
     P.spw = 64 / geo.b;
     P.mask = P.spw * P.b >= 64 ? ~0ull : (~0ull << (64 - P.spw * P.b));
-    key_kernel<<<std::min<unsigned>(grid_for(n, kKeyTile), c.sm_count * 8), kKeyThreads, 0,
-                 c.stream>>>(P, n, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf, hist_shift,
-                             key_passes, seg_bits ? geo.total : 0, keys_a, counts);
+    key_kernel<<<std::min<unsigned>(grid_for(n_rec, kKeyTile), c.sm_count * 8), kKeyThreads, 0,
+                 c.stream>>>(P, n, n_rec, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf,
+                             hist_shift, key_passes, seg_bits ? geo.total : 0, keys_a, counts);
     CAPSSA_LAUNCHED(c);
     cudaEventRecord(c.pev[1], c.stream);
     bool in_b = false;
     int passes = 0;
     capssa_status s =
-        vbits ? radix::sort_keys(c, keys_a, keys_b, nn, vbits, vbits + sort_bits, &in_b, &passes,
-                                 /*hist_ready=*/true)
+        vbits ? radix::sort_keys(c, keys_a, keys_b, (uint32_t)n_rec, vbits, vbits + sort_bits,
+                                 &in_b, &passes, /*hist_ready=*/true)
               : radix::sort_pairs(c, keys_a, vals_a, keys_b, vals_b, nn, hist_shift, sort_bits,
                                   true, 0, &in_b, &passes, /*hist_ready=*/true);
     if (s != CAPSSA_OK) return s;
@@ -1877,11 +1949,46 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     G.big[0] = (BigGroup *)cursor;
     G.big[1] = G.big[0] + big_cap;
     uint64_t h = (uint64_t)geo.k;
+    // flagless: where the short suffixes go among the sorted full ones
+    ShortList SL{};
+    ShortSlots SW{};
+    if (n_short) {
+        uint32_t *d_ip = (uint32_t *)ws_get(c, WS_SAMPLE, 64 * 12 + 64);
+        if (!d_ip) return set_err(c, CAPSSA_ENOMEM, "short suffixes");
+        uint64_t *d_key = (uint64_t *)(d_ip + 64);
+        short_place_kernel<<<1, 64, 0, c.stream>>>(P, n, (uint32_t)n_rec, geo.k, skeys, vbits,
+                                                   d_ip, d_key);
+        CAPSSA_LAUNCHED(c);
+        uint32_t *h_ip = (uint32_t *)c.h_scratch;
+        uint64_t *h_key = (uint64_t *)(h_ip + 64);
+        CAPSSA_CUDA(c, cudaMemcpyAsync(h_ip, d_ip, 64 * 12, cudaMemcpyDeviceToHost, c.stream));
+        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+        // order of the short suffixes: by key, equal keys shorter first (the
+        // later position); each takes the SA slot after its insertion point
+        // and the short suffixes ordered before it
+        std::vector<uint32_t> ord(n_short);
+        for (uint32_t j = 0; j < n_short; j++) ord[j] = j;
+        std::sort(ord.begin(), ord.end(), [&](uint32_t x, uint32_t y) {
+            if (h_key[x] != h_key[y]) return h_key[x] < h_key[y];
+            return x > y;
+        });
+        SL.n = SW.n = (uint32_t)n_short;
+        for (uint32_t q = 0; q < n_short; q++) {
+            const uint32_t j = ord[q];
+            SL.ip[q] = h_ip[j];
+            SW.slot[q] = h_ip[j] + q;
+            SW.pos[q] = (uint32_t)(n_rec + j);
+        }
+    }
     CAPSSA_CUDA(c, cudaMemsetAsync(G.ctr, 0, sizeof(Counters), c.stream));
-    init_groups_kernel<<<grid_for(n, kInitTile), 256, 0, c.stream>>>(
-        skeys, nn, geo.k, (1ull << geo.lbits) - 1, lf, geo.flag_len, vbits, hd,
-        vbits ? sa : nullptr, G);
+    init_groups_kernel<<<grid_for(n_rec, kInitTile), 256, 0, c.stream>>>(
+        skeys, (uint32_t)n_rec, geo.k, (1ull << geo.lbits) - 1, lf, geo.flag_len, vbits, hd,
+        vbits ? sa : nullptr, G, SL);
     CAPSSA_LAUNCHED(c);
+    if (n_short) {
+        short_write_kernel<<<1, 64, 0, c.stream>>>(SW, sa, hd);
+        CAPSSA_LAUNCHED(c);
+    }
 
     const int k2bits = bits_for(n + 1);
     const uint64_t empty_lf = (1ull << k2bits) - 1;  // above every rank

@@ -518,3 +518,32 @@ def test_radix_autotuner_picks_a_shape_and_keeps_it():
         assert s1 in (16, 20, 24) and s1 == s2
     finally:
         c.close()
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.uint16])
+def test_flagless_short_suffix_placement(ctx, dtype):
+    """n = 150,000 over 4 symbols: dropping the early-end flag saves a radix
+    pass (12-symbol keys, 3 passes), so the 11 suffixes that end inside the
+    key are placed after the sort.  Endings that tie them with many full
+    suffixes (long runs of the smallest and largest code, a period-2 tail,
+    an all-equal text) must still give the oracle's order."""
+    rng = np.random.default_rng(150)
+    n = 150000
+    base = rng.integers(0, 4, n)
+    endings = {
+        "random": base,
+        "zeros": np.concatenate([base[:n - 5000], np.zeros(5000, np.int64)]),
+        "threes": np.concatenate([base[:n - 3000], np.full(3000, 3)]),
+        "period2": np.concatenate([base[:n - 4000], np.tile([0, 1], 2000)]),
+        "zero_then_one": np.concatenate([base[:n - 41], np.zeros(40, np.int64), [1]]),
+        "all_equal": np.concatenate([np.zeros(n - 3, np.int64), [1, 2, 3]]),
+    }
+    for name, t in endings.items():
+        t = t.astype(dtype)
+        got = ctx.build_in_memory(t)
+        st = ctx.stats()
+        assert st["key_symbols"] == 12 and st["sort_passes"] <= 3, name
+        assert np.array_equal(got, orc.build_in_memory(t)), name
+    # LongerFirst keeps the flag (and its own order)
+    t = endings["zeros"].astype(dtype)
+    check_against_oracle(ctx, t, longer_first=True)
