@@ -392,59 +392,71 @@ __device__ __forceinline__ uint64_t block_excl_scan64(uint64_t v, uint64_t *excl
     return total;
 }
 
-// The short suffixes of a flagless sort (KeyGeom::flagless), by value: the
-// SA index each sorted record moves up by is the number of short suffixes
-// inserted at or before it (ip[] ascending, one entry per short suffix).
+// The short suffixes of a flagless sort (KeyGeom::flagless), in device
+// memory: ip[] ascending, one insertion point per short suffix (sorted record
+// i moves up to SA index i + #{ip <= i}), and each short suffix's own SA
+// slot and position.
 struct ShortList {
     uint32_t n;
     uint32_t ip[63];
-};
-
-__device__ __forceinline__ uint32_t short_shift(const ShortList &S, uint32_t i) {
-    uint32_t c = 0;
-    for (uint32_t j = 0; j < S.n; j++) c += S.ip[j] <= i ? 1u : 0u;
-    return c;
-}
-
-// Key (first lim symbols, zero padded) and insertion point of each short
-// suffix n_rec + j of a flagless sort: the number of sorted records whose
-// key is smaller (a short suffix precedes every full suffix whose key is at
-// least its padded key, ShorterFirst).
-__global__ void short_place_kernel(Packed P, uint64_t n, uint32_t n_rec, int k,
-                                   const uint64_t *__restrict__ recs, int vbits,
-                                   uint32_t *__restrict__ ip_out, uint64_t *__restrict__ key_out) {
-    const uint32_t j = threadIdx.x;
-    if (n_rec + (uint64_t)j >= n) return;
-    const uint64_t sp = n_rec + (uint64_t)j;
-    const int take = (int)(n - sp);  // < k
-    const int kbits = k * P.b;
-    uint64_t key = window_at(P, sp) >> (64 - kbits);
-    key &= ~((1ull << ((k - take) * P.b)) - 1);
-    uint32_t lo = 0, hi = n_rec;
-    while (lo < hi) {
-        const uint32_t mid = lo + ((hi - lo) >> 1);
-        if ((recs[mid] >> vbits) < key)
-            lo = mid + 1;
-        else
-            hi = mid;
-    }
-    ip_out[j] = lo;
-    key_out[j] = key;
-}
-
-// The short suffixes' own SA slots (singleton groups).
-struct ShortSlots {
-    uint32_t n;
     uint32_t slot[63];
     uint32_t pos[63];
 };
 
-__global__ void short_write_kernel(ShortSlots W, uint32_t *__restrict__ sa,
+__device__ __forceinline__ uint32_t short_shift(const ShortList *S, uint32_t ns, uint32_t i) {
+    uint32_t c = 0;
+    for (uint32_t j = 0; j < ns; j++) c += __ldg(&S->ip[j]) <= i ? 1u : 0u;
+    return c;
+}
+
+// Places the short suffixes n_rec + j of a flagless sort (one block): each
+// one's key (first lim symbols, zero padded) and insertion point, the number
+// of sorted records with a smaller key (a short suffix precedes every full
+// suffix whose key is at least its padded key, ShorterFirst); ordered among
+// themselves by key, equal keys shorter first.
+__global__ void short_place_kernel(Packed P, uint64_t n, uint32_t n_rec, int k,
+                                   const uint64_t *__restrict__ recs, int vbits,
+                                   ShortList *__restrict__ S) {
+    __shared__ uint64_t s_key[64];
+    const uint32_t j = threadIdx.x;
+    const uint32_t ns = (uint32_t)(n - n_rec);
+    uint64_t key = 0;
+    uint32_t ip = 0;
+    if (j < ns) {
+        const uint64_t sp = n_rec + (uint64_t)j;
+        const int take = (int)(n - sp);  // < k
+        key = window_at(P, sp) >> (64 - k * P.b);
+        key &= ~((1ull << ((k - take) * P.b)) - 1);
+        uint32_t lo = 0, hi = n_rec;
+        while (lo < hi) {
+            const uint32_t mid = lo + ((hi - lo) >> 1);
+            if ((recs[mid] >> vbits) < key)
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        ip = lo;
+        s_key[j] = key;
+    }
+    __syncthreads();
+    if (j < ns) {
+        uint32_t r = 0;  // short suffixes ordered before this one
+        for (uint32_t q = 0; q < ns; q++)
+            if (s_key[q] < key || (s_key[q] == key && q > j)) r++;
+        S->ip[r] = ip;
+        S->slot[r] = ip + r;
+        S->pos[r] = n_rec + j;
+    }
+    if (j == 0) S->n = ns;
+}
+
+// The short suffixes' own SA slots (singleton groups).
+__global__ void short_write_kernel(const ShortList *__restrict__ S, uint32_t *__restrict__ sa,
                                    uint32_t *__restrict__ hd) {
     const uint32_t j = threadIdx.x;
-    if (j >= W.n) return;
-    sa[W.slot[j]] = W.pos[j];
-    hd[W.slot[j]] = W.slot[j];
+    if (j >= S->n) return;
+    sa[S->slot[j]] = S->pos[j];
+    hd[S->slot[j]] = S->slot[j];
 }
 
 constexpr int kInitPer = 16;  // sorted keys per thread in init_groups_kernel
@@ -460,7 +472,8 @@ constexpr int kInitTile = 256 * kInitPer;
 __global__ void __launch_bounds__(256)
     init_groups_kernel(const uint64_t *__restrict__ keys, uint32_t n, int k, uint64_t lmask,
                        int lf, int flag_len, int vshift, uint32_t *__restrict__ hd,
-                       uint32_t *__restrict__ sa_out, GroupLists G, ShortList S) {
+                       uint32_t *__restrict__ sa_out, GroupLists G,
+                       const ShortList *__restrict__ S) {
     static_assert(kLists <= 8, "two packed words of four 16-bit counters");
     __shared__ uint64_t sk[kInitTile + 2];  // sk[l + 1] = key of sorted index base + l
     __shared__ uint32_t s_base[kLists];
@@ -469,9 +482,10 @@ __global__ void __launch_bounds__(256)
     const uint64_t vmask = (1ull << vshift) - 1;
     // SA index of sorted record i: i + (short suffixes inserted at or before
     // it), one shift for the whole block unless an insertion falls inside
-    const uint32_t sh_lo = S.n ? short_shift(S, base) : 0u;
-    const bool sh_flat = !S.n || short_shift(S, base + valid - 1) == sh_lo;
-    auto shift_of = [&](uint32_t i) { return sh_flat ? sh_lo : short_shift(S, i); };
+    const uint32_t ns = S ? __ldg(&S->n) : 0u;
+    const uint32_t sh_lo = ns ? short_shift(S, ns, base) : 0u;
+    const bool sh_flat = !ns || short_shift(S, ns, base + valid - 1) == sh_lo;
+    auto shift_of = [&](uint32_t i) { return sh_flat ? sh_lo : short_shift(S, ns, i); };
     for (uint32_t l = threadIdx.x; l < valid; l += 256) {
         const uint64_t item = keys[base + l];
         sk[l + 1] = item >> vshift;
@@ -1949,53 +1963,34 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     G.big[0] = (BigGroup *)cursor;
     G.big[1] = G.big[0] + big_cap;
     uint64_t h = (uint64_t)geo.k;
+    KernelTimes kt(profile_on());
+    kt.start(c.stream);
     // flagless: where the short suffixes go among the sorted full ones
-    ShortList SL{};
-    ShortSlots SW{};
+    ShortList *d_short = nullptr;
     if (n_short) {
-        uint32_t *d_ip = (uint32_t *)ws_get(c, WS_SAMPLE, 64 * 12 + 64);
-        if (!d_ip) return set_err(c, CAPSSA_ENOMEM, "short suffixes");
-        uint64_t *d_key = (uint64_t *)(d_ip + 64);
+        d_short = (ShortList *)ws_get(c, WS_SAMPLE, sizeof(ShortList) + 64);
+        if (!d_short) return set_err(c, CAPSSA_ENOMEM, "short suffixes");
         short_place_kernel<<<1, 64, 0, c.stream>>>(P, n, (uint32_t)n_rec, geo.k, skeys, vbits,
-                                                   d_ip, d_key);
+                                                   d_short);
         CAPSSA_LAUNCHED(c);
-        uint32_t *h_ip = (uint32_t *)c.h_scratch;
-        uint64_t *h_key = (uint64_t *)(h_ip + 64);
-        CAPSSA_CUDA(c, cudaMemcpyAsync(h_ip, d_ip, 64 * 12, cudaMemcpyDeviceToHost, c.stream));
-        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
-        // order of the short suffixes: by key, equal keys shorter first (the
-        // later position); each takes the SA slot after its insertion point
-        // and the short suffixes ordered before it
-        std::vector<uint32_t> ord(n_short);
-        for (uint32_t j = 0; j < n_short; j++) ord[j] = j;
-        std::sort(ord.begin(), ord.end(), [&](uint32_t x, uint32_t y) {
-            if (h_key[x] != h_key[y]) return h_key[x] < h_key[y];
-            return x > y;
-        });
-        SL.n = SW.n = (uint32_t)n_short;
-        for (uint32_t q = 0; q < n_short; q++) {
-            const uint32_t j = ord[q];
-            SL.ip[q] = h_ip[j];
-            SW.slot[q] = h_ip[j] + q;
-            SW.pos[q] = (uint32_t)(n_rec + j);
-        }
     }
     CAPSSA_CUDA(c, cudaMemsetAsync(G.ctr, 0, sizeof(Counters), c.stream));
     init_groups_kernel<<<grid_for(n_rec, kInitTile), 256, 0, c.stream>>>(
         skeys, (uint32_t)n_rec, geo.k, (1ull << geo.lbits) - 1, lf, geo.flag_len, vbits, hd,
-        vbits ? sa : nullptr, G, SL);
+        vbits ? sa : nullptr, G, d_short);
     CAPSSA_LAUNCHED(c);
     if (n_short) {
-        short_write_kernel<<<1, 64, 0, c.stream>>>(SW, sa, hd);
+        short_write_kernel<<<1, 64, 0, c.stream>>>(d_short, sa, hd);
         CAPSSA_LAUNCHED(c);
     }
+    kt.mark(c.stream, "groups");
+    kt.print();
 
     const int k2bits = bits_for(n + 1);
     const uint64_t empty_lf = (1ull << k2bits) - 1;  // above every rank
     const uint64_t empty = lf ? empty_lf : 0ull;
     bool ranks_ready = false;
     int cur = 0;
-    KernelTimes kt(profile_on());
     Counters *hc = (Counters *)c.h_scratch;
     for (;;) {
         CAPSSA_CUDA(c, cudaMemcpyAsync(hc, G.ctr, sizeof(Counters), cudaMemcpyDeviceToHost,
