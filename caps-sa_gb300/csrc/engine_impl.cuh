@@ -482,9 +482,16 @@ __global__ void __launch_bounds__(256)
     const uint64_t vmask = (1ull << vshift) - 1;
     // SA index of sorted record i: i + (short suffixes inserted at or before
     // it), one shift for the whole block unless an insertion falls inside
+    __shared__ uint32_t s_shift[2];
     const uint32_t ns = S ? __ldg(&S->n) : 0u;
-    const uint32_t sh_lo = ns ? short_shift(S, ns, base) : 0u;
-    const bool sh_flat = !ns || short_shift(S, ns, base + valid - 1) == sh_lo;
+    if (threadIdx.x == 0) {
+        const uint32_t lo = ns ? short_shift(S, ns, base) : 0u;
+        s_shift[0] = lo;
+        s_shift[1] = !ns || short_shift(S, ns, base + valid - 1) == lo;
+    }
+    __syncthreads();
+    const uint32_t sh_lo = s_shift[0];
+    const bool sh_flat = s_shift[1] != 0;
     auto shift_of = [&](uint32_t i) { return sh_flat ? sh_lo : short_shift(S, ns, i); };
     for (uint32_t l = threadIdx.x; l < valid; l += 256) {
         const uint64_t item = keys[base + l];
