@@ -1947,6 +1947,9 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     const uint64_t *skeys = in_b ? keys_b : keys_a;
     // packed positions are unpacked into vals_a by init_groups
     uint32_t *sa = (in_b && !vbits) ? vals_b : vals_a;
+    // packed records are unpacked straight into a u32 output of a full build,
+    // which then needs no final copy
+    if (vbits && !a.positions && a.out_bytes == 4 && a.out_sa) sa = (uint32_t *)a.out_sa;
     uint32_t *spare_vals = sa == vals_a ? vals_b : vals_a;
 
     // ---- 4. tied groups: direct comparison while shallow, rank doubling when deep
@@ -2422,7 +2425,9 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
     FinishTimer ft(c);
     if (!subset) {
         if (a.out_bytes == 4) {
-            CAPSSA_CUDA(c, cudaMemcpyAsync(a.out_sa, sa, n * 4, cudaMemcpyDeviceToDevice, c.stream));
+            if (sa != a.out_sa)
+                CAPSSA_CUDA(c, cudaMemcpyAsync(a.out_sa, sa, n * 4, cudaMemcpyDeviceToDevice,
+                                               c.stream));
         } else {
             widen_kernel<uint64_t><<<grid_for(n, 256), 256, 0,
                                      c.stream>>>(sa, (uint64_t *)a.out_sa, n);
