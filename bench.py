@@ -435,9 +435,11 @@ def run_ours(args):
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
         el = max_over_ranks(el, dist, "cuda")
+        st = ctx.stats()  # the last step's host-side copy times
         e2e = {"value": job_throughput(n, ws, args.steps, el), "unit": "Msuffixes/s",
                "h2d_bytes_per_step": int(n), "d2h_bytes_per_step": int(4 * n),
-               "ms_per_step": el / args.steps * 1e3}
+               "ms_per_step": el / args.steps * 1e3,
+               "h2d_ms": round(st["h2d_ms"], 3), "d2h_ms": round(st["d2h_ms"], 3)}
         if not np.array_equal(h_out.numpy().view(np.uint32), sa_dev.cpu().numpy().view(np.uint32)):
             raise SystemExit("host-path suffix array differs from the device-path one")
 
