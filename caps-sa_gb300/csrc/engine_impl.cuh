@@ -1547,15 +1547,13 @@ __global__ void head_key_kernel(const uint32_t *__restrict__ sa, uint32_t n,
 }
 
 // Chunk-major order of the sorted suffixes (full text): key = chunk of the
-// position, value = the position, in SA order (a stable sort by the key then
-// lists every chunk's positions in sorted order).
+// position, in SA order; a stable sort by the key with the SA indices as
+// generated values then lists every chunk's suffixes in sorted order, each
+// by its rank.
 __global__ void chunk_key_kernel(const uint32_t *__restrict__ sa, uint32_t n, uint32_t chunk,
-                                 uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint32_t p = sa[j];
-        keys[j] = p / chunk;
-        vals[j] = p;
-    }
+                                 uint64_t *__restrict__ keys) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        keys[j] = sa[j] / chunk;
 }
 
 // Subsets: key = (chunk of the input index, rank of the suffix), value =
@@ -1575,7 +1573,8 @@ __global__ void chunk_key_subset_kernel(const PT *__restrict__ pos, uint64_t m, 
 }
 
 // Evenly spaced midpoints of every sorted chunk (evenly_spaced,
-// src/ext_mem.rs:1291-1305), with each sample's rank key.
+// src/ext_mem.rs:1291-1305), with each sample's rank key.  `isa` null: the
+// chunks hold SA indices (full text), which are the ranks.
 __global__ void sample_kernel(const uint32_t *__restrict__ chunked, uint64_t m, uint32_t chunk,
                               uint32_t p, uint32_t per, const uint32_t *__restrict__ soff,
                               uint64_t n, const uint32_t *__restrict__ isa, int lf,
@@ -1593,20 +1592,23 @@ __global__ void sample_kernel(const uint32_t *__restrict__ chunked, uint64_t m, 
         const uint32_t q = chunked[start + at];
         const uint32_t o = soff[i] + sidx;
         spos[o] = q;
-        skey[o] = q >= n ? (lf ? n + 1 : 0ull) : (uint64_t)__ldg(isa + q) + 1;
+        skey[o] = !isa ? (uint64_t)q + 1
+                       : (q >= n ? (lf ? n + 1 : 0ull) : (uint64_t)__ldg(isa + q) + 1);
     }
 }
 
 // Pivots samples[j * ns / p] (phase 2, src/ext_mem.rs:1309-1342) with their
-// comparison keys.
+// comparison keys.  `sa` non-null: the samples are SA indices (full text),
+// keyed by their tie-run head (or themselves), and the pivot is sa[q].
 __global__ void pivot_kernel(const uint32_t *__restrict__ sorted_samples, uint32_t ns, uint32_t p,
-                             const uint32_t *__restrict__ hkey, uint32_t *__restrict__ piv_pos,
+                             const uint32_t *__restrict__ hkey, const uint32_t *__restrict__ sa,
+                             const uint32_t *__restrict__ head, uint32_t *__restrict__ piv_pos,
                              uint32_t *__restrict__ piv_key) {
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j + 1 < p;
          j += gridDim.x * blockDim.x) {
         const uint32_t q = sorted_samples[(uint64_t)(j + 1) * ns / p];
-        piv_pos[j] = q;
-        piv_key[j] = hkey[q];
+        piv_pos[j] = sa ? sa[q] : q;
+        piv_key[j] = sa ? (head ? head[q] : q) + 1 : hkey[q];
     }
 }
 
@@ -1614,10 +1616,12 @@ __global__ void pivot_kernel(const uint32_t *__restrict__ sorted_samples, uint32
 // its packed prefix and its rank fraction among all ns samples.
 __global__ void train_set_kernel(const uint32_t *__restrict__ sorted_samples, uint32_t ns,
                                  uint32_t stride, uint32_t tn, Packed P,
-                                 uint64_t *__restrict__ x, float *__restrict__ t) {
+                                 const uint32_t *__restrict__ sa, uint64_t *__restrict__ x,
+                                 float *__restrict__ t) {
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < tn; j += gridDim.x * blockDim.x) {
         const uint32_t q = j * stride;
-        x[j] = window_at(P, sorted_samples[q]);
+        const uint32_t s = sorted_samples[q];
+        x[j] = window_at(P, sa ? sa[s] : s);
         t[j] = ((float)q + 0.5f) / (float)ns;
     }
 }
@@ -1628,14 +1632,16 @@ __global__ void train_set_kernel(const uint32_t *__restrict__ sorted_samples, ui
 // the comparison keys.  SPLITTERS: binary search over the pivots.  LEARNED:
 // the CDF model predicts b from the suffix's packed prefix; the prediction
 // is checked against its two neighbouring pivots and moved until both hold.
-// `items` lists the suffixes (nullptr: every position 0..m-1, read in text
-// order so that keys and prefixes stream); b must never decrease along the
-// sorted order (checked by the caller).  Pivot keys and the bucket histogram
-// live in shared memory.
+// `sa` non-null (full text): the suffixes are visited in SA order, item j
+// keyed by its tie-run head (or j) and its prefix read at sa[j]; otherwise
+// `items` lists the subset's positions in sorted order, keyed by hkey.
+// b must never decrease along the sorted order (checked by the caller).
+// Pivot keys and the bucket histogram live in shared memory.
 template <bool LEARNED>
 __global__ void __launch_bounds__(256)
     partition_kernel(const uint32_t *__restrict__ items, uint32_t m, Packed P,
-                     const uint32_t *__restrict__ hkey, const uint32_t *__restrict__ piv_key,
+                     const uint32_t *__restrict__ hkey, const uint32_t *__restrict__ sa,
+                     const uint32_t *__restrict__ head, const uint32_t *__restrict__ piv_key,
                      uint32_t n_piv, uint32_t p, const __nv_bfloat16 *__restrict__ w,
                      uint32_t *__restrict__ bucket_of, unsigned long long *__restrict__ sizes,
                      unsigned long long *__restrict__ stats) {
@@ -1651,10 +1657,10 @@ __global__ void __launch_bounds__(256)
     unsigned long long probes = 0, mis = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
         const uint32_t s = items ? items[i] : i;
-        const uint32_t ks = hkey[s];
+        const uint32_t ks = sa ? (head ? head[i] : i) + 1 : hkey[s];
         uint32_t b;
         if (LEARNED) {
-            const float y = cdf::infer_bf16(sw, window_at(P, s));
+            const float y = cdf::infer_bf16(sw, window_at(P, sa ? sa[i] : s));
             float g = floorf(y * (float)p);
             g = g < 0.0f ? 0.0f : (g > (float)n_piv ? (float)n_piv : g);
             b = (uint32_t)g;
@@ -2230,10 +2236,10 @@ capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
     uint32_t *head = (uint32_t *)(w + 2 * m8 + 3 * m4);
     uint32_t *hkey = (uint32_t *)(w + 2 * m8 + 3 * m4 + n4);
     const bool subset = a.positions != nullptr;
-    if (!subset) {
-        isa_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa_full, (uint32_t)n, isa);
-        CAPSSA_LAUNCHED(c);
-    }  // (subsets: the caller's isa is already in place)
+    KernelTimes kt(profile_on());
+    kt.start(c.stream);
+    // full text: every key below is an SA index or its tie-run head, so no
+    // position-indexed array is built; subsets: the caller's isa is in place
     // 0. comparison keys (run heads of the comparator's ties)
     const bool ties = a.lim.segmented && !lf;
     if (ties) {
@@ -2243,18 +2249,22 @@ capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
         capssa_status s0 = scan_u32(c, head, head, n, /*max_op=*/true, /*inclusive=*/true);
         if (s0 != CAPSSA_OK) return s0;
     }
-    head_key_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa_full, (uint32_t)n,
-                                                            ties ? head : nullptr, lf, hkey);
-    CAPSSA_LAUNCHED(c);
+    if (subset) {
+        head_key_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa_full, (uint32_t)n,
+                                                                ties ? head : nullptr, lf, hkey);
+        CAPSSA_LAUNCHED(c);
+    }
+    kt.mark(c.stream, "isa+heads");
     // 1. every chunk's positions in sorted order
     const int cbits = bits_for(p > 1 ? p - 1 : 1);
     bool in_b = false;
     capssa_status s;
     if (!subset) {
-        chunk_key_kernel<<<grid_for(m, 256), 256, 0, c.stream>>>(sa_full, (uint32_t)m, chunk, ka,
-                                                                 va);
+        chunk_key_kernel<<<grid_for(m, 256), 256, 0, c.stream>>>(sa_full, (uint32_t)m, chunk,
+                                                                 ka);
         CAPSSA_LAUNCHED(c);
-        s = radix::sort_pairs(c, ka, va, kb, vb, (uint32_t)m, 0, cbits, false, 0, &in_b);
+        s = radix::sort_pairs(c, ka, va, kb, vb, (uint32_t)m, 0, cbits, /*gen_vals=*/true, 0,
+                              &in_b);
     } else {
         const int rbits = bits_for(n + 1);
         if (a.pos_bytes == 4)
@@ -2267,6 +2277,7 @@ capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
         s = radix::sort_pairs(c, ka, va, kb, vb, (uint32_t)m, 0, rbits + cbits, false, 0, &in_b);
     }
     if (s != CAPSSA_OK) return s;
+    kt.mark(c.stream, "chunks");
     const uint32_t *chunked = in_b ? vb : va;
     // 2. samples and their rank keys, sorted; pivots
     std::vector<uint32_t> soff(p + 1, 0);
@@ -2298,15 +2309,16 @@ capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
     CAPSSA_CUDA(c, cudaMemcpyAsync(d_soff, soff.data(), (p + 1) * 4, cudaMemcpyHostToDevice,
                                    c.stream));
     sample_kernel<<<grid_for((uint64_t)p * per, 256), 256, 0, c.stream>>>(
-        chunked, m, chunk, p, per, d_soff, n, isa, lf, sk_a, sp_a);
+        chunked, m, chunk, p, per, d_soff, n, subset ? isa : nullptr, lf, sk_a, sp_a);
     CAPSSA_LAUNCHED(c);
     bool s_in_b = false;
     s = radix::sort_pairs(c, sk_a, sp_a, sk_b, sp_b, ns, 0, bits_for(n + 1), false, 0, &s_in_b);
     if (s != CAPSSA_OK) return s;
     const uint32_t *sorted_samples = s_in_b ? sp_b : sp_a;
     if (n_piv) {
-        pivot_kernel<<<grid_for(n_piv, 256), 256, 0, c.stream>>>(sorted_samples, ns, p, hkey,
-                                                                piv_pos, piv_key);
+        pivot_kernel<<<grid_for(n_piv, 256), 256, 0, c.stream>>>(
+            sorted_samples, ns, p, hkey, subset ? nullptr : sa_full,
+            !subset && ties ? head : nullptr, piv_pos, piv_key);
         CAPSSA_LAUNCHED(c);
     }
     // 3. learned CDF model on the sample (learned mode)
@@ -2315,8 +2327,8 @@ capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
         const uint32_t tn = std::min<uint32_t>(ns, 65536);
         const uint32_t stride = (ns + tn - 1) / tn;
         const uint32_t tn_eff = (ns + stride - 1) / stride;
-        train_set_kernel<<<grid_for(tn_eff, 256), 256, 0, c.stream>>>(sorted_samples, ns, stride,
-                                                                     tn_eff, P, tx, tt);
+        train_set_kernel<<<grid_for(tn_eff, 256), 256, 0, c.stream>>>(
+            sorted_samples, ns, stride, tn_eff, P, subset ? nullptr : sa_full, tx, tt);
         CAPSSA_LAUNCHED(c);
         cudaEvent_t t0, t1;
         cudaEventCreate(&t0);
@@ -2345,26 +2357,29 @@ capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
     else
         cudaFuncSetAttribute(partition_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
+    kt.mark(c.stream, "samples+pivots+model");
     cudaEvent_t q0, q1;
     cudaEventCreate(&q0);
     cudaEventCreate(&q1);
     cudaEventRecord(q0, c.stream);
-    // every position in text order (full text) or the sorted subset
+    // the full text in SA order, or the sorted subset
     const uint32_t *items = subset ? sorted : nullptr;
+    const uint32_t *psa = subset ? nullptr : sa_full;
+    const uint32_t *phead = !subset && ties ? head : nullptr;
     if (learned)
-        partition_kernel<true><<<grid, 256, smem, c.stream>>>(items, (uint32_t)m, P, hkey,
-                                                              piv_key, n_piv, p, wbf, bucket_of,
-                                                              sizes, pstats);
+        partition_kernel<true><<<grid, 256, smem, c.stream>>>(items, (uint32_t)m, P, hkey, psa,
+                                                              phead, piv_key, n_piv, p, wbf,
+                                                              bucket_of, sizes, pstats);
     else
-        partition_kernel<false><<<grid, 256, smem, c.stream>>>(items, (uint32_t)m, P, hkey,
-                                                               piv_key, n_piv, p, wbf, bucket_of,
-                                                               sizes, pstats);
+        partition_kernel<false><<<grid, 256, smem, c.stream>>>(items, (uint32_t)m, P, hkey, psa,
+                                                               phead, piv_key, n_piv, p, wbf,
+                                                               bucket_of, sizes, pstats);
     CAPSSA_LAUNCHED(c);
     cudaEventRecord(q1, c.stream);
     int *bad = c.d_flags + 1;
     CAPSSA_CUDA(c, cudaMemsetAsync(bad, 0, 4, c.stream));
-    partition_check_kernel<<<grid_for(m, 256), 256, 0, c.stream>>>(
-        bucket_of, subset ? nullptr : sa_full, (uint32_t)m, bad);
+    partition_check_kernel<<<grid_for(m, 256), 256, 0, c.stream>>>(bucket_of, nullptr,
+                                                                   (uint32_t)m, bad);
     CAPSSA_LAUNCHED(c);
     std::vector<unsigned long long> h_sizes((size_t)p + 4);
     std::vector<uint32_t> h_piv(n_piv + 1);
@@ -2375,6 +2390,8 @@ capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
                                        cudaMemcpyDeviceToHost, c.stream));
     int h_bad = 0;
     CAPSSA_CUDA(c, cudaMemcpyAsync(&h_bad, bad, 4, cudaMemcpyDeviceToHost, c.stream));
+    kt.mark(c.stream, "partition+check");
+    kt.print();
     CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
     float pms = 0.0f;
     cudaEventElapsedTime(&pms, q0, q1);
