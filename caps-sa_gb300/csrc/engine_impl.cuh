@@ -1510,6 +1510,58 @@ __global__ void subset_isa_key_kernel(const PT *__restrict__ pos, uint64_t m, ui
     }
 }
 
+// Subsets of distinct positions: one bit per requested position (p < n),
+// set by warp-combined atomics. flags[0]: a position beyond n; flags[1]: a
+// position requested twice; count[0]: requests of the empty suffix n.  Every
+// lane of a warp takes the same number of steps (the match and reduction
+// below need them together).
+template <typename PT>
+__global__ void subset_bits_kernel(const PT *__restrict__ pos, uint64_t m, uint64_t n,
+                                   uint32_t *__restrict__ bits, int *__restrict__ flags,
+                                   unsigned long long *__restrict__ count) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t base = warp * 32; base < m; base += nwarps * 32) {
+        const uint64_t i = base + lane;
+        const bool valid = i < m;
+        const uint64_t p = valid ? (uint64_t)pos[i] : 0ull;
+        if (valid && p > n) atomicExch(&flags[0], 1);
+        if (valid && p == n) atomicAdd(count, 1ull);
+        const bool set = valid && p < n;
+        const unsigned active = __ballot_sync(0xffffffffu, set);
+        if (set) {
+            const uint32_t w = (uint32_t)(p >> 5);
+            const unsigned peers = __match_any_sync(active, w);
+            const uint32_t mask = __reduce_or_sync(peers, 1u << (uint32_t)(p & 31));
+            if ((int)lane == __ffs((int)peers) - 1) {
+                const uint32_t old = atomicOr(&bits[w], mask);
+                if ((old & mask) != 0u || __popc(mask) != __popc(peers)) atomicExch(&flags[1], 1);
+            }
+        }
+    }
+}
+
+// flag[j] = 1 when the suffix at SA index j was requested.
+__global__ void subset_flag_kernel(const uint32_t *__restrict__ sa, uint32_t n,
+                                   const uint32_t *__restrict__ bits, uint32_t *__restrict__ flag) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t p = sa[j];
+        flag[j] = (__ldg(bits + (p >> 5)) >> (p & 31)) & 1u;
+    }
+}
+
+// The requested suffixes in SA order: slot incl[j] - 1 (+ off) for each
+// flagged j (incl = inclusive scan of the flags).
+__global__ void subset_compact_kernel(const uint32_t *__restrict__ sa, uint32_t n,
+                                      const uint32_t *__restrict__ incl, uint32_t off,
+                                      uint32_t *__restrict__ out) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t c = incl[j], before = j ? incl[j - 1] : 0u;
+        if (c != before) out[c - 1 + off] = sa[j];
+    }
+}
+
 // ---------------------------------------------------------------- sample-sort partition
 
 // Comparison keys of the sorted text for the partition: suffixes that
@@ -2458,36 +2510,86 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
         return CAPSSA_OK;
     }
     // subset: order the requested positions by their index in the full SA
-    uint32_t *isa = (uint32_t *)ws_get(c, WS_RANK, (size_t)n * 4 + 64);
-    uint64_t *sk_a = (uint64_t *)ws_get(c, WS_MISC, (size_t)m * 8 + 64);
-    uint64_t *sk_b = (uint64_t *)ws_get(c, WS_MISC2, (size_t)m * 8 + 64);
     uint32_t *sv = (uint32_t *)ws_get(c, WS_MISC3, (size_t)m * 8 + 64);
-    if (!isa || !sk_a || !sk_b || !sv) return set_err(c, CAPSSA_ENOMEM, "subset workspace");
+    if (!sv) return set_err(c, CAPSSA_ENOMEM, "subset workspace");
     uint32_t *sv_b = sv + m;
-    if (n > 0) {
-        isa_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(
-            sa, (uint32_t)n, isa);
+    const unsigned gm = grid_for(m, 256);
+    const uint32_t *res = nullptr;
+    if (!a.part_p && n > 0) {
+        // distinct positions: mark them in a bitmap (L2-sized: n / 8 bytes)
+        // and compact the full order, instead of sorting them by rank
+        uint32_t *bits = (uint32_t *)ws_get(c, WS_KEYS_A, (size_t)n * 8);
+        uint32_t *flag = (uint32_t *)ws_get(c, WS_KEYS_B, (size_t)n * 8);
+        if (!bits || !flag) return set_err(c, CAPSSA_ENOMEM, "subset workspace");
+        int *fl = c.d_flags + 1;  // [0] beyond the end, [1] repeated
+        unsigned long long *cnt = (unsigned long long *)(c.d_flags + 4);
+        CAPSSA_CUDA(c, cudaMemsetAsync(fl, 0, 12 + 8, c.stream));
+        CAPSSA_CUDA(c, cudaMemsetAsync(bits, 0, ((size_t)n / 32 + 1) * 4, c.stream));
+        const unsigned gb = std::min<unsigned>(grid_for(m, 256), (unsigned)c.sm_count * 8);
+        if (a.pos_bytes == 4)
+            subset_bits_kernel<uint32_t><<<gb, 256, 0, c.stream>>>(
+                (const uint32_t *)a.positions, m, n, bits, fl, cnt);
+        else
+            subset_bits_kernel<uint64_t><<<gb, 256, 0, c.stream>>>(
+                (const uint64_t *)a.positions, m, n, bits, fl, cnt);
         CAPSSA_LAUNCHED(c);
+        int *h = (int *)c.h_scratch;
+        unsigned long long *h_cnt = (unsigned long long *)c.h_scratch + 2;
+        CAPSSA_CUDA(c, cudaMemcpyAsync(h, fl, 8, cudaMemcpyDeviceToHost, c.stream));
+        CAPSSA_CUDA(c, cudaMemcpyAsync(h_cnt, cnt, 8, cudaMemcpyDeviceToHost, c.stream));
+        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+        if (h[0]) return set_err(c, CAPSSA_EINVAL, "a position lies beyond the end of the text");
+        const unsigned long long n_empty = *h_cnt;
+        if (!h[1] && n_empty <= 1) {
+            subset_flag_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa, (uint32_t)n, bits,
+                                                                        flag);
+            CAPSSA_LAUNCHED(c);
+            capssa_status s0 = scan_u32(c, flag, flag, n, /*max_op=*/false, /*inclusive=*/true);
+            if (s0 != CAPSSA_OK) return s0;
+            // the empty suffix n sorts first (ShorterFirst) or last
+            const uint32_t off = (n_empty && !lf) ? 1u : 0u;
+            subset_compact_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa, (uint32_t)n, flag,
+                                                                           off, sv);
+            CAPSSA_LAUNCHED(c);
+            if (n_empty) {
+                const uint32_t nv = (uint32_t)n;
+                CAPSSA_CUDA(c, cudaMemcpyAsync(sv + (lf ? m - 1 : 0), &nv, 4,
+                                               cudaMemcpyHostToDevice, c.stream));
+                CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));  // nv is on this stack
+            }
+            res = sv;
+        }
     }
-    int *bad = c.d_flags + 1;
-    CAPSSA_CUDA(c, cudaMemsetAsync(bad, 0, 4, c.stream));
-    unsigned gm = grid_for(m, 256);
-    if (a.pos_bytes == 4)
-        subset_isa_key_kernel<uint32_t><<<gm, 256, 0, c.stream>>>(
-            (const uint32_t *)a.positions, m, n, isa, lf, sk_a, sv, bad);
-    else
-        subset_isa_key_kernel<uint64_t><<<gm, 256, 0, c.stream>>>(
-            (const uint64_t *)a.positions, m, n, isa, lf, sk_a, sv, bad);
-    CAPSSA_LAUNCHED(c);
-    int *h_bad = (int *)c.h_scratch;
-    CAPSSA_CUDA(c, cudaMemcpyAsync(h_bad, bad, 4, cudaMemcpyDeviceToHost, c.stream));
-    CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
-    if (*h_bad) return set_err(c, CAPSSA_EINVAL, "a position lies beyond the end of the text");
-    bool in_b = false;
-    capssa_status s = radix::sort_pairs(c, sk_a, sv, sk_b, sv_b, (uint32_t)m, 0, bits_for(n + 1),
-                                        false, 0, &in_b);
-    if (s != CAPSSA_OK) return s;
-    const uint32_t *res = in_b ? sv_b : sv;
+    if (!res) {
+        uint32_t *isa = (uint32_t *)ws_get(c, WS_RANK, (size_t)n * 4 + 64);
+        uint64_t *sk_a = (uint64_t *)ws_get(c, WS_MISC, (size_t)m * 8 + 64);
+        uint64_t *sk_b = (uint64_t *)ws_get(c, WS_MISC2, (size_t)m * 8 + 64);
+        if (!isa || !sk_a || !sk_b) return set_err(c, CAPSSA_ENOMEM, "subset workspace");
+        if (n > 0) {
+            isa_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(
+                sa, (uint32_t)n, isa);
+            CAPSSA_LAUNCHED(c);
+        }
+        int *bad = c.d_flags + 1;
+        CAPSSA_CUDA(c, cudaMemsetAsync(bad, 0, 4, c.stream));
+        if (a.pos_bytes == 4)
+            subset_isa_key_kernel<uint32_t><<<gm, 256, 0, c.stream>>>(
+                (const uint32_t *)a.positions, m, n, isa, lf, sk_a, sv, bad);
+        else
+            subset_isa_key_kernel<uint64_t><<<gm, 256, 0, c.stream>>>(
+                (const uint64_t *)a.positions, m, n, isa, lf, sk_a, sv, bad);
+        CAPSSA_LAUNCHED(c);
+        int *h_bad = (int *)c.h_scratch;
+        CAPSSA_CUDA(c, cudaMemcpyAsync(h_bad, bad, 4, cudaMemcpyDeviceToHost, c.stream));
+        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+        if (*h_bad) return set_err(c, CAPSSA_EINVAL, "a position lies beyond the end of the text");
+        bool in_b = false;
+        capssa_status s = radix::sort_pairs(c, sk_a, sv, sk_b, sv_b, (uint32_t)m, 0, bits_for(n + 1),
+                                            false, 0, &in_b);
+        if (s != CAPSSA_OK) return s;
+        res = in_b ? sv_b : sv;
+    }
+    capssa_status s = CAPSSA_OK;
     if (a.part_p) {
         s = partition_phase<S>(c, a, P, sa, res, m);
         if (s != CAPSSA_OK) return s;

@@ -206,8 +206,17 @@ def test_for_positions_subsets_duplicates_and_end(ctx):
         assert sorted(got.tolist()) == sorted(want.tolist())
         runs = tie_runs(t, want, orc.Limits(n))
         assert canon(got, runs) == canon(want, runs)
+        # distinct positions with the empty suffix once (bitmap path), both
+        # boundary orders, u32 and u64
+        pos1 = rng.permutation(np.concatenate([keep, [n]]))
+        for lf in (False, True):
+            for index in (np.uint32, np.uint64):
+                check_against_oracle(ctx, t, positions=pos1, longer_first=lf, index=index)
     with pytest.raises(ValueError):
         ctx.build_in_memory_for_positions(b"banana", np.array([0, 7], dtype=np.uint32))
+    with pytest.raises(ValueError):  # beyond the end, among distinct positions
+        ctx.build_in_memory_for_positions(np.zeros(5000, np.uint8) + 1,
+                                          np.arange(0, 5002, dtype=np.uint64))
 
 
 def test_invalid_segments_rejected(ctx):
