@@ -307,9 +307,11 @@ template <typename ST>
 capssa_status build_common(Ctx &c, const ST *text, uint64_t n, const void *positions,
                            int pos_bytes, uint64_t m, const capssa_limits *lp,
                            const capssa_opts *opts, void *out_sa, int out_bytes, void *out_lcp,
-                           const PartRequest *part = nullptr, uint64_t seg_major_len = 0) {
+                           const PartRequest *part = nullptr, uint64_t seg_major_len = 0,
+                           const uint32_t *keep_bits = nullptr) {
     if (!text && n) return set_err(c, CAPSSA_EINVAL, "null text");
-    if (!out_sa && (positions ? m : n)) return set_err(c, CAPSSA_EINVAL, "null output");
+    const bool chosen = positions || keep_bits;  // a subset, m suffixes
+    if (!out_sa && (chosen ? m : n)) return set_err(c, CAPSSA_EINVAL, "null output");
     if (out_bytes == 4 && n > 0xFFFFFFFFull)
         return set_err(c, CAPSSA_EINVAL, "u32 index cannot address this text");
     uint64_t max_ctx = opts ? opts->max_context : CAPSSA_UNBOUNDED;
@@ -319,7 +321,7 @@ capssa_status build_common(Ctx &c, const ST *text, uint64_t n, const void *posit
     void *d_text = nullptr;
     s = stage_text(c, text, n, &d_text);
     if (s != CAPSSA_OK) return s;
-    const uint64_t count = positions ? m : n;
+    const uint64_t count = chosen ? m : n;
     void *d_pos = nullptr;
     if (positions && m) {
         s = stage_in(c, WS_POS_IN, positions, m * (size_t)pos_bytes, 64, &d_pos);
@@ -345,6 +347,7 @@ capssa_status build_common(Ctx &c, const ST *text, uint64_t n, const void *posit
     a.max_ctx = max_ctx;
     a.positions = positions ? d_pos : nullptr;
     a.pos_bytes = pos_bytes;
+    a.keep_bits = keep_bits;
     a.m = m;
     a.out_sa = d_out;
     a.out_bytes = out_bytes;
@@ -455,14 +458,15 @@ capssa_status sample_sort_common(Ctx &c, const ST *text, uint64_t n, const uint6
 template <typename ST>
 capssa_status ext_mem_common(Ctx &c, const ST *text, uint64_t n, const void *positions,
                              int pos_bytes, uint64_t m, const capssa_limits *lp,
-                             const capssa_opts *opts, capssa_emit_fn emit, void *user) {
+                             const capssa_opts *opts, capssa_emit_fn emit, void *user,
+                             const uint32_t *keep_bits = nullptr) {
     if (!emit) return set_err(c, CAPSSA_EINVAL, "null emit callback");
-    const uint64_t count = positions ? m : n;
+    const uint64_t count = (positions || keep_bits) ? m : n;
     if (count == 0) return CAPSSA_OK;
     uint64_t *d_sa = (uint64_t *)ws_get(c, WS_OUT, count * 8 + 64);
     if (!d_sa) return set_err(c, CAPSSA_ENOMEM, "output buffer");
-    capssa_status s =
-        build_common<ST>(c, text, n, positions, pos_bytes, m, lp, opts, d_sa, 8, nullptr);
+    capssa_status s = build_common<ST>(c, text, n, positions, pos_bytes, m, lp, opts, d_sa, 8,
+                                       nullptr, nullptr, 0, keep_bits);
     if (s != CAPSSA_OK) return s;
     return emit_stream(c, d_sa, count, emit, user);
 }
@@ -487,25 +491,31 @@ __global__ void localize_kernel(const uint32_t *__restrict__ sa, uint32_t n,
     }
 }
 
-// Positions kept by the symbol range [lo, hi): flag[p] = 1.
+// Positions kept by the symbol range [lo, hi), one bit each (a warp ballot
+// per 32 positions), and their count.
 template <typename ST>
-__global__ void filter_flag_kernel(const ST *__restrict__ text, uint64_t n, uint64_t lo,
-                                   uint64_t hi, uint32_t *__restrict__ flag) {
-    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n;
-         p += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t v = (uint64_t)text[p];
-        flag[p] = (v >= lo && v < hi) ? 1u : 0u;
+__global__ void filter_bits_kernel(const ST *__restrict__ text, uint64_t n, uint64_t lo,
+                                   uint64_t hi, uint32_t *__restrict__ bits,
+                                   unsigned long long *__restrict__ count) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t words = (n + 31) / 32;
+    unsigned long long kept = 0;
+    for (uint64_t w = warp; w < words; w += nwarps) {
+        const uint64_t p = w * 32 + lane;
+        bool keep = false;
+        if (p < n) {
+            const uint64_t v = (uint64_t)text[p];
+            keep = v >= lo && v < hi;
+        }
+        const unsigned b = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) {
+            bits[w] = b;
+            kept += (unsigned long long)__popc(b);
+        }
     }
-}
-
-// Compaction: every kept p lands at its inclusive count - 1.
-__global__ void filter_scatter_kernel(const uint32_t *__restrict__ incl, uint64_t n,
-                                      uint32_t *__restrict__ pos) {
-    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n;
-         p += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t c = incl[p], before = p ? incl[p - 1] : 0u;
-        if (c != before) pos[c - 1] = (uint32_t)p;
-    }
+    if (lane == 0 && kept) atomicAdd(count, kept);
 }
 
 template <typename ST>
@@ -521,25 +531,27 @@ capssa_status filter_common(Ctx &c, const ST *text, uint64_t n, uint64_t lo, uin
     void *d_text = nullptr;
     capssa_status s = stage_text(c, text, n, &d_text);
     if (s != CAPSSA_OK) return s;
-    uint32_t *flag = (uint32_t *)ws_get(c, WS_MISC, n * 4 + 64);
-    uint32_t *pos = (uint32_t *)ws_get(c, WS_MISC2, n * 4 + 64);
-    if (!flag || !pos) return set_err(c, CAPSSA_ENOMEM, "filter workspace");
-    filter_flag_kernel<ST><<<grid_for(n, 256), 256, 0, c.stream>>>((const ST *)d_text, n, lo,
-                                                                    hi, flag);
+    // the kept positions as a bitmap (n / 8 bytes); the engine takes the kept
+    // suffixes from the full order, no position list is built
+    uint32_t *bits = (uint32_t *)ws_get(c, WS_KEEP, (n / 32 + 2) * 4 + 64);
+    if (!bits) return set_err(c, CAPSSA_ENOMEM, "filter workspace");
+    unsigned long long *cnt = (unsigned long long *)(c.d_flags + 4);
+    CAPSSA_CUDA(c, cudaMemsetAsync(cnt, 0, 8, c.stream));
+    filter_bits_kernel<ST><<<std::min<unsigned>(grid_for((n + 31) / 32 * 32, 256),
+                                                 (unsigned)c.sm_count * 16),
+                             256, 0, c.stream>>>((const ST *)d_text, n, lo, hi, bits, cnt);
     CAPSSA_LAUNCHED(c);
-    s = scan_u32(c, flag, flag, n, /*max_op=*/false, /*inclusive=*/true);
-    if (s != CAPSSA_OK) return s;
-    uint32_t m32 = 0;
-    CAPSSA_CUDA(c, cudaMemcpyAsync(&m32, flag + (n - 1), 4, cudaMemcpyDeviceToHost, c.stream));
+    unsigned long long *h_cnt = (unsigned long long *)c.h_scratch;
+    CAPSSA_CUDA(c, cudaMemcpyAsync(h_cnt, cnt, 8, cudaMemcpyDeviceToHost, c.stream));
     CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
-    *m_out = m32;
-    if ((!out_sa && !emit) || m32 == 0) return CAPSSA_OK;
-    filter_scatter_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(flag, n, pos);
-    CAPSSA_LAUNCHED(c);
+    const uint64_t m = *h_cnt;
+    *m_out = m;
+    if ((!out_sa && !emit) || m == 0) return CAPSSA_OK;
     if (emit)
-        return ext_mem_common<ST>(c, (const ST *)d_text, n, pos, 4, m32, lp, opts, emit, user);
-    return build_common<ST>(c, (const ST *)d_text, n, pos, 4, m32, lp, opts, out_sa, out_bytes,
-                            nullptr);
+        return ext_mem_common<ST>(c, (const ST *)d_text, n, nullptr, 4, m, lp, opts, emit, user,
+                                  bits);
+    return build_common<ST>(c, (const ST *)d_text, n, nullptr, 4, m, lp, opts, out_sa, out_bytes,
+                            nullptr, nullptr, 0, bits);
 }
 
 // Many texts: one segmented sort of the concatenation in segment-major

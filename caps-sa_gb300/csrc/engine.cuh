@@ -36,6 +36,9 @@ struct EngineArgs {
     uint64_t max_ctx;      // CAPSSA_UNBOUNDED or finite
     const void *positions; // device or nullptr (= every position)
     int pos_bytes;         // 4 or 8
+    // instead of positions: one bit per kept position (device, n bits), m of
+    // them set; the kept suffixes come out in suffix order
+    const uint32_t *keep_bits;
     uint64_t m;
     void *out_sa;          // device, m (or n) entries of out_bytes
     int out_bytes;         // 4 or 8

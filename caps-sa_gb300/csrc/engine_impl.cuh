@@ -2007,7 +2007,8 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     uint32_t *sa = (in_b && !vbits) ? vals_b : vals_a;
     // packed records are unpacked straight into a u32 output of a full build,
     // which then needs no final copy
-    if (vbits && !a.positions && a.out_bytes == 4 && a.out_sa) sa = (uint32_t *)a.out_sa;
+    if (vbits && !a.positions && !a.keep_bits && a.out_bytes == 4 && a.out_sa)
+        sa = (uint32_t *)a.out_sa;
     uint32_t *spare_vals = sa == vals_a ? vals_b : vals_a;
 
     // ---- 4. tied groups: direct comparison while shallow, rank doubling when deep
@@ -2469,7 +2470,7 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
     using namespace eng;
     const uint64_t n = a.n;
     const int lf = a.lim.longer_first;
-    const bool subset = a.positions != nullptr;
+    const bool subset = a.positions != nullptr || a.keep_bits != nullptr;
     const uint64_t m = subset ? a.m : n;
     c.stats.n_suffixes = m;
     if (n > 0xFFFFFFFEull) return set_err(c, CAPSSA_EUNSUPPORTED, "texts of 2^32-1 or more symbols");
@@ -2515,32 +2516,40 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
     uint32_t *sv_b = sv + m;
     const unsigned gm = grid_for(m, 256);
     const uint32_t *res = nullptr;
+    if (a.keep_bits && a.part_p) return set_err(c, CAPSSA_EINVAL, "no partition plan for a kept-bit set");
     if (!a.part_p && n > 0) {
         // distinct positions: mark them in a bitmap (L2-sized: n / 8 bytes)
         // and compact the full order, instead of sorting them by rank
         uint32_t *bits = (uint32_t *)ws_get(c, WS_KEYS_A, (size_t)n * 8);
         uint32_t *flag = (uint32_t *)ws_get(c, WS_KEYS_B, (size_t)n * 8);
         if (!bits || !flag) return set_err(c, CAPSSA_ENOMEM, "subset workspace");
-        int *fl = c.d_flags + 1;  // [0] beyond the end, [1] repeated
-        unsigned long long *cnt = (unsigned long long *)(c.d_flags + 4);
-        CAPSSA_CUDA(c, cudaMemsetAsync(fl, 0, 12 + 8, c.stream));
-        CAPSSA_CUDA(c, cudaMemsetAsync(bits, 0, ((size_t)n / 32 + 1) * 4, c.stream));
-        const unsigned gb = std::min<unsigned>(grid_for(m, 256), (unsigned)c.sm_count * 8);
-        if (a.pos_bytes == 4)
-            subset_bits_kernel<uint32_t><<<gb, 256, 0, c.stream>>>(
-                (const uint32_t *)a.positions, m, n, bits, fl, cnt);
-        else
-            subset_bits_kernel<uint64_t><<<gb, 256, 0, c.stream>>>(
-                (const uint64_t *)a.positions, m, n, bits, fl, cnt);
-        CAPSSA_LAUNCHED(c);
-        int *h = (int *)c.h_scratch;
-        unsigned long long *h_cnt = (unsigned long long *)c.h_scratch + 2;
-        CAPSSA_CUDA(c, cudaMemcpyAsync(h, fl, 8, cudaMemcpyDeviceToHost, c.stream));
-        CAPSSA_CUDA(c, cudaMemcpyAsync(h_cnt, cnt, 8, cudaMemcpyDeviceToHost, c.stream));
-        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
-        if (h[0]) return set_err(c, CAPSSA_EINVAL, "a position lies beyond the end of the text");
-        const unsigned long long n_empty = *h_cnt;
-        if (!h[1] && n_empty <= 1) {
+        unsigned long long n_empty = 0;
+        bool distinct = true;
+        if (a.keep_bits) {
+            bits = const_cast<uint32_t *>(a.keep_bits);
+        } else {
+            int *fl = c.d_flags + 1;  // [0] beyond the end, [1] repeated
+            unsigned long long *cnt = (unsigned long long *)(c.d_flags + 4);
+            CAPSSA_CUDA(c, cudaMemsetAsync(fl, 0, 12 + 8, c.stream));
+            CAPSSA_CUDA(c, cudaMemsetAsync(bits, 0, ((size_t)n / 32 + 1) * 4, c.stream));
+            const unsigned gb = std::min<unsigned>(grid_for(m, 256), (unsigned)c.sm_count * 8);
+            if (a.pos_bytes == 4)
+                subset_bits_kernel<uint32_t><<<gb, 256, 0, c.stream>>>(
+                    (const uint32_t *)a.positions, m, n, bits, fl, cnt);
+            else
+                subset_bits_kernel<uint64_t><<<gb, 256, 0, c.stream>>>(
+                    (const uint64_t *)a.positions, m, n, bits, fl, cnt);
+            CAPSSA_LAUNCHED(c);
+            int *h = (int *)c.h_scratch;
+            unsigned long long *h_cnt = (unsigned long long *)c.h_scratch + 2;
+            CAPSSA_CUDA(c, cudaMemcpyAsync(h, fl, 8, cudaMemcpyDeviceToHost, c.stream));
+            CAPSSA_CUDA(c, cudaMemcpyAsync(h_cnt, cnt, 8, cudaMemcpyDeviceToHost, c.stream));
+            CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+            if (h[0]) return set_err(c, CAPSSA_EINVAL, "a position lies beyond the end of the text");
+            n_empty = *h_cnt;
+            distinct = !h[1];
+        }
+        if (distinct && n_empty <= 1) {
             subset_flag_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa, (uint32_t)n, bits,
                                                                         flag);
             CAPSSA_LAUNCHED(c);
