@@ -31,8 +31,7 @@ import ctypes as C
 import enum
 import os
 import threading
-from dataclasses import dataclass, field
-from typing import Callable, Optional, Sequence
+from dataclasses import dataclass
 
 import numpy as np
 
