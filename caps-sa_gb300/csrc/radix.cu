@@ -240,7 +240,11 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
         if (lane < kWarps) s_scan[lane] = w;
     }
     __syncthreads();
-    s_lstart[dg] = x - total + (warp > 0 ? s_scan[warp - 1] : 0);
+    const uint32_t lstart = x - total + (warp > 0 ? s_scan[warp - 1] : 0);
+    s_lstart[dg] = lstart;
+    // from here s_gbase holds global start - local start: one lookup per
+    // record in the write-out
+    s_gbase[dg] -= lstart;
     __syncthreads();
 
 #pragma unroll
@@ -253,7 +257,7 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
     for (uint32_t i = tid; i < valid; i += kThreads) {
         uint64_t key = s_keys[i];
         uint32_t dd = (uint32_t)(key >> shift) & 255u;
-        uint32_t out = s_gbase[dd] + (i - s_lstart[dd]);
+        uint32_t out = s_gbase[dd] + i;
         if (out < n) {  // only false after a timed-out look-back (flagged)
             keys_out[out] = key;
             if (kVals) vals_out[out] = s_vals[i];
