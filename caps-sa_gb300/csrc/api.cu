@@ -88,8 +88,11 @@ KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits, int top_bits, uint
     // the position rides below the key when both fit in 64 bits; a plain
     // text then marks its k-1 short suffixes with one flag bit instead of a
     // length field (they are refined from depth 0)
+    // position bits below the key: segment-local positions when a segment
+    // index rides above it (the index recovers the global position)
+    const uint64_t npos = top_bits ? n_k : n;
     int vbits = 1;
-    while (vbits < 32 && (1ull << vbits) < n) vbits++;
+    while (vbits < 32 && (1ull << vbits) < npos) vbits++;
     if (plain && top_bits == 0 && kmin * g.b + 1 + vbits <= 64) {
         const int passes = (kmin * g.b + 1 + 7) / 8;
         // without the flag, one symbol less than kmin (random ties 2^H times
@@ -131,14 +134,20 @@ KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits, int top_bits, uint
     int k = kmax;
     if (kmin < kmax) {
         int passes = (top_bits + kmin * g.b + lbits_of(kmin) + 7) / 8;
+        // widening never gives up a packed position that fits at kmin (the
+        // sort then moves 8 bytes a record instead of 12)
+        const bool pos_fits = top_bits + kmin * g.b + lbits_of(kmin) + vbits <= 64;
         k = kmin;
-        while (k + 1 <= kmax && top_bits + (k + 1) * g.b + lbits_of(k + 1) <= 8 * passes) k++;
+        while (k + 1 <= kmax && top_bits + (k + 1) * g.b + lbits_of(k + 1) <= 8 * passes &&
+               (!pos_fits || top_bits + (k + 1) * g.b + lbits_of(k + 1) + vbits <= 64))
+            k++;
     }
     g.k = k;
     g.lbits = lbits_of(k);
     g.total = g.k * g.b + g.lbits;
     g.flag_len = 0;
     g.vbits = top_bits + g.total + vbits <= 64 ? vbits : 0;
+    g.local_pos = top_bits && g.vbits;
     return g;
 }
 

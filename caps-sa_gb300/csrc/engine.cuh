@@ -82,6 +82,8 @@ struct KeyGeom {
     // afterwards (a short suffix precedes exactly the full suffixes whose
     // key is >= its zero-padded key).
     int flagless;
+    // 1: the packed position is local to its segment (segment-major keys)
+    int local_pos;
 };
 // plain: the limits are PlainText's (only the last k-1 suffixes end early);
 // hbits: entropy of the symbols in bits (<= b).

@@ -162,7 +162,7 @@ __device__ __forceinline__ uint64_t window_at(const Packed &P, uint64_t p) {
 // (one 64-bit word per suffix).
 __global__ void __launch_bounds__(kKeyThreads)
     key_kernel(Packed P, uint64_t n, uint64_t n_rec, DevLimits L, int k, int lbits, int flag_len,
-               int vbits, int lf, int hist_shift, int n_passes, int seg_shift,
+               int vbits, int lf, int hist_shift, int n_passes, int seg_shift, int local_pos,
                uint64_t *__restrict__ keys, uint32_t *__restrict__ counts) {
     __shared__ uint32_t hist[8 * 256];
     for (int i = threadIdx.x; i < n_passes * 256; i += kKeyThreads) hist[i] = 0;
@@ -176,6 +176,8 @@ __global__ void __launch_bounds__(kKeyThreads)
         uint64_t end = p0 + dev_lim_at(L, p0);  // one past the last symbol of p0's suffix
         // segment-major keys carry the segment index above the key bits
         uint64_t seg = seg_shift ? dev_seg_at(L, p0) : 0;
+        // first position of p0's segment (segment-local packed positions)
+        uint64_t start = local_pos && seg ? __ldg(L.ends + seg - 1) : 0;
         uint64_t out[kKeyPer];
 #pragma unroll
         for (int e = 0; e < kKeyPer; e++) {
@@ -185,6 +187,7 @@ __global__ void __launch_bounds__(kKeyThreads)
                 if (p >= end) {  // p == end: the next segment starts here
                     end = p + dev_lim_at(L, p);
                     seg++;
+                    if (local_pos) start = p;
                 }
                 const uint64_t bit = p * (uint64_t)b;
                 const uint64_t wi = bit >> 6;
@@ -212,7 +215,7 @@ __global__ void __launch_bounds__(kKeyThreads)
                     if (ps < n_passes)
                         atomicAdd(&hist[ps * 256 + (((ps < 4 ? lo : hi) >> (8 * (ps & 3))) & 255u)],
                                   1u);
-                if (vbits) key = (key << vbits) | p;
+                if (vbits) key = (key << vbits) | (p - start);
             }
             out[e] = key;
         }
@@ -473,7 +476,8 @@ __global__ void __launch_bounds__(256)
     init_groups_kernel(const uint64_t *__restrict__ keys, uint32_t n, int k, uint64_t lmask,
                        int lf, int flag_len, int vshift, uint32_t *__restrict__ hd,
                        uint32_t *__restrict__ sa_out, GroupLists G,
-                       const ShortList *__restrict__ S) {
+                       const ShortList *__restrict__ S, int seg_at,
+                       const uint64_t *__restrict__ seg_ends) {
     static_assert(kLists <= 8, "two packed words of four 16-bit counters");
     __shared__ uint64_t sk[kInitTile + 2];  // sk[l + 1] = key of sorted index base + l
     __shared__ uint32_t s_base[kLists];
@@ -496,7 +500,16 @@ __global__ void __launch_bounds__(256)
     for (uint32_t l = threadIdx.x; l < valid; l += 256) {
         const uint64_t item = keys[base + l];
         sk[l + 1] = item >> vshift;
-        if (sa_out) sa_out[base + l + shift_of(base + l)] = (uint32_t)(item & vmask);
+        if (sa_out) {
+            // segment-local positions (seg_at > 0): the segment index above
+            // the key gives the segment's first position
+            uint64_t pos = item & vmask;
+            if (seg_at) {
+                const uint64_t sg = item >> seg_at;
+                pos += sg ? __ldg(seg_ends + sg - 1) : 0ull;
+            }
+            sa_out[base + l + shift_of(base + l)] = (uint32_t)pos;
+        }
     }
     if (threadIdx.x == 0) sk[0] = base > 0 ? keys[base - 1] >> vshift : 0ull;
     if (threadIdx.x == 32) sk[valid + 1] = base + valid < n ? keys[base + valid] >> vshift : 0ull;
@@ -1944,6 +1957,7 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     // otherwise, when key and position fit one word, the sort moves 8 B per
     // suffix and pass instead of 12
     const int vbits = msd ? 0 : geo.vbits;
+    const int local_pos = vbits && seg_bits && geo.local_pos ? 1 : 0;
     const int hist_shift = msd ? geo.total - bb : 0;
     const int key_passes = msd ? (bb + 7) / 8 : (sort_bits + 7) / 8;
     uint32_t *counts = radix::hist_buffer(c);
@@ -1968,7 +1982,8 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     P.mask = P.spw * P.b >= 64 ? ~0ull : (~0ull << (64 - P.spw * P.b));
     key_kernel<<<std::min<unsigned>(grid_for(n_rec, kKeyTile), c.sm_count * 8), kKeyThreads, 0,
                  c.stream>>>(P, n, n_rec, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf,
-                             hist_shift, key_passes, seg_bits ? geo.total : 0, keys_a, counts);
+                             hist_shift, key_passes, seg_bits ? geo.total : 0, local_pos, keys_a,
+                             counts);
     CAPSSA_LAUNCHED(c);
     cudaEventRecord(c.pev[1], c.stream);
     bool in_b = false;
@@ -2046,7 +2061,7 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     CAPSSA_CUDA(c, cudaMemsetAsync(G.ctr, 0, sizeof(Counters), c.stream));
     init_groups_kernel<<<grid_for(n_rec, kInitTile), 256, 0, c.stream>>>(
         skeys, (uint32_t)n_rec, geo.k, (1ull << geo.lbits) - 1, lf, geo.flag_len, vbits, hd,
-        vbits ? sa : nullptr, G, d_short);
+        vbits ? sa : nullptr, G, d_short, local_pos ? vbits + geo.total : 0, a.lim.ends);
     CAPSSA_LAUNCHED(c);
     if (n_short) {
         short_write_kernel<<<1, 64, 0, c.stream>>>(d_short, sa, hd);
