@@ -1611,14 +1611,14 @@ __global__ void head_key_kernel(const uint32_t *__restrict__ sa, uint32_t n,
     if (blockIdx.x == 0 && threadIdx.x == 0) hkey[n] = lf ? n + 1 : 0u;
 }
 
-// Chunk-major order of the sorted suffixes (full text): key = chunk of the
-// position, in SA order; a stable sort by the key with the SA indices as
-// generated values then lists every chunk's suffixes in sorted order, each
-// by its rank.
+// Chunk-major order of the sorted suffixes (full text): record = chunk of
+// the position above the SA index, in SA order; a stable sort on the chunk
+// bits then lists every chunk's suffixes in sorted order, each by its rank
+// (the record's low 32 bits).
 __global__ void chunk_key_kernel(const uint32_t *__restrict__ sa, uint32_t n, uint32_t chunk,
                                  uint64_t *__restrict__ keys) {
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-        keys[j] = sa[j] / chunk;
+        keys[j] = ((uint64_t)(sa[j] / chunk) << 32) | j;
 }
 
 // Subsets: key = (chunk of the input index, rank of the suffix), value =
@@ -1640,7 +1640,8 @@ __global__ void chunk_key_subset_kernel(const PT *__restrict__ pos, uint64_t m, 
 // Evenly spaced midpoints of every sorted chunk (evenly_spaced,
 // src/ext_mem.rs:1291-1305), with each sample's rank key.  `isa` null: the
 // chunks hold SA indices (full text), which are the ranks.
-__global__ void sample_kernel(const uint32_t *__restrict__ chunked, uint64_t m, uint32_t chunk,
+__global__ void sample_kernel(const uint32_t *__restrict__ chunked,
+                              const uint64_t *__restrict__ chunked_rec, uint64_t m, uint32_t chunk,
                               uint32_t p, uint32_t per, const uint32_t *__restrict__ soff,
                               uint64_t n, const uint32_t *__restrict__ isa, int lf,
                               uint64_t *__restrict__ skey, uint32_t *__restrict__ spos) {
@@ -1654,7 +1655,7 @@ __global__ void sample_kernel(const uint32_t *__restrict__ chunked, uint64_t m, 
         const uint64_t cnt = per < len ? per : len;
         if (sidx >= cnt) continue;
         const uint64_t at = cnt >= len ? sidx : (2 * (uint64_t)sidx + 1) * len / (2 * cnt);
-        const uint32_t q = chunked[start + at];
+        const uint32_t q = chunked ? chunked[start + at] : (uint32_t)chunked_rec[start + at];
         const uint32_t o = soff[i] + sidx;
         spos[o] = q;
         skey[o] = !isa ? (uint64_t)q + 1
@@ -2331,8 +2332,7 @@ capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
         chunk_key_kernel<<<grid_for(m, 256), 256, 0, c.stream>>>(sa_full, (uint32_t)m, chunk,
                                                                  ka);
         CAPSSA_LAUNCHED(c);
-        s = radix::sort_pairs(c, ka, va, kb, vb, (uint32_t)m, 0, cbits, /*gen_vals=*/true, 0,
-                              &in_b);
+        s = radix::sort_keys(c, ka, kb, (uint32_t)m, 32, 32 + cbits, &in_b);
     } else {
         const int rbits = bits_for(n + 1);
         if (a.pos_bytes == 4)
@@ -2346,7 +2346,9 @@ capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
     }
     if (s != CAPSSA_OK) return s;
     kt.mark(c.stream, "chunks");
-    const uint32_t *chunked = in_b ? vb : va;
+    // full text: SA indices in the low halves of the sorted records
+    const uint32_t *chunked = subset ? (in_b ? vb : va) : nullptr;
+    const uint64_t *chunked_rec = subset ? nullptr : (in_b ? kb : ka);
     // 2. samples and their rank keys, sorted; pivots
     std::vector<uint32_t> soff(p + 1, 0);
     for (uint32_t i = 0; i < p; i++) {
@@ -2377,7 +2379,7 @@ capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
     CAPSSA_CUDA(c, cudaMemcpyAsync(d_soff, soff.data(), (p + 1) * 4, cudaMemcpyHostToDevice,
                                    c.stream));
     sample_kernel<<<grid_for((uint64_t)p * per, 256), 256, 0, c.stream>>>(
-        chunked, m, chunk, p, per, d_soff, n, subset ? isa : nullptr, lf, sk_a, sp_a);
+        chunked, chunked_rec, m, chunk, p, per, d_soff, n, subset ? isa : nullptr, lf, sk_a, sp_a);
     CAPSSA_LAUNCHED(c);
     bool s_in_b = false;
     s = radix::sort_pairs(c, sk_a, sp_a, sk_b, sp_b, ns, 0, bits_for(n + 1), false, 0, &s_in_b);
