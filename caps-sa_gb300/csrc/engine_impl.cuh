@@ -159,7 +159,9 @@ __device__ __forceinline__ uint64_t window_at(const Packed &P, uint64_t p) {
 // consecutive positions of a tile (the segment end is tracked across
 // them); blocks stride over the tiles and add their histograms to the
 // global counts once.  With vbits > 0 the position is packed below the key
-// (one 64-bit word per suffix).
+// (one 64-bit word per suffix).  kPlain: a PlainText text with no segment
+// index and no bucket shift (limits are n - p, nothing to track).
+template <bool kPlain>
 __global__ void __launch_bounds__(kKeyThreads)
     key_kernel(Packed P, uint64_t n, uint64_t n_rec, DevLimits L, int k, int lbits, int flag_len,
                int vbits, int lf, int hist_shift, int n_passes, int seg_shift, int local_pos,
@@ -173,18 +175,19 @@ __global__ void __launch_bounds__(kKeyThreads)
          t0 += (uint64_t)gridDim.x * kKeyTile) {
         const uint64_t p0 = t0 + (uint64_t)threadIdx.x * kKeyPer;
         if (p0 >= n_rec) continue;
-        uint64_t end = p0 + dev_lim_at(L, p0);  // one past the last symbol of p0's suffix
+        // one past the last symbol of p0's suffix
+        uint64_t end = kPlain ? n : p0 + dev_lim_at(L, p0);
         // segment-major keys carry the segment index above the key bits
-        uint64_t seg = seg_shift ? dev_seg_at(L, p0) : 0;
+        uint64_t seg = !kPlain && seg_shift ? dev_seg_at(L, p0) : 0;
         // first position of p0's segment (segment-local packed positions)
-        uint64_t start = local_pos && seg ? __ldg(L.ends + seg - 1) : 0;
+        uint64_t start = !kPlain && local_pos && seg ? __ldg(L.ends + seg - 1) : 0;
         uint64_t out[kKeyPer];
 #pragma unroll
         for (int e = 0; e < kKeyPer; e++) {
             const uint64_t p = p0 + e;
             uint64_t key = 0;
             if (p < n_rec) {
-                if (p >= end) {  // p == end: the next segment starts here
+                if (!kPlain && p >= end) {  // p == end: the next segment starts here
                     end = p + dev_lim_at(L, p);
                     seg++;
                     if (local_pos) start = p;
@@ -207,8 +210,8 @@ __global__ void __launch_bounds__(kKeyThreads)
                 const uint64_t field = flag_len ? (uint64_t)((take == k) != (lf != 0))
                                                 : (uint64_t)(lf ? k - take : take);
                 key = lbits ? (content << lbits) | field : content;
-                if (seg_shift) key |= seg << seg_shift;
-                const uint64_t hk = key >> hist_shift;
+                if (!kPlain && seg_shift) key |= seg << seg_shift;
+                const uint64_t hk = kPlain ? key : key >> hist_shift;
                 const uint32_t lo = (uint32_t)hk, hi = (uint32_t)(hk >> 32);
 #pragma unroll
                 for (int ps = 0; ps < 8; ps++)
@@ -1981,10 +1984,15 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     P.b = geo.b;
     P.spw = 64 / geo.b;
     P.mask = P.spw * P.b >= 64 ? ~0ull : (~0ull << (64 - P.spw * P.b));
-    key_kernel<<<std::min<unsigned>(grid_for(n_rec, kKeyTile), c.sm_count * 8), kKeyThreads, 0,
-                 c.stream>>>(P, n, n_rec, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf,
-                             hist_shift, key_passes, seg_bits ? geo.total : 0, local_pos, keys_a,
-                             counts);
+    const unsigned kgrid = std::min<unsigned>(grid_for(n_rec, kKeyTile), c.sm_count * 8);
+    if (!a.lim.segmented && !seg_bits && hist_shift == 0)
+        key_kernel<true><<<kgrid, kKeyThreads, 0, c.stream>>>(
+            P, n, n_rec, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf, hist_shift, key_passes,
+            0, 0, keys_a, counts);
+    else
+        key_kernel<false><<<kgrid, kKeyThreads, 0, c.stream>>>(
+            P, n, n_rec, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf, hist_shift, key_passes,
+            seg_bits ? geo.total : 0, local_pos, keys_a, counts);
     CAPSSA_LAUNCHED(c);
     cudaEventRecord(c.pev[1], c.stream);
     bool in_b = false;
