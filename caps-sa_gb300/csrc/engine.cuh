@@ -6,18 +6,22 @@
 //
 //  1. alphabet scan -> order-preserving dense codes (Packer::new,
 //     src/pack.rs:103-167), b bits per symbol;
-//  2. one 64-bit composite key per text position: the first k symbols of
-//     the suffix, truncated at its limit (min(k, lim_at(p)), as
-//     key_at_bounded does, src/pack.rs:187-203), padded, followed by the
-//     number of symbols taken.  Key order never contradicts
-//     suffix_cmp_with (src/lcp.rs:184-201); equal keys mean "equal through
-//     k symbols" or, when fewer than k were taken, a finished comparison;
-//  3. stable LSD radix sort of (key, position);
-//  4. rank doubling on the groups that are still tied: a suffix p of an
-//     unresolved group of depth h is re-keyed by the rank of p + h (or by
-//     "ended" when lim_at(p) == h); each round doubles h.  Ranks are
-//     group-head SA indices, so equal rank == equal comparison so far.
-//
+//  2. one composite record per text position: the first k symbols of the
+//     suffix, truncated at its limit (min(k, lim_at(p)), as key_at_bounded
+//     does, src/pack.rs:187-203), padded, followed by a length field (the
+//     number of symbols taken), a one-bit "ended early" flag (plain texts),
+//     or nothing (flagless plain texts, whose k - 1 short suffixes are left
+//     out of the sort and placed afterwards); the position rides below the
+//     key when it fits, and a segment index above it in segment-major order.
+//     Key order never contradicts suffix_cmp_with (src/lcp.rs:184-201);
+//  3. stable LSD radix sort of the records;
+//  4. the groups still tied are resolved by size class: direct comparison
+//     on a bit-packed copy of the text for groups of up to 2048 members and
+//     depths up to 4096 symbols, rank doubling for the rest (a suffix p of
+//     a group of depth h is re-keyed by the rank of p + h, or by "ended"
+//     when lim_at(p) == h; ranks are group-head SA indices, so equal rank ==
+//     equal comparison so far).
+
 // Boundary orders: ShorterFirst (the default boundary_order) leaves suffixes
 // that end together with equal content tied; their output order is
 // ascending position.  LongerFirst (STAR) orders them by position, which the
