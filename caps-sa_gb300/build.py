@@ -2,7 +2,8 @@
 
 Each translation unit compiles in parallel; the objects link into one
 shared library with the CUDA runtime linked statically, so the library
-carries no dependency beyond the driver.  Output: _build/ next to this file.
+carries no dependency beyond the NVIDIA kernel driver.  Output: _build/ next to
+this file.
 """
 from __future__ import annotations
 
