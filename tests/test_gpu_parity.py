@@ -556,3 +556,22 @@ def test_flagless_short_suffix_placement(ctx, dtype):
     # LongerFirst keeps the flag (and its own order)
     t = endings["zeros"].astype(dtype)
     check_against_oracle(ctx, t, longer_first=True)
+
+
+def test_flagless_with_context_bound_and_lcp(ctx):
+    """Flagless keys (n = 150,000 over 4 symbols) combined with a finite
+    max_context, a LongerFirst subset, and the LCP output."""
+    rng = np.random.default_rng(151)
+    n = 150000
+    t = rng.integers(0, 4, n).astype(np.uint8)
+    t[20000:26000] = t[60000:66000]      # a long repeat
+    t[n - 3000:] = 0                     # a run at the end
+    for max_ctx in (5, 40):
+        check_against_oracle(ctx, t, max_ctx=max_ctx)
+    sa, lcp = ctx.build_in_memory_lcp(t, index=np.uint64)
+    want = orc.build_in_memory(t, index=np.uint64)
+    assert np.array_equal(sa, want)
+    assert lcp[0] == 0
+    assert np.array_equal(lcp[1:], ctx.lcp(t, sa[:-1], sa[1:]))
+    keep = np.nonzero(rng.random(n) < 0.5)[0]
+    check_against_oracle(ctx, t, positions=keep, index=np.uint64)
