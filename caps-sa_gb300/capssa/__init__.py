@@ -22,8 +22,9 @@ Texts are numpy arrays of uint8/uint16/uint32 (or CUDA tensors exposing
 ``I: Index`` (``index=np.uint32`` or ``np.uint64``).  Contract violations the
 reference panics on raise ``ValueError``; emit aborts raise ``BuildError``.
 
-Every call runs the CUDA library; there is no CPU fallback, and importing
-this module fails loudly when the library has not been built.
+Every call runs the CUDA library; there is no CPU fallback.  The library is
+mapped on first use (a Context, or an attribute of ``lib``), which fails
+loudly when it has not been built.
 """
 from __future__ import annotations
 
@@ -92,7 +93,6 @@ class _Opts(C.Structure):
                 ("flags", C.c_uint64), ("reserved", C.c_uint64 * 5)]
 
 
-FLAG_BUCKET_FRONT = 1
 
 
 class _Stats(C.Structure):
@@ -188,7 +188,22 @@ def _load():
     return L
 
 
-lib = _load()
+class _LazyLib:
+    """The CUDA library, loaded on first use: importing the package (for
+    example only for its workload generators or file formats) maps nothing."""
+
+    _L = None
+
+    def _get(self):
+        if _LazyLib._L is None:
+            _LazyLib._L = _load()
+        return _LazyLib._L
+
+    def __getattr__(self, name):
+        return getattr(self._get(), name)
+
+
+lib = _LazyLib()
 
 
 # ------------------------------------------------------------------ providers
@@ -244,10 +259,8 @@ class SegmentedText:
 
 @dataclass
 class Opts:
-    """src/sample_sort.rs:70-85.  bucket_front: sort through the 16-bit bucket
-    front end (same output; CAPSSA_FLAG_BUCKET_FRONT)."""
+    """src/sample_sort.rs:70-85."""
     max_context: int = UNBOUNDED
-    bucket_front: bool = False
 
 
 @dataclass
@@ -257,7 +270,6 @@ class ExtMemOpts:
     subproblem_count: int = 0
     partition: Partition = Partition.AUTO
     host_threads: int = 0
-    bucket_front: bool = False
 
 
 def _copts(o) -> _Opts:
@@ -268,7 +280,7 @@ def _copts(o) -> _Opts:
         c.subproblem_count = int(getattr(o, "subproblem_count", 0))
         c.partition = int(getattr(o, "partition", 0))
         c.host_threads = int(getattr(o, "host_threads", 0))
-        c.flags = FLAG_BUCKET_FRONT if getattr(o, "bucket_front", False) else 0
+        c.flags = 0
     return c
 
 

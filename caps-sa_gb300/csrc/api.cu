@@ -361,7 +361,6 @@ capssa_status build_common(Ctx &c, const ST *text, uint64_t n, const void *posit
     a.out_sa = d_out;
     a.out_bytes = out_bytes;
     a.out_lcp = d_lcp;
-    a.bucket_front = opts && (opts->flags & CAPSSA_FLAG_BUCKET_FRONT) ? 1 : 0;
     a.seg_major = seg_major_len ? 1 : 0;
     a.seg_max_len = seg_major_len;
     if (part) {

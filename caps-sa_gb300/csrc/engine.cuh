@@ -47,7 +47,6 @@ struct EngineArgs {
     void *out_sa;          // device, m (or n) entries of out_bytes
     int out_bytes;         // 4 or 8
     void *out_lcp;         // device or nullptr
-    int bucket_front;      // 1: bucket the keys by their top 16 bits first (bucket.cuh)
     int seg_major;         // 1: sort by (segment, suffix): every segment's suffixes
                            // contiguous, in their own order (many independent texts)
     uint64_t seg_max_len;  // seg_major: the longest segment

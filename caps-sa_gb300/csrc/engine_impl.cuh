@@ -11,7 +11,6 @@
 #include <vector>
 
 #include "engine.cuh"
-#include "bucket.cuh"
 #include "cdf.cuh"
 #include "lcp.cuh"
 #include "radix.cuh"
@@ -45,9 +44,7 @@ enum GroupList : int {
 };
 constexpr uint32_t kTinyMax = 8;
 constexpr uint32_t kTiny4 = 4;
-#ifndef CAPSSA_PAIR_BURST
-#define CAPSSA_PAIR_BURST 4  // windows the pair kernel loads in its first round trip
-#endif
+constexpr int kPairBurst = 4;  // windows the pair kernel loads in its first round trip
 
 // Device counters of the refinement rounds, double-buffered by round parity.
 struct Counters {
@@ -160,11 +157,11 @@ __device__ __forceinline__ uint64_t window_at(const Packed &P, uint64_t p) {
 // them); blocks stride over the tiles and add their histograms to the
 // global counts once.  With vbits > 0 the position is packed below the key
 // (one 64-bit word per suffix).  kPlain: a PlainText text with no segment
-// index and no bucket shift (limits are n - p, nothing to track).
+// index (limits are n - p, nothing to track).
 template <bool kPlain>
 __global__ void __launch_bounds__(kKeyThreads)
     key_kernel(Packed P, uint64_t n, uint64_t n_rec, DevLimits L, int k, int lbits, int flag_len,
-               int vbits, int lf, int hist_shift, int n_passes, int seg_shift, int local_pos,
+               int vbits, int lf, int n_passes, int seg_shift, int local_pos,
                uint64_t *__restrict__ keys, uint32_t *__restrict__ counts) {
     __shared__ uint32_t hist[8 * 256];
     for (int i = threadIdx.x; i < n_passes * 256; i += kKeyThreads) hist[i] = 0;
@@ -211,8 +208,7 @@ __global__ void __launch_bounds__(kKeyThreads)
                                                 : (uint64_t)(lf ? k - take : take);
                 key = lbits ? (content << lbits) | field : content;
                 if (!kPlain && seg_shift) key |= seg << seg_shift;
-                const uint64_t hk = kPlain ? key : key >> hist_shift;
-                const uint32_t lo = (uint32_t)hk, hi = (uint32_t)(hk >> 32);
+                const uint32_t lo = (uint32_t)key, hi = (uint32_t)(key >> 32);
 #pragma unroll
                 for (int ps = 0; ps < 8; ps++)
                     if (ps < n_passes)
@@ -923,7 +919,7 @@ __global__ void __launch_bounds__(256)
         cap = o > kDirectCap ? o : kDirectCap;
         uint32_t p0 = sa[g.x], p1 = sa[g.x + 1];
         uint64_t l0 = dev_lim_at(L, p0), l1 = dev_lim_at(L, p1);
-        int r = direct_cmp<CAPSSA_PAIR_BURST>(P, p0, l0, p1, l1, o, cap, lf);
+        int r = direct_cmp<kPairBurst>(P, p0, l0, p1, l1, o, cap, lf);
         if (r == 1 || ((r == 0 || r == 2) && p0 > p1)) {
             uint32_t t = p0;
             p0 = p1;
@@ -1932,8 +1928,8 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     // one segment is already in segment-major order
     c.seg_major_done = a.seg_major && (seg_bits > 0 || a.lim.n_ends <= 1);
     // a ShorterFirst plain text may drop the early-end flag when that saves a
-    // radix pass (not with the bucket front end, which sorts key + value)
-    const bool allow_flagless = !a.lim.segmented && !lf && !a.bucket_front && n <= 0xFFFFFFFEull;
+    // radix pass
+    const bool allow_flagless = !a.lim.segmented && !lf && n <= 0xFFFFFFFEull;
     const KeyGeom geo = key_geom(b, n, !a.lim.segmented, hbits, seg_bits,
                                  seg_bits ? a.seg_max_len : 0, allow_flagless);
     // records the radix sort orders: every suffix, or the full ones only
@@ -1954,16 +1950,11 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     if (!keys_a || !keys_b || !vals_a || !vals_b || !rank || !key2)
         return set_err(c, CAPSSA_ENOMEM, "suffix-sort workspace");
     Coder<S> coder{table, minv};
-    // large texts: two passes on the top 16 key bits make 65536 buckets
-    // contiguous, then each bucket is sorted on chip (bucket.cuh)
-    const int bb = bucket::kBucketBits;
-    const bool msd = a.bucket_front && !seg_bits && n >= (1ull << 22) && geo.total > bb + 8;
-    // otherwise, when key and position fit one word, the sort moves 8 B per
-    // suffix and pass instead of 12
-    const int vbits = msd ? 0 : geo.vbits;
+    // when key and position fit one word, the sort moves 8 B per suffix and
+    // pass instead of 12
+    const int vbits = geo.vbits;
     const int local_pos = vbits && seg_bits && geo.local_pos ? 1 : 0;
-    const int hist_shift = msd ? geo.total - bb : 0;
-    const int key_passes = msd ? (bb + 7) / 8 : (sort_bits + 7) / 8;
+    const int key_passes = (sort_bits + 7) / 8;
     uint32_t *counts = radix::hist_buffer(c);
     if (!counts) return set_err(c, CAPSSA_ENOMEM, "radix histograms");
     CAPSSA_CUDA(c, cudaMemsetAsync(counts, 0, radix::kMaxPasses * 256 * 4, c.stream));
@@ -1985,13 +1976,13 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     P.spw = 64 / geo.b;
     P.mask = P.spw * P.b >= 64 ? ~0ull : (~0ull << (64 - P.spw * P.b));
     const unsigned kgrid = std::min<unsigned>(grid_for(n_rec, kKeyTile), c.sm_count * 8);
-    if (!a.lim.segmented && !seg_bits && hist_shift == 0)
+    if (!a.lim.segmented && !seg_bits)
         key_kernel<true><<<kgrid, kKeyThreads, 0, c.stream>>>(
-            P, n, n_rec, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf, hist_shift, key_passes,
-            0, 0, keys_a, counts);
+            P, n, n_rec, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf, key_passes, 0, 0,
+            keys_a, counts);
     else
         key_kernel<false><<<kgrid, kKeyThreads, 0, c.stream>>>(
-            P, n, n_rec, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf, hist_shift, key_passes,
+            P, n, n_rec, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf, key_passes,
             seg_bits ? geo.total : 0, local_pos, keys_a, counts);
     CAPSSA_LAUNCHED(c);
     cudaEventRecord(c.pev[1], c.stream);
@@ -2000,31 +1991,11 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     capssa_status s =
         vbits ? radix::sort_keys(c, keys_a, keys_b, (uint32_t)n_rec, vbits, vbits + sort_bits,
                                  &in_b, &passes, /*hist_ready=*/true)
-              : radix::sort_pairs(c, keys_a, vals_a, keys_b, vals_b, nn, hist_shift, sort_bits,
-                                  true, 0, &in_b, &passes, /*hist_ready=*/true);
+              : radix::sort_pairs(c, keys_a, vals_a, keys_b, vals_b, nn, 0, sort_bits, true, 0,
+                                  &in_b, &passes, /*hist_ready=*/true);
     if (s != CAPSSA_OK) return s;
     c.stats.sort_passes = (uint32_t)passes;
     c.stats.sort_item_bytes = vbits ? 8u : 12u;
-    if (msd) {
-        uint64_t *xk = in_b ? keys_b : keys_a, *yk = in_b ? keys_a : keys_b;
-        uint32_t *xv = in_b ? vals_b : vals_a, *yv = in_b ? vals_a : vals_b;
-        uint32_t *d_start = (uint32_t *)ws_get(c, WS_MISC2, (bucket::kBuckets + 1) * 4 + 64);
-        if (!d_start) return set_err(c, CAPSSA_ENOMEM, "bucket starts");
-        s = bucket::bucket_starts(c, xk, nn, hist_shift, d_start);
-        if (s != CAPSSA_OK) return s;
-        std::vector<uint32_t> h_start(bucket::kBuckets + 1);
-        CAPSSA_CUDA(c, cudaMemcpyAsync(h_start.data(), d_start, h_start.size() * 4,
-                                       cudaMemcpyDeviceToHost, c.stream));
-        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
-        uint32_t maxb = 0;
-        for (uint32_t b = 0; b < bucket::kBuckets; b++) maxb = std::max(maxb, h_start[b + 1] - h_start[b]);
-        c.stats.partitions = bucket::kBuckets;
-        c.stats.max_partition = maxb;
-        s = bucket::sort_buckets(c, xk, xv, yk, yv, (uint64_t *)key2, rank, nn, d_start,
-                                 h_start.data(), hist_shift);
-        if (s != CAPSSA_OK) return s;
-        in_b = xk == keys_b;
-    }
     cudaEventRecord(c.pev[2], c.stream);
     const uint64_t *skeys = in_b ? keys_b : keys_a;
     // packed positions are unpacked into vals_a by init_groups

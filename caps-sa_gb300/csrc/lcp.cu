@@ -2,7 +2,6 @@
 // suffix_cmp_with, the bounded-context run flags, and the merge-path
 // version of the reference's LCP-enhanced two-way merge.
 #include <algorithm>
-#include <mutex>
 
 #include "lcp.cuh"
 
@@ -423,23 +422,17 @@ constexpr size_t kNoAllocScratchBytes = kNoAllocFlagOff + 256;  // about 1.2 MiB
 // call shares it and it keeps the last call's contents.
 static __device__ __align__(256) unsigned char g_noalloc_merge_scratch[kNoAllocScratchBytes];
 
-constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void *g_noalloc_ptr[kNoAllocMaxDevices] = {};
-
-// Device address of the scratch array on the current device, looked up once
-// per device (the host-side symbol is only a stand-in, never a device
-// address).
-cudaError_t noalloc_scratch(int dev, unsigned char **out) {
-    if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_merge_scratch);
-        if (e != cudaSuccess) return e;
-        g_noalloc_ptr[dev] = p;
-    }
-    *out = (unsigned char *)g_noalloc_ptr[dev];
+// Device address of the scratch array in the current context.  The
+// host-side symbol is only a stand-in, never a device address, and the
+// address belongs to the context that loaded this module: it is looked up
+// on every call (after the first call on a device, which loads the module,
+// this is a runtime table lookup), so a reset device or another current
+// context never sees a stale address.
+cudaError_t noalloc_scratch(unsigned char **out) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_merge_scratch);
+    if (e != cudaSuccess) return e;
+    *out = (unsigned char *)p;
     return cudaSuccess;
 }
 
@@ -474,18 +467,22 @@ extern "C" capssa_status capssa_merge_noalloc_u8_u32(
     const uint32_t *y, const uint32_t *lcp_y, uint64_t len_y, uint64_t max_context, uint32_t *z,
     uint32_t *lcp_z) {
     using namespace capssa;
+    // refuse oversize merges before any work, without letting the sum wrap
+    if (len_x > kNoAllocMaxRecords || len_y > kNoAllocMaxRecords - len_x) return CAPSSA_EINVAL;
     const uint64_t total = len_x + len_y;
     if (total == 0) return CAPSSA_OK;
-    if (total > kNoAllocMaxRecords) return CAPSSA_EINVAL;
     if (boundary != CAPSSA_SHORTER_FIRST && boundary != CAPSSA_LONGER_FIRST) return CAPSSA_EINVAL;
     if (!text || !z || !lcp_z || (len_x && (!x || !lcp_x)) || (len_y && (!y || !lcp_y)) ||
         (n_ends && !ends))
         return CAPSSA_EINVAL;
     cudaStream_t stream = (cudaStream_t)cuda_stream;
+    // an error the caller left pending is theirs: report it without clearing
+    // it, so that every error read after the launches below is this call's
+    if (cudaPeekAtLastError() != cudaSuccess) return CAPSSA_ECUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return CAPSSA_ECUDA;
     unsigned char *scratch = nullptr;
-    if (noalloc_scratch(dev, &scratch) != cudaSuccess) return CAPSSA_ECUDA;
+    if (noalloc_scratch(&scratch) != cudaSuccess) return CAPSSA_ECUDA;
     uint64_t *split = (uint64_t *)scratch;
     uint8_t *safe = scratch + kNoAllocSafeOff;
     uint32_t *bad = (uint32_t *)(scratch + kNoAllocFlagOff);

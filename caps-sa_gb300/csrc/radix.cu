@@ -23,13 +23,7 @@
 namespace capssa {
 namespace radix {
 
-#ifndef CAPSSA_RADIX_MIN_BLOCKS
-#define CAPSSA_RADIX_MIN_BLOCKS 3
-#endif
-#ifndef CAPSSA_RADIX_RANK
-#define CAPSSA_RADIX_RANK 2  // 0: load/store ranking, 1: match + atomics, 2: ballots + atomics
-#endif
-
+constexpr int kMinBlocks = 3;  // resident blocks per SM the register budget is sized for
 constexpr int kRadix = 256;
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
@@ -79,10 +73,7 @@ __device__ __forceinline__ void st_volatile_u64(unsigned long long *p, unsigned 
 // nearest inclusive prefix (P).  kLookBatch predecessors are read per round trip;
 // a predecessor that has published nothing yet is polled again (bounded by
 // kSpinLimit polls, then DEV_LOOKBACK_TIMEOUT).
-#ifndef CAPSSA_RADIX_LOOKBATCH
-#define CAPSSA_RADIX_LOOKBATCH 4
-#endif
-constexpr int kLookBatch = CAPSSA_RADIX_LOOKBATCH;
+constexpr int kLookBatch = 4;
 
 __device__ __forceinline__ uint64_t lookback(const unsigned long long *status, uint32_t tile,
                                              uint32_t dg, int *err) {
@@ -128,7 +119,7 @@ constexpr int kPairs = 0, kGenVals = 1, kKeysOnly = 2;
 // IT records per thread (the tile is 256 * IT records): a template
 // parameter so that the tuner below can pick the shape per workload.
 template <int MODE, int IT>
-__global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
     onesweep_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
                     uint64_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out,
                     uint32_t n, int shift, const uint32_t *__restrict__ digit_offsets,
@@ -175,28 +166,11 @@ __global__ void __launch_bounds__(kThreads, CAPSSA_RADIX_MIN_BLOCKS)
     // warp-level multisplit: rank of each item among equal digits of this warp
     uint32_t *wh = s_whist + warp * kRadix;
     const unsigned lt_mask = (1u << lane) - 1u;
-#if CAPSSA_RADIX_RANK == 0
 #pragma unroll
     for (int j = 0; j < IT; j++) {
-        unsigned peers = __match_any_sync(0xffffffffu, d[j]);
-        uint32_t pre = __popc(peers & lt_mask);
-        uint32_t cnt = wh[d[j]];
-        __syncwarp();
-        if (pre == 0) wh[d[j]] = cnt + __popc(peers);
-        __syncwarp();
-        r[j] = cnt + pre;
-    }
-#else
-#pragma unroll
-    for (int j = 0; j < IT; j++) {
-#if CAPSSA_RADIX_RANK == 1
-        const unsigned peers = __match_any_sync(0xffffffffu, d[j]);
-#else
         const unsigned peers = warp_match_bits<8>(d[j]);
-#endif
         r[j] = warp_rank_digit(wh, d[j], peers, lt_mask, lane);
     }
-#endif
     __syncthreads();
 
     // thread `tid` owns digit `tid`: warp prefixes, tile total, look-back

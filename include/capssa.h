@@ -88,14 +88,9 @@ typedef struct capssa_opts {
                                   effective_subproblem_count, src/ext_mem.rs:1159-1178 */
     int32_t partition;         /* capssa_partition (sample-sort builders) */
     int32_t host_threads;      /* thread count the auto p rule assumes; 0 = all cores */
-    uint64_t flags;            /* CAPSSA_FLAG_* */
+    uint64_t flags;            /* no flags are defined: 0 */
     uint64_t reserved[5];
 } capssa_opts;
-
-/* capssa_opts.flags: sort through the 16-bit bucket front end (two global
- * passes on the top key bits, then one shared-memory sort per bucket)
- * instead of the full LSD sort; same output. */
-#define CAPSSA_FLAG_BUCKET_FRONT 1ull
 
 void capssa_opts_default(capssa_opts *o);
 
@@ -325,10 +320,9 @@ capssa_status capssa_seed_subarray_u8_u64(capssa_ctx *ctx, const uint8_t *text, 
  * where the synchronisation an allocation may imply is not acceptable, or a
  * caller without a capssa_ctx).
  *
- * Same result as capssa_merge_u8_u32 (sample_sort::merge,
- * src/sample_sort.rs:397-522), but it allocates nothing: every pointer is a
- * device pointer owned by the caller, and the merge-path scratch lives in a
- * fixed static device array of about 1.2 MiB that every GPU loading the
+ * Same result as capssa_merge_u8_u32, bit for bit, but it allocates
+ * nothing: every pointer is a device pointer owned by the caller, and the
+ * merge-path scratch lives in a fixed static device array of about 1.2 MiB that every GPU loading the
  * library holds until the process exits.
  *   - len_x + len_y must be at most 2^24 records; larger merges return
  *     CAPSSA_EINVAL.
@@ -338,9 +332,11 @@ capssa_status capssa_seed_subarray_u8_u64(capssa_ctx *ctx, const uint8_t *text, 
  *     ends on the device (checked like from_ends).  boundary is a
  *     capssa_boundary.
  *   - runs on `cuda_stream` (NULL = legacy default stream) of the current
- *     device and returns after the merge has finished.  The first call on a
- *     device looks up the scratch array's device address; make that first
- *     call before any stream capture.
+ *     device and returns after the merge has finished.  Every call looks up
+ *     the scratch array's device address in the current context; the first
+ *     call on a device also loads the library's device code, so make that
+ *     first call before any stream capture.  An error already pending on
+ *     the calling thread is reported as CAPSSA_ECUDA and left pending.
  *   - every call shares the one scratch array (it keeps the last call's
  *     contents); calls that overlap on the GPU, on any streams or host
  *     threads, race on it and must be serialised by the caller.

@@ -53,15 +53,13 @@ def limits_pair(n, ends=None, longer_first=False):
 
 
 def check_against_oracle(ctx, text, positions=None, ends=None, longer_first=False,
-                         max_ctx=orc.UNBOUNDED, index=np.uint32, partition=None,
-                         bucket_front=False):
+                         max_ctx=orc.UNBOUNDED, index=np.uint32, partition=None):
     n = len(text)
     lp, lo = limits_pair(n, ends, longer_first)
     if partition is None:
-        opts = capssa.Opts(max_context=max_ctx, bucket_front=bucket_front)
+        opts = capssa.Opts(max_context=max_ctx)
     else:
-        opts = capssa.ExtMemOpts(max_context=max_ctx, partition=partition,
-                                 bucket_front=bucket_front)
+        opts = capssa.ExtMemOpts(max_context=max_ctx, partition=partition)
     if positions is None:
         got = ctx.build_in_memory(text, lp, opts, index=index)
         want = orc.build_in_memory(text, None, lo, max_ctx, index=index)
@@ -440,9 +438,8 @@ def test_repeat_text_bit_exact(ctx):
     assert np.array_equal(ctx.build_in_memory(t), orc.build_in_memory(t))
 
 
-def _bucket_text(n, seed):
-    """Repeat DNA with one long run and one periodic stretch, so that some
-    16-bit key buckets exceed what one block sorts on chip."""
+def _runs_text(n, seed):
+    """Repeat DNA with one 60,000-symbol run and one periodic stretch."""
     from capssa import workloads
     t = workloads.dna_with_repeats(n, seed=seed).copy()
     t[1000:61000] = 0
@@ -451,31 +448,28 @@ def _bucket_text(n, seed):
 
 
 @pytest.mark.parametrize("dtype", [np.uint8, np.uint32])
-def test_bucket_front_end_plain(ctx, dtype):
-    """Texts of 2^22+ symbols take the bucket front end (two global passes on
-    the top 16 key bits, on-chip sort of each bucket, oversize buckets by the
-    global sort): bit-exact against the oracle."""
-    t = _bucket_text((1 << 22) + 12345, seed=11).astype(dtype)
-    got = ctx.build_in_memory(t, None, capssa.Opts(bucket_front=True))
+def test_large_text_runs_and_period(ctx, dtype):
+    """2^22+ symbols with a 60,000-symbol run and a 90,000-symbol periodic
+    stretch (large tied groups, deep rank doubling): bit-exact."""
+    t = _runs_text((1 << 22) + 12345, seed=11).astype(dtype)
+    got = ctx.build_in_memory(t)
     assert np.array_equal(got, orc.build_in_memory(t))
-    assert ctx.stats()["partitions"] == 65536  # the front end ran
 
 
-def test_bucket_front_end_star_segments(ctx):
-    t = _bucket_text((1 << 22) + 777, seed=12).astype(np.uint8)
+def test_large_text_star_segments(ctx):
+    t = _runs_text((1 << 22) + 777, seed=12).astype(np.uint8)
     rng = np.random.default_rng(5)
     ends = np.unique(np.concatenate([rng.integers(1, len(t), 300), [len(t)]])).tolist()
-    check_against_oracle(ctx, t, ends=ends, longer_first=True, bucket_front=True)
+    check_against_oracle(ctx, t, ends=ends, longer_first=True)
     assert ctx.stats()["partitions"] == 65536
 
 
-def test_bucket_front_end_text_alphabet(ctx):
-    """A 5-bit alphabet (key of 11 symbols + length field) through the front end."""
+def test_large_text_wide_alphabet(ctx):
+    """A 5-bit alphabet (key of 11 symbols + length field) with a long run."""
     rng = np.random.default_rng(13)
     t = rng.integers(0, 20, (1 << 22) + 99).astype(np.uint8)
     t[5000:25000] = 7
-    check_against_oracle(ctx, t, bucket_front=True)
-    assert ctx.stats()["partitions"] == 65536
+    check_against_oracle(ctx, t)
 
 
 def test_bounded_wait_times_out_and_context_survives(ctx):
