@@ -534,3 +534,20 @@ int or_brute_sa(const void *text, uint64_t n, int sym_bytes,
 }
 
 int or_max_threads(void) { return omp_get_max_threads(); }
+
+/* suffix_cmp_with (src/lcp.rs:184-201) of every adjacent pair of `sa`, in
+ * parallel: out[i] = sign of cmp(sa[i], sa[i + 1]) for i < m - 1.  The
+ * checker's tie classes (runs of 0) and order property (no +1) for outputs
+ * too large for a per-pair call from the test driver. */
+void or_adjacent_cmp(const void *text, int sym_bytes, const or_limits *lp, int idx_bytes,
+                     const void *sa, uint64_t m, uint64_t max_ctx, int8_t *out) {
+    if (m < 2) return;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)(m - 1); i++) {
+        const uint64_t p = idx_bytes == 4 ? ((const uint32_t *)sa)[i] : ((const uint64_t *)sa)[i];
+        const uint64_t q =
+            idx_bytes == 4 ? ((const uint32_t *)sa)[i + 1] : ((const uint64_t *)sa)[i + 1];
+        const int c = or_suffix_cmp(text, sym_bytes, lp, p, q, max_ctx);
+        out[i] = (int8_t)(c < 0 ? -1 : c > 0 ? 1 : 0);
+    }
+}

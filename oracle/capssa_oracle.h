@@ -120,6 +120,10 @@ int or_brute_sa(const void *text, uint64_t n, int sym_bytes,
 
 int or_max_threads(void);
 
+/* Sign of suffix_cmp_with for every adjacent pair of sa (m - 1 entries). */
+void or_adjacent_cmp(const void *text, int sym_bytes, const or_limits *lp, int idx_bytes,
+                     const void *sa, uint64_t m, uint64_t max_ctx, int8_t *out);
+
 /* Learned CDF model (no reference counterpart; cdf_oracle.c): 2 inputs from
  * the 64-bit packed prefix, OR_CDF_HIDDEN ReLU units, 1 output. */
 #define OR_CDF_HIDDEN 64

@@ -81,6 +81,7 @@ def lib():
                                        C.c_uint32, C.c_uint32, vp, vp, u64]
         L.or_brute_sa.argtypes = [vp, u64, i, C.POINTER(_Limits), u64, vp, u64, vp]
         L.or_max_threads.restype = i
+        L.or_adjacent_cmp.argtypes = [vp, i, C.POINTER(_Limits), i, vp, u64, u64, vp]
         L.or_cdf_forward.argtypes = [vp, u64]
         L.or_cdf_forward.restype = C.c_double
         L.or_cdf_loss_grad.argtypes = [vp, vp, vp, u64, vp]
@@ -253,6 +254,42 @@ def brute_sa(text, positions=None, limits=None, max_ctx=UNBOUNDED):
     if rc != 0:
         raise ValueError("oracle brute rc=%d" % rc)
     return out
+
+
+def adjacent_cmp(text, sa, limits=None, max_ctx=UNBOUNDED):
+    """Sign (-1, 0, 1) of suffix_cmp_with for every adjacent pair of sa."""
+    t = _text(text)
+    lp = limits or Limits(len(t))
+    a = np.ascontiguousarray(sa)
+    if a.dtype not in (np.uint32, np.uint64):
+        a = a.astype(np.uint64)
+    out = np.zeros(max(len(a) - 1, 0), dtype=np.int8)
+    lib().or_adjacent_cmp(_ptr(t), t.itemsize, lp.ref, a.itemsize, _ptr(a), len(a),
+                          int(max_ctx), _ptr(out))
+    return out
+
+
+def canonical_ties(sa, cmp):
+    """sa with every tie class (a run of adjacent pairs comparing equal)
+    sorted by position: the reference leaves the order inside a class
+    unpinned under SegmentedText's default boundary order.  Only the members
+    of classes of two or more are reordered."""
+    a = np.array(sa, copy=True)
+    tie = np.asarray(cmp) == 0
+    if len(a) < 2 or not tie.any():
+        return a
+    mem = np.zeros(len(a), dtype=bool)
+    at = np.nonzero(tie)[0]
+    mem[at] = True
+    mem[at + 1] = True
+    sel = np.nonzero(mem)[0]
+    start = np.ones(len(sel), dtype=bool)  # a member opens a class unless tied to its left
+    inner = sel > 0
+    start[inner] = ~tie[sel[inner] - 1]
+    run = np.cumsum(start)
+    vals = a[sel]
+    a[sel] = vals[np.lexsort((vals, run))]
+    return a
 
 
 def max_threads():

@@ -255,3 +255,27 @@ def test_cdf_oracle_features():
     assert f.tolist() == [-1.0, -1.0]
     f = orc.cdf_features(1 << 63)
     assert f.tolist() == [0.0, -1.0]
+
+
+def test_adjacent_cmp_and_tie_canonicalisation():
+    """The checker's vectorised tie handling (used on outputs too large for a
+    per-pair loop) agrees with per-pair suffix_cmp_with calls and with
+    sorting each tie class by position."""
+    rng = np.random.default_rng(21)
+    for _ in range(100):
+        n = int(rng.integers(2, 400))
+        t = rng.integers(0, 2, n).astype(np.uint8)
+        ends = np.unique(np.concatenate([rng.integers(1, n, max(1, n // 4)), [n]]))
+        lo = orc.Limits(n, ends.astype(np.uint64))
+        sa = orc.build_in_memory(t, None, lo)
+        c = orc.adjacent_cmp(t, sa, lo)
+        pair = [orc.suffix_cmp(t, int(sa[i]), int(sa[i + 1]), lo) for i in range(n - 1)]
+        assert c.tolist() == [(x > 0) - (x < 0) for x in pair]
+        out, i = [], 0
+        while i < n:
+            j = i + 1
+            while j < n and c[j - 1] == 0:
+                j += 1
+            out.extend(sorted(int(x) for x in sa[i:j]))
+            i = j
+        assert orc.canonical_ties(sa, c).tolist() == out
