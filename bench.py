@@ -279,22 +279,30 @@ def run_forms(ctx, t_dev, n):
     from capssa import workloads
 
     out = {}
-    # ---- sample sort: splitter vs learned partition (plan = SA + partition)
+    # ---- sample sort: splitter vs learned partition (plan = SA + partition),
+    # bucketed before the sort; and the reference's sampling rule, whose
+    # chunk order comes from a full sort first
     ss = {}
-    for name, part in (("splitters", capssa.Partition.SPLITTERS),
-                       ("learned", capssa.Partition.LEARNED)):
-        opts = capssa.ExtMemOpts(subproblem_count=4096, partition=part)
+    for name, part, smp in (("splitters", capssa.Partition.SPLITTERS, capssa.Sampling.AUTO),
+                            ("learned", capssa.Partition.LEARNED, capssa.Sampling.AUTO),
+                            ("reference_rule_sort_first", capssa.Partition.SPLITTERS,
+                             capssa.Sampling.REFERENCE)):
+        opts = capssa.ExtMemOpts(subproblem_count=4096, partition=part, sampling=smp)
         ctx.sample_sort_plan(t_dev, opts)  # warm
         ms = _timed(lambda: ctx.sample_sort_plan(t_dev, opts), 3)
         k, pv, sz = ctx.sample_sort_plan(t_dev, opts)
         st = ctx.stats()
         ss[name] = {"value": n / (ms / 1e3) / 1e6, "unit": "Msuffixes/s", "ms": ms,
                     "partition_ms": st["partition_ms"],
+                    "partition_gbs": (n * 8.25 / (st["partition_ms"] / 1e3) / 1e9
+                                      if st["partition_ms"] > 0 else None),
                     "probes_per_suffix": st["partition_probes"] / n,
                     "mispredicted_rate": st["mispredicted"] / n,
                     "imbalance_max_over_mean": float(sz.max()) / (n / k),
                     "train_ms": st["train_ms"], "train_samples": st["train_samples"],
                     "model_loss": st["model_loss"], "p": k,
+                    "keys_ms": st["keys_ms"], "sort_ms": st["sort_ms"],
+                    "refine_ms": st["refine_ms"], "sort_passes": st["sort_passes"],
                     "sizes_sha": hash(sz.tobytes()) & 0xFFFFFFFF}
     ss["same_partition"] = ss["splitters"]["sizes_sha"] == ss["learned"]["sizes_sha"]
     out["sample_sort_p4096"] = ss

@@ -82,6 +82,13 @@ class Partition(enum.IntEnum):
     LEARNED = 2
 
 
+class Sampling(enum.IntEnum):
+    """capssa_sampling: where the sample sort's splitter sample comes from."""
+    AUTO = 0
+    REFERENCE = 1
+    PARTITION_FIRST = 2
+
+
 class _Limits(C.Structure):
     _fields_ = [("kind", C.c_int32), ("boundary", C.c_int32),
                 ("ends", C.c_void_p), ("n_ends", C.c_uint64)]
@@ -90,7 +97,8 @@ class _Limits(C.Structure):
 class _Opts(C.Structure):
     _fields_ = [("max_context", C.c_uint64), ("subproblem_count", C.c_uint64),
                 ("partition", C.c_int32), ("host_threads", C.c_int32),
-                ("flags", C.c_uint64), ("reserved", C.c_uint64 * 5)]
+                ("flags", C.c_uint64), ("sampling", C.c_int32), ("reserved32", C.c_int32),
+                ("reserved", C.c_uint64 * 4)]
 
 
 
@@ -270,6 +278,7 @@ class ExtMemOpts:
     subproblem_count: int = 0
     partition: Partition = Partition.AUTO
     host_threads: int = 0
+    sampling: Sampling = Sampling.AUTO
 
 
 def _copts(o) -> _Opts:
@@ -281,6 +290,7 @@ def _copts(o) -> _Opts:
         c.partition = int(getattr(o, "partition", 0))
         c.host_threads = int(getattr(o, "host_threads", 0))
         c.flags = 0
+        c.sampling = int(getattr(o, "sampling", 0))
     return c
 
 

@@ -151,6 +151,38 @@ KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits, int top_bits, uint
     return g;
 }
 
+KeyGeom pf_geom(int b, uint64_t n, bool plain, double hbits, int bucket_bits) {
+    KeyGeom g{};
+    g.b = b < 1 ? 1 : b;
+    int logn = 0;
+    while (logn < 64 && (n >> logn) > 1) logn++;
+    const double h = hbits > 0.25 ? (hbits < g.b ? hbits : (double)g.b) : 0.25;
+    // the same target as key_geom (log2(n) / H + 3 symbols), less the
+    // symbols of information the bucket index already carries
+    const int ktot = (int)std::ceil((double)logn / h - 1e-9) + 3;
+    const int kb = (int)std::floor((double)bucket_bits / h + 1e-9);
+    int k = std::max(2, ktot - kb);
+    int vbits = 1;
+    while (vbits < 32 && (1ull << vbits) < n) vbits++;
+    auto lb = [&](int kk) {
+        if (plain) return 1;
+        int x = 0;
+        while ((1 << x) <= kk) x++;
+        return x;
+    };
+    auto bits = [&](int kk) { return bucket_bits + kk * g.b + lb(kk); };
+    while (k > 1 && (bits(k) + vbits > 64 || k * g.b > 63)) k--;
+    if (bits(k) + vbits > 64 || k * g.b > 63) return g;  // g.k == 0
+    const int passes = (bits(k) + 7) / 8;
+    while ((k + 1) * g.b <= 63 && bits(k + 1) <= 8 * passes && bits(k + 1) + vbits <= 64) k++;
+    g.k = k;
+    g.lbits = lb(k);
+    g.flag_len = plain ? 1 : 0;
+    g.total = k * g.b + g.lbits;
+    g.vbits = vbits;
+    return g;
+}
+
 namespace {
 
 bool is_device_ptr(const void *p) {
@@ -368,6 +400,7 @@ capssa_status build_common(Ctx &c, const ST *text, uint64_t n, const void *posit
         a.part_mode = part->mode;
         a.part_pivots = part->pivots;
         a.part_sizes = part->sizes;
+        a.part_first = !opts || opts->sampling != CAPSSA_SAMPLING_REFERENCE ? 1 : 0;
     }
     if (positions && m == 0) return CAPSSA_OK;
     s = engine_build(c, a);

@@ -56,6 +56,7 @@ struct EngineArgs {
     int part_mode;           // CAPSSA_PARTITION_SPLITTERS or CAPSSA_PARTITION_LEARNED
     uint64_t *part_pivots;   // host, part_p - 1 entries (out) or nullptr
     uint64_t *part_sizes;    // host, part_p entries (out) or nullptr
+    int part_first;          // 1: partition before the sort (CAPSSA_SAMPLING_PARTITION_FIRST)
 };
 
 // Runs the whole sort; all buffers are device buffers.
@@ -95,5 +96,11 @@ struct KeyGeom {
 // a ShorterFirst plain text may drop the early-end flag (see KeyGeom).
 KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits, int top_bits = 0,
                  uint64_t n_k = 0, bool allow_flagless = false);
+
+// Key geometry of a partition-first sort: a bucket index of bucket_bits
+// above a window of k symbols taken after the bucket's common prefix, a
+// flag (plain) or length field, and the global position below (k = 0: no
+// geometry packs the position with at least one symbol).
+KeyGeom pf_geom(int b, uint64_t n, bool plain, double hbits, int bucket_bits);
 
 }  // namespace capssa

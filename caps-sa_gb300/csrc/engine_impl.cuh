@@ -1775,6 +1775,254 @@ __global__ void partition_check_kernel(const uint32_t *__restrict__ bucket_of,
     }
 }
 
+// ---------------------------------------------------------------- partition-first sample sort
+//
+// build_in_memory_sample_sort with the partition ahead of the sort: the
+// splitter sample is sorted on its own, every suffix finds its bucket by
+// comparing itself with the pivots (phase 3, src/ext_mem.rs:1361-1428 and
+// upper_bound_by_pivot :1705-1734) inside the kernel that builds its sort
+// record, and the bucket becomes the top field of that record.  Every
+// member of bucket b (pivot[b-1] < s <= pivot[b]) starts with the common
+// prefix of its two pivots (ell[b] symbols), so the record's key window
+// starts there: the bucket carries the prefix, the window the symbols after
+// it.  The one radix sort of (bucket, window, field, position) then leaves
+// every bucket contiguous and in suffix order up to the window, and the
+// usual refinement finishes each bucket (phase 4, src/ext_mem.rs:1745-2108).
+
+constexpr uint64_t kPfCmpCap = 1ull << 16;  // symbols an exact pivot comparison may read
+constexpr uint32_t kPfTieMax = 64;          // largest run of equal sample keys sorted exactly
+constexpr uint32_t kPfEllCap = 1u << 15;    // window offsets are capped (any prefix length works)
+
+// Comparison key of a suffix on its first spw symbols: the packed window,
+// truncated at the limit and padded low (ShorterFirst) or high
+// (LongerFirst).  Strictly smaller keys mean strictly smaller suffixes under
+// suffix_cmp_with (src/lcp.rs:184-201); equal keys need an exact compare.
+__device__ __forceinline__ uint64_t prefix_key(const Packed &P, uint64_t p, uint64_t lim, int lf) {
+    uint64_t w = window_at(P, p);
+    if (lim < (uint64_t)P.spw) {
+        const uint32_t keep = (uint32_t)lim * (uint32_t)P.b;  // < 64
+        const uint64_t low = ~0ull >> keep;                    // the bits after the kept symbols
+        w = lf ? (w | low) : (w & ~low);
+    }
+    return w;
+}
+
+// Sample of the input order: ns evenly spaced midpoints of the text, each
+// with its comparison key.
+__global__ void pf_sample_kernel(Packed P, DevLimits L, uint64_t n, uint32_t ns, int lf,
+                                 uint64_t *__restrict__ keys, uint32_t *__restrict__ pos) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
+        const uint64_t p = ((2 * (uint64_t)i + 1) * n) / (2 * (uint64_t)ns);
+        keys[i] = prefix_key(P, p, dev_lim_at(L, p), lf);
+        pos[i] = (uint32_t)p;
+    }
+}
+
+// Runs of equal keys in the key-sorted sample, each put in exact suffix
+// order by one thread (insertion sort, exact compares); a run longer than
+// kPfTieMax or a compare deeper than kPfCmpCap sets *fallback.
+__global__ void pf_sample_ties_kernel(const uint64_t *__restrict__ keys, uint32_t *__restrict__ pos,
+                                      uint32_t ns, Packed P, DevLimits L, int lf,
+                                      int *__restrict__ fallback) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i + 1 < ns;
+         i += gridDim.x * blockDim.x) {
+        const uint64_t k = keys[i];
+        if ((i > 0 && keys[i - 1] == k) || keys[i + 1] != k) continue;  // not the head of a run
+        uint32_t j = i + 1;
+        while (j < ns && keys[j] == k && j - i <= kPfTieMax) j++;
+        if (j - i > kPfTieMax) {
+            atomicExch(fallback, 1);
+            continue;
+        }
+        for (uint32_t a = i + 1; a < j; a++) {  // insertion sort, stable
+            const uint32_t x = pos[a];
+            const uint64_t lx = dev_lim_at(L, x);
+            uint32_t b = a;
+            while (b > i) {
+                const uint32_t y = pos[b - 1];
+                const int c = direct_cmp(P, y, dev_lim_at(L, y), x, lx, 0, kPfCmpCap, lf);
+                if (c == 2) atomicExch(fallback, 1);
+                if (c <= 0 || c == 2) break;
+                pos[b] = y;
+                b--;
+            }
+            pos[b] = x;
+        }
+    }
+}
+
+// Pivots samples[(j + 1) * ns / p] (phase 2, src/ext_mem.rs:1309-1342) with
+// their keys and limits.
+__global__ void pf_pivot_kernel(const uint32_t *__restrict__ spos, uint32_t ns, uint32_t p,
+                                Packed P, DevLimits L, int lf, uint64_t *__restrict__ pkey,
+                                uint32_t *__restrict__ ppos, uint64_t *__restrict__ plim) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j + 1 < p;
+         j += gridDim.x * blockDim.x) {
+        const uint32_t q = spos[(uint64_t)(j + 1) * ns / p];
+        const uint64_t lim = dev_lim_at(L, q);
+        ppos[j] = q;
+        plim[j] = lim;
+        pkey[j] = prefix_key(P, q, lim, lf);
+    }
+}
+
+// Key-window offset of every bucket: the common prefix of its two pivots
+// (0 for the first and last buckets, which have one pivot), capped.
+__global__ void pf_ell_kernel(const uint32_t *__restrict__ ppos, const uint64_t *__restrict__ plim,
+                              uint32_t p, Packed P, uint32_t *__restrict__ ell) {
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < p; b += gridDim.x * blockDim.x) {
+        uint64_t t = 0;
+        if (b > 0 && b + 1 < p) {
+            const uint64_t x = ppos[b - 1], y = ppos[b];
+            uint64_t lim = plim[b - 1] < plim[b] ? plim[b - 1] : plim[b];
+            if (lim > kPfEllCap) lim = kPfEllCap;
+            while (t < lim) {
+                const uint64_t d = window_at(P, x + t) ^ window_at(P, y + t);
+                if (d) {
+                    t += (uint64_t)__clzll((long long)d) / (uint64_t)P.b;
+                    break;
+                }
+                t += (uint64_t)P.spw;
+            }
+            if (t > lim) t = lim;
+        }
+        ell[b] = (uint32_t)t;
+    }
+}
+
+// Sort record of every text position with its bucket (the fused partition):
+// bucket b = the number of pivots that compare less than the suffix, found
+// by binary search over the pivot keys in shared memory (SPLITTERS) or
+// predicted by the learned CDF model from the suffix's packed prefix and
+// walked until both neighbouring pivots agree (LEARNED); key ties with a
+// pivot are settled by an exact comparison.  The record is
+//   bucket | window of k symbols from ell[b] | length field | position,
+// with the digit histograms of every radix pass and the bucket sizes
+// accumulated on the way (shared memory, then one global add per block).
+// kPlain: PlainText limits (n - p).
+template <bool kPlain, bool LEARNED>
+__global__ void __launch_bounds__(kKeyThreads)
+    pf_key_kernel(Packed P, uint64_t n, DevLimits L, int k, int lbits, int flag_len, int vbits,
+                  int lf, int n_passes, int bucket_shift, const uint64_t *__restrict__ pkey,
+                  const uint32_t *__restrict__ ppos, const uint64_t *__restrict__ plim,
+                  const uint32_t *__restrict__ ell, uint32_t p, const __nv_bfloat16 *__restrict__ w,
+                  uint64_t *__restrict__ keys, uint32_t *__restrict__ counts,
+                  unsigned long long *__restrict__ sizes, unsigned long long *__restrict__ stats,
+                  int *__restrict__ fallback) {
+    extern __shared__ __align__(16) unsigned char pfs[];
+    const uint32_t n_piv = p - 1;
+    uint64_t *sk = reinterpret_cast<uint64_t *>(pfs);    // n_piv pivot keys
+    uint32_t *sell = reinterpret_cast<uint32_t *>(sk + n_piv);  // p offsets
+    uint32_t *bh = sell + p;                              // p bucket counts
+    uint32_t *hist = bh + p;                              // 8 * 256 digit counts
+    __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(hist + 8 * 256);
+    for (uint32_t j = threadIdx.x; j < n_piv; j += kKeyThreads) sk[j] = pkey[j];
+    for (uint32_t j = threadIdx.x; j < p; j += kKeyThreads) {
+        sell[j] = ell[j];
+        bh[j] = 0;
+    }
+    for (int i = threadIdx.x; i < 8 * 256; i += kKeyThreads) hist[i] = 0;
+    if (LEARNED)
+        for (int j = threadIdx.x; j < cdf::kParams; j += kKeyThreads) sw[j] = w[j];
+    __syncthreads();
+    const int b = P.b;
+    const int kbits = k * b;  // 1..63
+    unsigned long long probes = 0, mis = 0;
+    bool deep = false;
+    // consecutive threads take consecutive positions (coalesced record stores)
+    for (uint64_t q = (uint64_t)blockIdx.x * kKeyThreads + threadIdx.x; q < n;
+         q += (uint64_t)gridDim.x * kKeyThreads) {
+        const uint64_t lim = kPlain ? n - q : dev_lim_at(L, q);
+        const uint64_t K = prefix_key(P, q, lim, lf);
+        // suffix q > pivot j ?
+        auto greater = [&](uint32_t j) -> bool {
+            probes++;
+            const uint64_t pk = sk[j];
+            if (K != pk) return K > pk;
+            const int c =
+                direct_cmp(P, q, lim, __ldg(ppos + j), __ldg(plim + j), 0, kPfCmpCap, lf);
+            if (c == 2) deep = true;
+            return c == 1;
+        };
+        uint32_t bk;
+        if (LEARNED) {
+            const float y = cdf::infer_bf16(sw, K);
+            float g = floorf(y * (float)p);
+            g = g < 0.0f ? 0.0f : (g > (float)n_piv ? (float)n_piv : g);
+            bk = (uint32_t)g;
+            const uint32_t guess = bk;
+            while (bk > 0 && !greater(bk - 1)) bk--;
+            if (bk == guess)
+                while (bk < n_piv && greater(bk)) bk++;
+            mis += bk != guess ? 1u : 0u;
+        } else {
+            uint32_t lo = 0, hi = n_piv;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (greater(mid))
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            bk = lo;
+        }
+        atomicAdd(&bh[bk], 1u);
+        // window of k symbols after the bucket's common prefix
+        const uint64_t off = sell[bk];
+        const uint64_t rest = lim > off ? lim - off : 0;
+        const uint64_t bit = (q + off) * (uint64_t)b;
+        const uint64_t wi = bit >> 6;
+        const uint32_t sh = (uint32_t)(bit & 63);
+        const uint64_t w0 = __ldg(P.w + wi), w1 = __ldg(P.w + wi + 1);
+        uint64_t content = ((w0 << sh) | ((w1 >> 1) >> (63 - sh))) >> (64 - kbits);
+        int take = k;
+        if (rest < (uint64_t)k) {
+            take = (int)rest;
+            const uint64_t lowmask = (1ull << ((k - take) * b)) - 1;
+            content = lf ? (content | lowmask) : (content & ~lowmask);
+        }
+        const uint64_t field = flag_len ? (uint64_t)((take == k) != (lf != 0))
+                                        : (uint64_t)(lf ? k - take : take);
+        uint64_t rec =
+            (lbits ? (content << lbits) | field : content) | ((uint64_t)bk << bucket_shift);
+        const uint32_t rlo = (uint32_t)rec, rhi = (uint32_t)(rec >> 32);
+#pragma unroll
+        for (int ps = 0; ps < 8; ps++)
+            if (ps < n_passes)
+                atomicAdd(&hist[ps * 256 + (((ps < 4 ? rlo : rhi) >> (8 * (ps & 3))) & 255u)], 1u);
+        keys[q] = (rec << vbits) | q;
+    }
+    if (deep) atomicExch(fallback, 1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        probes += __shfl_xor_sync(0xffffffffu, probes, o);
+        mis += __shfl_xor_sync(0xffffffffu, mis, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&stats[0], probes);
+        atomicAdd(&stats[1], mis);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n_passes * 256; i += kKeyThreads)
+        if (hist[i]) atomicAdd(&counts[i], hist[i]);
+    for (uint32_t j = threadIdx.x; j < p; j += kKeyThreads)
+        if (bh[j]) atomicAdd(&sizes[j], (unsigned long long)bh[j]);
+}
+
+// Training set of the learned model from the exactly sorted sample: every
+// stride-th sample's comparison key and its rank fraction.
+__global__ void pf_train_set_kernel(const uint32_t *__restrict__ spos,
+                                    const uint64_t *__restrict__ skeys_unused, uint32_t ns,
+                                    uint32_t stride, uint32_t tn, Packed P, DevLimits L, int lf,
+                                    uint64_t *__restrict__ x, float *__restrict__ t) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < tn; j += gridDim.x * blockDim.x) {
+        const uint32_t q = j * stride;
+        const uint32_t s = spos[q];
+        x[j] = prefix_key(P, s, dev_lim_at(L, s), lf);
+        t[j] = ((float)q + 0.5f) / (float)ns;
+    }
+}
+
 }  // namespace eng
 
 // ---------------------------------------------------------------- host
@@ -1831,10 +2079,154 @@ inline int bits_for(uint64_t v) {  // bits to represent 0..v
     return b == 0 ? 1 : b;
 }
 
-// Steps 1-4 of engine.cuh over every text position under the unbounded
-// comparator; *sa_out receives the device SA (n entries).
+// Request and outcome of a partition-first core_sort (the sample sort's
+// buckets computed before the sort and leading its records).
+struct PfRun {
+    uint32_t p = 0;
+    bool learned = false;
+    bool fell_back = false;                  // out: a comparison ran too deep; nothing sorted
+    const uint32_t *d_pivots = nullptr;      // out: device, p - 1 pivot positions
+    const unsigned long long *d_sizes = nullptr;  // out: device, p bucket sizes + 2 stats
+};
+
+// The partition-first front of core_sort: the splitter sample (the same
+// count as the reference's sampler, as evenly spaced midpoints of the text)
+// sorted exactly, its pivots and their common prefixes, the learned model
+// (LEARNED), then the fused partition + record kernel over every position.
+// A sample run or pivot comparison deeper than kPfCmpCap symbols sets
+// pf->fell_back (one synchronisation after the fused kernel).
 template <typename S>
-capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Packed *pk_out) {
+capssa_status pf_keys(Ctx &c, const EngineArgs &a, const eng::Packed &P, const KeyGeom &geo,
+                      int bucket_bits, int key_passes, uint64_t *keys, uint32_t *counts,
+                      PfRun *pf) {
+    using namespace eng;
+    const uint64_t n = a.n;
+    const int lf = a.lim.longer_first;
+    const uint32_t p = pf->p;
+    // sample count of the reference's sampler (src/ext_mem.rs:1282-1287)
+    double ln_n = std::log((double)n);
+    if (ln_n < 1.0) ln_n = 1.0;
+    uint64_t total = (uint64_t)p * (uint64_t)std::ceil(4.0 * ln_n);
+    total = std::min<uint64_t>(std::max<uint64_t>(total, p), n);
+    const uint32_t per = (uint32_t)((total + p - 1) / p);
+    const uint32_t ns = (uint32_t)std::min<uint64_t>((uint64_t)per * p, n);
+    const size_t nsb = (size_t)ns + 64;
+    const size_t bytes = nsb * 8 * 2 + nsb * 4 * 2 + (size_t)p * (8 + 4 + 8 + 4) +
+                         ((size_t)p + 4) * 8 + (size_t)65536 * 12 + cdf::kParams * 6 + 16 * 256;
+    char *w = (char *)ws_get(c, WS_PART, bytes);
+    if (!w) return set_err(c, CAPSSA_ENOMEM, "partition-first workspace");
+    auto carve = [&](size_t sz) {
+        char *r = w;
+        w += (sz + 255) & ~(size_t)255;
+        return r;
+    };
+    uint64_t *sk_a = (uint64_t *)carve(nsb * 8), *sk_b = (uint64_t *)carve(nsb * 8);
+    uint32_t *sp_a = (uint32_t *)carve(nsb * 4), *sp_b = (uint32_t *)carve(nsb * 4);
+    uint64_t *pkey = (uint64_t *)carve((size_t)p * 8);
+    uint32_t *ppos = (uint32_t *)carve((size_t)p * 4);
+    uint64_t *plim = (uint64_t *)carve((size_t)p * 8);
+    uint32_t *ell = (uint32_t *)carve((size_t)p * 4);
+    unsigned long long *sizes = (unsigned long long *)carve(((size_t)p + 4) * 8);
+    uint64_t *tx = (uint64_t *)carve((size_t)65536 * 8);
+    float *tt = (float *)carve((size_t)65536 * 4);
+    float *params = (float *)carve(cdf::kParams * 4);
+    __nv_bfloat16 *wbf = (__nv_bfloat16 *)carve(cdf::kParams * 2);
+    int *fb = c.d_flags + 1;
+    CAPSSA_CUDA(c, cudaMemsetAsync(fb, 0, 4, c.stream));
+    // 1. sample, sorted by key, then exactly
+    pf_sample_kernel<<<grid_for(ns, 256), 256, 0, c.stream>>>(P, a.lim, n, ns, lf, sk_a, sp_a);
+    CAPSSA_LAUNCHED(c);
+    bool in_b = false;
+    const int kb = P.spw * P.b;
+    capssa_status s = radix::sort_pairs(c, sk_a, sp_a, sk_b, sp_b, ns, 64 - kb, 64, false, 0, &in_b);
+    if (s != CAPSSA_OK) return s;
+    const uint64_t *skeys = in_b ? sk_b : sk_a;
+    uint32_t *spos = in_b ? sp_b : sp_a;
+    pf_sample_ties_kernel<<<grid_for(ns, 256), 256, 0, c.stream>>>(skeys, spos, ns, P, a.lim, lf,
+                                                                   fb);
+    CAPSSA_LAUNCHED(c);
+    // 2. pivots and the buckets' common prefixes
+    pf_pivot_kernel<<<grid_for(p, 256), 256, 0, c.stream>>>(spos, ns, p, P, a.lim, lf, pkey,
+                                                            ppos, plim);
+    CAPSSA_LAUNCHED(c);
+    pf_ell_kernel<<<grid_for(p, 256), 256, 0, c.stream>>>(ppos, plim, p, P, ell);
+    CAPSSA_LAUNCHED(c);
+    // 3. the learned CDF model on the sorted sample
+    if (pf->learned) {
+        const uint32_t tn = std::min<uint32_t>(ns, 65536);
+        const uint32_t stride = (ns + tn - 1) / tn;
+        const uint32_t tn_eff = (ns + stride - 1) / stride;
+        pf_train_set_kernel<<<grid_for(tn_eff, 256), 256, 0, c.stream>>>(
+            spos, skeys, ns, stride, tn_eff, P, a.lim, lf, tx, tt);
+        CAPSSA_LAUNCHED(c);
+        cudaEvent_t t0, t1;
+        cudaEventCreate(&t0);
+        cudaEventCreate(&t1);
+        cudaEventRecord(t0, c.stream);
+        float loss = 0.0f;
+        s = cdf::train(c, tx, tt, tn_eff, 300, params, wbf, &loss);
+        cudaEventRecord(t1, c.stream);
+        cudaEventSynchronize(t1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, t0, t1);
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+        if (s != CAPSSA_OK) return s;
+        c.stats.train_ms = ms;
+        c.stats.model_loss = loss;
+        c.stats.train_samples = tn_eff;
+    }
+    // 4. the fused partition + record kernel (the sample's sort used the
+    // histogram buffer: clear it for the records' digit counts)
+    CAPSSA_CUDA(c, cudaMemsetAsync(counts, 0, radix::kMaxPasses * 256 * 4, c.stream));
+    CAPSSA_CUDA(c, cudaMemsetAsync(sizes, 0, ((size_t)p + 4) * 8, c.stream));
+    const size_t smem = (size_t)(p - 1) * 8 + (size_t)p * 8 + 8 * 256 * 4 + cdf::kParams * 2 + 16;
+    const bool plain = !a.lim.segmented;
+    const unsigned grid = std::min<unsigned>(grid_for(n, kKeyThreads), (unsigned)c.sm_count * 8);
+    cudaEvent_t q0, q1;
+    cudaEventCreate(&q0);
+    cudaEventCreate(&q1);
+#define CAPSSA_PF_LAUNCH(PL, LE)                                                                  \
+    do {                                                                                          \
+        cudaFuncSetAttribute(pf_key_kernel<PL, LE>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                             (int)smem);                                                          \
+        pf_key_kernel<PL, LE><<<grid, kKeyThreads, smem, c.stream>>>(                             \
+            P, n, a.lim, geo.k, geo.lbits, geo.flag_len, geo.vbits, lf, key_passes, geo.total,    \
+            pkey, ppos, plim, ell, p, wbf, keys, counts, sizes, sizes + p, fb);                    \
+    } while (0)
+    cudaEventRecord(q0, c.stream);
+    if (plain && pf->learned)
+        CAPSSA_PF_LAUNCH(true, true);
+    else if (plain)
+        CAPSSA_PF_LAUNCH(true, false);
+    else if (pf->learned)
+        CAPSSA_PF_LAUNCH(false, true);
+    else
+        CAPSSA_PF_LAUNCH(false, false);
+#undef CAPSSA_PF_LAUNCH
+    CAPSSA_LAUNCHED(c);
+    cudaEventRecord(q1, c.stream);
+    int *h_fb = (int *)c.h_scratch;
+    CAPSSA_CUDA(c, cudaMemcpyAsync(h_fb, fb, 4, cudaMemcpyDeviceToHost, c.stream));
+    CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+    float pms = 0.0f;
+    cudaEventElapsedTime(&pms, q0, q1);
+    cudaEventDestroy(q0);
+    cudaEventDestroy(q1);
+    c.stats.partition_ms = pms;
+    pf->fell_back = *h_fb != 0;
+    pf->d_pivots = ppos;
+    pf->d_sizes = sizes;
+    (void)bucket_bits;
+    return CAPSSA_OK;
+}
+
+// Steps 1-4 of engine.cuh over every text position under the unbounded
+// comparator; *sa_out receives the device SA (n entries).  With `pf`, the
+// records lead with the sample sort's bucket (partition first).
+template <typename S>
+capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Packed *pk_out,
+                        PfRun *pf = nullptr) {
     using namespace eng;
     const uint64_t n = a.n;
     const int lf = a.lim.longer_first;
@@ -1929,9 +2321,19 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     c.seg_major_done = a.seg_major && (seg_bits > 0 || a.lim.n_ends <= 1);
     // a ShorterFirst plain text may drop the early-end flag when that saves a
     // radix pass
-    const bool allow_flagless = !a.lim.segmented && !lf && n <= 0xFFFFFFFEull;
-    const KeyGeom geo = key_geom(b, n, !a.lim.segmented, hbits, seg_bits,
-                                 seg_bits ? a.seg_max_len : 0, allow_flagless);
+    const bool allow_flagless = !a.lim.segmented && !lf && n <= 0xFFFFFFFEull && !pf;
+    KeyGeom geo;
+    if (pf) {  // the bucket index leads the record
+        seg_bits = bits_for(pf->p - 1);
+        geo = pf_geom(b, n, !a.lim.segmented, hbits, seg_bits);
+        if (geo.k == 0) {
+            pf->fell_back = true;
+            return CAPSSA_OK;
+        }
+    } else {
+        geo = key_geom(b, n, !a.lim.segmented, hbits, seg_bits, seg_bits ? a.seg_max_len : 0,
+                       allow_flagless);
+    }
     // records the radix sort orders: every suffix, or the full ones only
     const uint64_t n_short = geo.flagless ? (uint64_t)geo.k - 1 : 0;
     const uint64_t n_rec = n - n_short;
@@ -1976,15 +2378,20 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     P.spw = 64 / geo.b;
     P.mask = P.spw * P.b >= 64 ? ~0ull : (~0ull << (64 - P.spw * P.b));
     const unsigned kgrid = std::min<unsigned>(grid_for(n_rec, kKeyTile), c.sm_count * 8);
-    if (!a.lim.segmented && !seg_bits)
+    if (pf) {
+        capssa_status s0 = pf_keys<S>(c, a, P, geo, seg_bits, key_passes, keys_a, counts, pf);
+        if (s0 != CAPSSA_OK || pf->fell_back) return s0;
+    } else if (!a.lim.segmented && !seg_bits) {
         key_kernel<true><<<kgrid, kKeyThreads, 0, c.stream>>>(
             P, n, n_rec, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf, key_passes, 0, 0,
             keys_a, counts);
-    else
+        CAPSSA_LAUNCHED(c);
+    } else {
         key_kernel<false><<<kgrid, kKeyThreads, 0, c.stream>>>(
             P, n, n_rec, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf, key_passes,
             seg_bits ? geo.total : 0, local_pos, keys_a, counts);
-    CAPSSA_LAUNCHED(c);
+        CAPSSA_LAUNCHED(c);
+    }
     cudaEventRecord(c.pev[1], c.stream);
     bool in_b = false;
     int passes = 0;
@@ -2461,6 +2868,30 @@ capssa_status partition_phase(Ctx &c, const EngineArgs &a, const eng::Packed &P,
     return CAPSSA_OK;
 }
 
+// Plan outputs and statistics of a partition-first sort: pivots, bucket
+// sizes, comparisons per suffix and mispredictions (learned model).
+inline capssa_status pf_report(Ctx &c, const EngineArgs &a, const PfRun &pf) {
+    const uint32_t p = pf.p;
+    std::vector<unsigned long long> h_sizes((size_t)p + 2);
+    std::vector<uint32_t> h_piv(p);
+    CAPSSA_CUDA(c, cudaMemcpyAsync(h_sizes.data(), pf.d_sizes, ((size_t)p + 2) * 8,
+                                   cudaMemcpyDeviceToHost, c.stream));
+    CAPSSA_CUDA(c, cudaMemcpyAsync(h_piv.data(), pf.d_pivots, (size_t)(p - 1) * 4,
+                                   cudaMemcpyDeviceToHost, c.stream));
+    CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+    c.stats.partitions = p;
+    c.stats.partition_probes = h_sizes[p];
+    c.stats.mispredicted = h_sizes[p + 1];
+    uint64_t mx = 0;
+    for (uint32_t j = 0; j < p; j++) mx = std::max<uint64_t>(mx, h_sizes[j]);
+    c.stats.max_partition = mx;
+    if (a.part_sizes)
+        for (uint32_t j = 0; j < p; j++) a.part_sizes[j] = h_sizes[j];
+    if (a.part_pivots)
+        for (uint32_t j = 0; j + 1 < p; j++) a.part_pivots[j] = h_piv[j];
+    return CAPSSA_OK;
+}
+
 template <typename S>
 capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
     using namespace eng;
@@ -2476,7 +2907,22 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
 
     uint32_t *sa = nullptr;
     eng::Packed P{};
-    if (n > 0) {
+    // the sample sort with its partition ahead of the sort (whole texts,
+    // unbounded context, at least two buckets)
+    bool part_done = false;
+    if (n > 0 && !subset && !bounded && a.part_p >= 2 && a.part_first && a.part_p <= 8192) {
+        PfRun pf;
+        pf.p = a.part_p;
+        pf.learned = a.part_mode == CAPSSA_PARTITION_LEARNED;
+        capssa_status s = core_sort<S>(c, a, &sa, &P, &pf);
+        if (s != CAPSSA_OK) return s;
+        if (!pf.fell_back) {
+            s = pf_report(c, a, pf);
+            if (s != CAPSSA_OK) return s;
+            part_done = true;
+        }
+    }
+    if (n > 0 && !part_done) {
         capssa_status s = core_sort<S>(c, a, &sa, &P);
         if (s != CAPSSA_OK) return s;
         if (bounded) {
@@ -2484,7 +2930,7 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
             if (s != CAPSSA_OK) return s;
         }
     }
-    if (!subset && a.part_p) {
+    if (!subset && a.part_p && !part_done) {
         capssa_status s = partition_phase<S>(c, a, P, sa, sa, n);
         if (s != CAPSSA_OK) return s;
     }

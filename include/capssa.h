@@ -78,6 +78,23 @@ typedef enum {
     CAPSSA_PARTITION_LEARNED = 2
 } capssa_partition;
 
+/* Where the sample sort's splitter sample comes from. */
+typedef enum {
+    /* PARTITION_FIRST for the sample-sort builders and plans over a whole
+     * text with an unbounded context; REFERENCE otherwise */
+    CAPSSA_SAMPLING_AUTO = 0,
+    /* the reference's rule (phase 1, src/ext_mem.rs:1191-1305): evenly
+     * spaced midpoints of every sorted chunk of the input; the chunks'
+     * order comes from the full sort, so the partition follows the sort */
+    CAPSSA_SAMPLING_REFERENCE = 1,
+    /* the same number of samples as evenly spaced midpoints of the input
+     * order, sorted on their own; every suffix is bucketed by comparison
+     * with the pivots before the sort, and the buckets drive it.  Texts
+     * whose sample or pivot comparisons run deeper than 2^16 symbols fall
+     * back to REFERENCE (same output) */
+    CAPSSA_SAMPLING_PARTITION_FIRST = 2
+} capssa_sampling;
+
 /* Opts{max_context} (src/sample_sort.rs:70-85) and the in-memory subset of
  * ExtMemOpts (src/ext_mem.rs:60-118).  Zero-initialise, then set
  * max_context = CAPSSA_UNBOUNDED for the reference default. */
@@ -89,7 +106,9 @@ typedef struct capssa_opts {
     int32_t partition;         /* capssa_partition (sample-sort builders) */
     int32_t host_threads;      /* thread count the auto p rule assumes; 0 = all cores */
     uint64_t flags;            /* no flags are defined: 0 */
-    uint64_t reserved[5];
+    int32_t sampling;          /* capssa_sampling (sample-sort builders and plans) */
+    int32_t reserved32;
+    uint64_t reserved[4];
 } capssa_opts;
 
 void capssa_opts_default(capssa_opts *o);

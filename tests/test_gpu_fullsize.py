@@ -1,8 +1,10 @@
 """The benchmark workloads at their real sizes, checked against the oracle.
 
   C2  n = 2^28 DNA with 30% planted repeats, PlainText, u32: bit-exact.
-  C4  the sample sort of the C2 text with p = 4096 learned partitions:
-      the emitted order bit-exact, the plan (pivots, sizes) equal to the
+  C4  the sample sort of the C2 text with p = 4096 learned partitions,
+      bucketed before the sort: the emitted order bit-exact, the pivots the
+      oracle's sorted sample and every bucket's size counted on the oracle's
+      suffix array; the reference-rule plan (pivots, sizes) equal to the
       oracle's sample sort.
   C3  n = 2^29 segmented text, the positions with text[p] < 4, u64:
       ShorterFirst equal after canonicalising each tie class (the reference
@@ -55,15 +57,27 @@ def test_c2_bench_text_2p28_bit_exact(ctx, c2):
 
 
 def test_c4_learned_sample_sort_2p28_bit_exact(ctx, c2):
+    from test_gpu_partition import pf_expected_plan
     t, want = c2
     opts = capssa.ExtMemOpts(subproblem_count=4096, partition=capssa.Partition.LEARNED)
     got = ctx.build_in_memory_sample_sort(t, opts)
     assert got.dtype == np.uint64
     assert np.array_equal(got, want.astype(np.uint64))
-    _, kp, opv, osz = orc.sample_sort(t, subproblem_count=4096)
+    del got
+    ends, sizes = pf_expected_plan(t, orc.Limits(len(t)), 4096, want)
     for part in (capssa.Partition.LEARNED, capssa.Partition.SPLITTERS):
         k, pv, sz = ctx.sample_sort_plan(t, capssa.ExtMemOpts(subproblem_count=4096,
                                                               partition=part))
+        assert k == 4096
+        assert np.array_equal(sz.astype(np.int64), sizes)
+        pos_of = np.empty(len(t), dtype=np.int64)
+        pos_of[want] = np.arange(len(t))
+        assert np.array_equal(pos_of[pv.astype(np.int64)], ends)  # PlainText: no ties
+        del pos_of
+    _, kp, opv, osz = orc.sample_sort(t, subproblem_count=4096)
+    for part in (capssa.Partition.LEARNED, capssa.Partition.SPLITTERS):
+        k, pv, sz = ctx.sample_sort_plan(t, capssa.ExtMemOpts(
+            subproblem_count=4096, partition=part, sampling=capssa.Sampling.REFERENCE))
         assert k == kp == 4096
         assert np.array_equal(pv, opv[:k - 1])
         assert np.array_equal(sz, osz[:k])

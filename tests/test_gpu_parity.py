@@ -461,7 +461,6 @@ def test_large_text_star_segments(ctx):
     rng = np.random.default_rng(5)
     ends = np.unique(np.concatenate([rng.integers(1, len(t), 300), [len(t)]])).tolist()
     check_against_oracle(ctx, t, ends=ends, longer_first=True)
-    assert ctx.stats()["partitions"] == 65536
 
 
 def test_large_text_wide_alphabet(ctx):

@@ -5,6 +5,8 @@ restatement of build_in_memory_sample_sort (src/ext_mem.rs:1191-1428); the
 learned partition must reproduce the splitter partition exactly; the model's
 GPU gradients are checked against the oracle's (relative 1e-4 of the largest
 component, FP32 against double accumulation)."""
+import math
+
 import numpy as np
 import pytest
 
@@ -61,10 +63,13 @@ def _orc_limits(n, ends=None, longer_first=False):
     return orc.Limits(n, ends, longer_first)
 
 
+REF = capssa.Sampling.REFERENCE
+
+
 @pytest.mark.parametrize("p", [2, 16, 100])
 def test_plan_matches_oracle_plain(ctx, p):
     t = _dna(60000, seed=3)
-    k, pv, sz = ctx.sample_sort_plan(t, capssa.ExtMemOpts(subproblem_count=p))
+    k, pv, sz = ctx.sample_sort_plan(t, capssa.ExtMemOpts(subproblem_count=p, sampling=REF))
     _, kp, opv, osz = orc.sample_sort(t, subproblem_count=p)
     assert k == kp == p
     assert pv.tolist() == opv.tolist()
@@ -78,13 +83,15 @@ def test_plan_matches_oracle_star_and_segmented(ctx):
     ends = sorted(set(rng.integers(1, 30000, 40).tolist()) | {30000})
     # STAR (total order): pivots and sizes equal
     lp = capssa.SegmentedText(len(t), ends, capssa.BoundaryRank.LONGER_FIRST)
-    k, pv, sz = ctx.sample_sort_plan(t, capssa.ExtMemOpts(subproblem_count=24), lp=lp)
+    k, pv, sz = ctx.sample_sort_plan(t, capssa.ExtMemOpts(subproblem_count=24, sampling=REF),
+                                     lp=lp)
     _, kp, opv, osz = orc.sample_sort(t, limits=_orc_limits(len(t), ends, True),
                                       subproblem_count=24)
     assert pv.tolist() == opv.tolist() and sz.tolist() == osz.tolist()
     # ShorterFirst: tied pivots may differ, the partition sizes may not
     lp = capssa.SegmentedText(len(t), ends)
-    k, pv, sz = ctx.sample_sort_plan(t, capssa.ExtMemOpts(subproblem_count=24), lp=lp)
+    k, pv, sz = ctx.sample_sort_plan(t, capssa.ExtMemOpts(subproblem_count=24, sampling=REF),
+                                     lp=lp)
     _, kp, opv, osz = orc.sample_sort(t, limits=_orc_limits(len(t), ends), subproblem_count=24)
     assert sz.tolist() == osz.tolist()
 
@@ -105,6 +112,123 @@ def test_plan_with_finite_context(ctx):
     k, pv, sz = ctx.sample_sort_plan(t, opts)
     _, kp, opv, osz = orc.sample_sort(t, max_ctx=8, subproblem_count=10)
     assert sz.tolist() == osz.tolist()
+
+
+# ---------------------------------------------------------------- partition first
+
+def pf_sample_count(n, p):
+    """The splitter sample's size: the reference sampler's count
+    (src/ext_mem.rs:1282-1287), capped at n."""
+    total = min(max(p * math.ceil(4 * max(math.log(n), 1.0)), p), n)
+    return min(-(-total // p) * p, n)
+
+
+def pf_expected_plan(t, lo, p, want_sa):
+    """The partition-first plan restated with the oracle: the sample (ns
+    evenly spaced midpoints of the text) in exact suffix order, pivots
+    sample[(j + 1) * ns / p], and every bucket's size counted on the oracle's
+    suffix array (bucket j: pivot[j-1] < s <= pivot[j], so it ends at the
+    last suffix of pivot j's tie class).  Returns (pivot tie-class ends,
+    sizes)."""
+    n = len(t)
+    ns = pf_sample_count(n, p)
+    samples = ((2 * np.arange(ns, dtype=np.uint64) + 1) * n) // (2 * ns)
+    ss = orc.build_in_memory(t, samples.astype(np.uint32), lo)
+    piv = ss[(np.arange(1, p, dtype=np.int64) * ns) // p]
+    cmp = orc.adjacent_cmp(t, want_sa, lo)
+    # last SA index of every suffix's tie class
+    last = np.arange(n, dtype=np.int64)
+    tie = np.nonzero(cmp == 0)[0]
+    for i in tie[::-1]:
+        last[i] = last[i + 1]
+    isa = np.empty(n, dtype=np.int64)
+    isa[want_sa] = np.arange(n)
+    ends = last[isa[piv.astype(np.int64)]]
+    sizes = np.diff(np.concatenate([[-1], ends, [n - 1]]))
+    return ends, sizes
+
+
+def check_pf(ctx, t, p, lp=None, lo=None, partition=capssa.Partition.SPLITTERS, ties=False):
+    n = len(t)
+    lo = lo or orc.Limits(n)
+    want = orc.build_in_memory(t, None, lo)
+    opts = capssa.ExtMemOpts(subproblem_count=p, partition=partition)
+    got = ctx.build_in_memory_sample_sort(t, opts, lp=lp)
+    if ties:
+        cw = orc.adjacent_cmp(t, want, lo)
+        assert np.array_equal(got, orc.canonical_ties(want, cw).astype(np.uint64))
+    else:
+        assert np.array_equal(got, want.astype(np.uint64))
+    k, pv, sz = ctx.sample_sort_plan(t, opts, lp=lp)
+    st = ctx.stats()
+    ends, sizes = pf_expected_plan(t, lo, p, want)
+    isa = np.empty(n, dtype=np.int64)
+    isa[want] = np.arange(n)
+    assert k == p
+    # pivots: the same suffixes, or (ShorterFirst ties) members of the same class
+    last = np.arange(n, dtype=np.int64)
+    cmp = orc.adjacent_cmp(t, want, lo)
+    for i in np.nonzero(cmp == 0)[0][::-1]:
+        last[i] = last[i + 1]
+    assert np.array_equal(last[isa[pv.astype(np.int64)]], ends)
+    assert np.array_equal(sz.astype(np.int64), sizes)
+    return st
+
+
+@pytest.mark.parametrize("p", [2, 64, 1024])
+def test_partition_first_plain_bit_exact(ctx, p):
+    """Buckets found before the sort by comparing every suffix with the
+    pivots: the emitted order is the oracle's, the pivots are the oracle's
+    sorted sample, and each bucket holds exactly the suffixes between its
+    pivots."""
+    st = check_pf(ctx, _dna(1 << 20, seed=30 + p), p)
+    assert st["partitions"] == p and st["partition_probes"] > 0
+
+
+def test_partition_first_learned_equals_splitters(ctx):
+    t = _dna(1 << 20, seed=40)
+    st = check_pf(ctx, t, 1024, partition=capssa.Partition.LEARNED)
+    assert st["train_samples"] > 0
+    assert st["mispredicted"] < len(t)
+
+
+@pytest.mark.parametrize("dtype", [np.uint16, np.uint32])
+def test_partition_first_wide_symbols(ctx, dtype):
+    rng = np.random.default_rng(41)
+    t = rng.integers(0, 300 if dtype == np.uint16 else 70000, 200000).astype(dtype)
+    t[5000:9000] = t[100:4100]  # a long repeat
+    check_pf(ctx, t, 128)
+
+
+def test_partition_first_star_segments(ctx):
+    t = _dna(300000, seed=42)
+    rng = np.random.default_rng(43)
+    ends = np.unique(np.concatenate([rng.integers(1, len(t), 400), [len(t)]])).astype(np.uint64)
+    lp = capssa.SegmentedText(len(t), ends, capssa.BoundaryRank.LONGER_FIRST)
+    check_pf(ctx, t, 200, lp, orc.Limits(len(t), ends, longer_first=True))
+
+
+def test_partition_first_shorter_first_segments(ctx):
+    """ShorterFirst segments tie: the emitted order equals the oracle's after
+    canonicalising each tie class (GPU classes in ascending position)."""
+    rng = np.random.default_rng(44)
+    t = rng.integers(0, 4, 200000).astype(np.uint8)
+    ends = np.unique(np.concatenate([rng.integers(1, len(t), 3000), [len(t)]])).astype(np.uint64)
+    lp = capssa.SegmentedText(len(t), ends)
+    check_pf(ctx, t, 100, lp, orc.Limits(len(t), ends), ties=True)
+
+
+def test_partition_first_falls_back_on_deep_ties(ctx):
+    """A single-symbol text: the sample's keys all tie and its comparisons run
+    past 2^16 symbols, so the sort runs first and the plan is the reference
+    rule's (equal to the oracle's sample sort); the output is the same."""
+    t = np.zeros(1 << 17, dtype=np.uint8)
+    want = orc.build_in_memory(t).astype(np.uint64)
+    opts = capssa.ExtMemOpts(subproblem_count=16)
+    assert np.array_equal(ctx.build_in_memory_sample_sort(t, opts), want)
+    k, pv, sz = ctx.sample_sort_plan(t, opts)
+    _, kp, opv, osz = orc.sample_sort(t, subproblem_count=16)
+    assert pv.tolist() == opv.tolist() and sz.tolist() == osz.tolist()
 
 
 # ---------------------------------------------------------------- learned partition
