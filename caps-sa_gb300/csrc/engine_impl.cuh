@@ -461,58 +461,46 @@ __global__ void short_write_kernel(const ShortList *__restrict__ S, uint32_t *__
     hd[S->slot[j]] = S->slot[j];
 }
 
-constexpr int kInitPer = 16;  // sorted keys per thread in init_groups_kernel
-constexpr int kInitTile = 256 * kInitPer;
+constexpr int kInitSteps = 16;                 // warp steps of 32 sorted records
+constexpr int kInitWarpSpan = 32 * kInitSteps;  // 512 consecutive records per warp
+constexpr int kInitTile = 8 * kInitWarpSpan;    // 4096 records per block of 256 threads
 
 // Group heads after the key sort, in SA order (hd[i] = first SA index of
 // i's group; equal heads == equal comparison so far); tied groups that need
 // more symbols become the first round's work (engine.cuh step 3 -> 4).
-// A block stages its 256 * kInitPer sorted keys (and their neighbours) in
-// shared memory once, unpacks the positions when they ride below the keys,
-// and appends its groups with one atomic per list (per-list counts packed
-// as 16-bit fields, 4096 keys per block at most).
+// Each warp walks 512 consecutive sorted records, 32 at a time: neighbours
+// come by shuffles, group starts by a ballot of the heads (carried across
+// steps), so every record costs a fixed handful of instructions.  The
+// block's group ends are staged in shared memory and appended with one
+// global atomic per list.  The positions riding below the keys are unpacked
+// into sa_out (segment-local ones rebased), and the short suffixes of a
+// flagless sort shift every record after their insertion points.
 __global__ void __launch_bounds__(256)
     init_groups_kernel(const uint64_t *__restrict__ keys, uint32_t n, int k, uint64_t lmask,
                        int lf, int flag_len, int vshift, uint32_t *__restrict__ hd,
                        uint32_t *__restrict__ sa_out, GroupLists G,
                        const ShortList *__restrict__ S, int seg_at,
                        const uint64_t *__restrict__ seg_ends) {
-    static_assert(kLists <= 8, "two packed words of four 16-bit counters");
-    __shared__ uint64_t sk[kInitTile + 2];  // sk[l + 1] = key of sorted index base + l
-    __shared__ uint32_t s_base[kLists];
-    const uint32_t base = blockIdx.x * (uint32_t)kInitTile;
-    const uint32_t valid = n - base < (uint32_t)kInitTile ? n - base : (uint32_t)kInitTile;
+    __shared__ uint4 s_pend[kInitTile / 2 + 1];  // (start, len, depth, list << 16 | index in list)
+    __shared__ uint32_t s_npend, s_cnt[kLists], s_base[kLists];
+    __shared__ uint32_t s_shift[2];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t bbase = blockIdx.x * (uint32_t)kInitTile;
+    const uint32_t bvalid = n - bbase < (uint32_t)kInitTile ? n - bbase : (uint32_t)kInitTile;
     const uint64_t vmask = (1ull << vshift) - 1;
     // SA index of sorted record i: i + (short suffixes inserted at or before
     // it), one shift for the whole block unless an insertion falls inside
-    __shared__ uint32_t s_shift[2];
     const uint32_t ns = S ? __ldg(&S->n) : 0u;
     if (threadIdx.x == 0) {
-        const uint32_t lo = ns ? short_shift(S, ns, base) : 0u;
+        const uint32_t lo = ns ? short_shift(S, ns, bbase) : 0u;
         s_shift[0] = lo;
-        s_shift[1] = !ns || short_shift(S, ns, base + valid - 1) == lo;
+        s_shift[1] = !ns || short_shift(S, ns, bbase + bvalid - 1) == lo;
+        s_npend = 0;
     }
+    if (threadIdx.x < kLists) s_cnt[threadIdx.x] = 0;
     __syncthreads();
     const uint32_t sh_lo = s_shift[0];
     const bool sh_flat = s_shift[1] != 0;
-    auto shift_of = [&](uint32_t i) { return sh_flat ? sh_lo : short_shift(S, ns, i); };
-    for (uint32_t l = threadIdx.x; l < valid; l += 256) {
-        const uint64_t item = keys[base + l];
-        sk[l + 1] = item >> vshift;
-        if (sa_out) {
-            // segment-local positions (seg_at > 0): the segment index above
-            // the key gives the segment's first position
-            uint64_t pos = item & vmask;
-            if (seg_at) {
-                const uint64_t sg = item >> seg_at;
-                pos += sg ? __ldg(seg_ends + sg - 1) : 0ull;
-            }
-            sa_out[base + l + shift_of(base + l)] = (uint32_t)pos;
-        }
-    }
-    if (threadIdx.x == 0) sk[0] = base > 0 ? keys[base - 1] >> vshift : 0ull;
-    if (threadIdx.x == 32) sk[valid + 1] = base + valid < n ? keys[base + valid] >> vshift : 0ull;
-    __syncthreads();
     // tie state of a key: complete (equal through both ends: nothing to
     // refine), and the depth its group's members are known to agree on
     // (0 for the early-ended suffixes of a flagged plain text)
@@ -530,88 +518,107 @@ __global__ void __launch_bounds__(256)
             depth = (uint64_t)k;
         }
     };
-    // first sorted index of the run of `key` that holds local index l
-    auto head_of = [&](uint32_t l, uint64_t key) -> uint32_t {
-        uint32_t m = l;
-        int steps = 0;
-        while (m > 0 && steps < 32 && sk[m] == key) {  // sk[m] = key of local m - 1
-            m--;
-            steps++;
-        }
-        if (steps < 32 && (m > 0 || base == 0 || sk[0] != key)) return base + m;
-        return run_head(keys, 0, base + m, key, vshift);  // long run or one that began earlier
-    };
-    uint64_t cnt_lo = 0, cnt_hi = 0;  // 16-bit counts: lists 0..3, lists 4..
-    uint32_t ends = 0;                 // bit j: key j ends a group that needs refining
     // only LongerFirst with a length field separates complete ties by position
     const bool lf_field = lf && !flag_len;
-    // pass 1: heads, and the groups this thread ends (singletons, the bulk,
-    // take the shortest path)
-#pragma unroll 4
-    for (int j = 0; j < kInitPer; j++) {
-        const uint32_t l = j * 256 + threadIdx.x;
-        if (l >= valid) break;
-        const uint32_t i = base + l;
-        const uint64_t key = sk[l + 1];
-        const bool head = (i == 0) || sk[l] != key;
-        const bool last = (i == n - 1) || sk[l + 2] != key;
-        // an insertion point only ever falls on a group head, so a group
-        // moves by one shift
-        const uint32_t sh = shift_of(i);
-        if (head && last) {
-            hd[i + sh] = i + sh;
-            continue;
-        }
-        const uint32_t g = head ? i : head_of(l, key);
-        bool complete = false;
-        uint64_t depth = (uint64_t)k;
-        if (lf_field || (last && !head)) state(key, complete, depth);
-        hd[i + sh] = ((complete && lf) ? i : g) + sh;
-        if (!complete && last && !head) {
-            const int li = list_of(i - g + 1, depth);
-            if (li == kLists) {
-                append_big(G, 0, g + sh, i - g + 1);
+    const uint32_t wbase = bbase + (uint32_t)warp * kInitWarpSpan;
+    const unsigned le_mask = 0xFFFFFFFFu >> (31 - lane);  // lanes <= this one
+    const unsigned lt_mask = (1u << lane) - 1u;
+    uint64_t carry_key = 0;   // key of the record before this step
+    uint32_t carry_start = 0;  // start of the group that record belongs to
+    if (wbase < n && wbase > 0) {
+        carry_key = keys[wbase - 1] >> vshift;
+        const uint64_t k0 = keys[wbase] >> vshift;
+        carry_start = carry_key == k0 ? run_head(keys, 0, wbase - 1, carry_key, vshift) : wbase;
+    }
+    for (int j = 0; j < kInitSteps; j++) {
+        const uint32_t sbase = wbase + (uint32_t)j * 32;
+        if (sbase >= n) break;  // warp-uniform
+        const uint32_t i = sbase + (uint32_t)lane;
+        const bool valid = i < n;
+        const uint64_t item = valid ? keys[i] : 0ull;
+        const uint64_t key = item >> vshift;
+        uint64_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+        uint64_t next = __shfl_down_sync(0xffffffffu, key, 1);
+        if (lane == 0) prev = carry_key;
+        if (lane == 31 && i + 1 < n) next = keys[i + 1] >> vshift;
+        const bool head = valid && (i == 0 || prev != key);
+        const bool last = valid && (i + 1 >= n || next != key);
+        const unsigned hm = __ballot_sync(0xffffffffu, head) & le_mask;
+        const uint32_t start = hm ? sbase + (uint32_t)(31 - __clz((int)hm)) : carry_start;
+        carry_start = __shfl_sync(0xffffffffu, start, 31);
+        carry_key = __shfl_sync(0xffffffffu, key, 31);
+        const uint32_t sh = sh_flat ? sh_lo : (valid ? short_shift(S, ns, i) : 0u);
+        bool end_here = false;
+        uint4 ent = make_uint4(0, 0, 0, 0);
+        int li = -1;
+        if (valid) {
+            if (sa_out) {
+                // segment-local positions (seg_at > 0): the segment index
+                // above the key gives the segment's first position
+                uint64_t pos = item & vmask;
+                if (seg_at) {
+                    const uint64_t sg = item >> seg_at;
+                    pos += sg ? __ldg(seg_ends + sg - 1) : 0ull;
+                }
+                sa_out[i + sh] = (uint32_t)pos;
+            }
+            if (head && last) {
+                hd[i + sh] = i + sh;
             } else {
-                if (li < 4)
-                    cnt_lo += 1ull << (16 * li);
-                else
-                    cnt_hi += 1ull << (16 * (li - 4));
-                ends |= 1u << j;
+                bool complete = false;
+                uint64_t depth = (uint64_t)k;
+                if (lf_field || last) state(key, complete, depth);
+                hd[i + sh] = ((complete && lf) ? i : start) + sh;
+                if (last && !complete) {
+                    // an insertion point only ever falls on a group head, so
+                    // a group moves by one shift
+                    const uint32_t len = i - start + 1;
+                    li = list_of(len, depth);
+                    if (li == kLists) {
+                        append_big(G, 0, start + sh, len);
+                        li = -1;
+                    } else {
+                        end_here = true;
+                        ent = group_entry(start + sh, len, depth);
+                    }
+                }
             }
         }
-    }
-    uint64_t off_lo, off_hi;
-    const uint64_t tot_lo = block_excl_scan64(cnt_lo, &off_lo);
-    const uint64_t tot_hi = block_excl_scan64(cnt_hi, &off_hi);
-    if (threadIdx.x < kLists) {
-        const int li = (int)threadIdx.x;
-        const uint32_t total =
-            (uint32_t)(((li < 4 ? tot_lo : tot_hi) >> (16 * (li & 3))) & 0xFFFFu);
-        if (total) s_base[li] = atomicAdd(&G.ctr->n[li][0], total);
+        // stage this step's group ends: one shared atomic per warp and list
+        const unsigned em = __ballot_sync(0xffffffffu, end_here);
+        if (em) {
+            uint32_t pbase = 0;
+            if (lane == 0) pbase = atomicAdd(&s_npend, (uint32_t)__popc(em));
+            pbase = __shfl_sync(0xffffffffu, pbase, 0);
+            uint32_t lidx = 0;
+#pragma unroll
+            for (int q = 0; q < kLists; q++) {
+                const unsigned qm = __ballot_sync(0xffffffffu, li == q);
+                if (qm) {
+                    uint32_t qb = 0;
+                    const int leader = __ffs((int)qm) - 1;
+                    if (lane == leader) qb = atomicAdd(&s_cnt[q], (uint32_t)__popc(qm));
+                    qb = __shfl_sync(0xffffffffu, qb, leader);
+                    if (li == q) lidx = qb + (uint32_t)__popc(qm & lt_mask);
+                }
+            }
+            if (end_here) {
+                ent.w = ((uint32_t)li << 16) | lidx;
+                s_pend[pbase + (uint32_t)__popc(em & lt_mask)] = ent;
+            }
+        }
     }
     __syncthreads();
-    // pass 2: write the entries of the groups found in pass 1
-    for (; ends; ends &= ends - 1) {
-        const int j = __ffs((int)ends) - 1;
-        const uint32_t l = j * 256 + threadIdx.x;
-        const uint32_t i = base + l;
-        const uint64_t key = sk[l + 1];
-        bool complete;
-        uint64_t depth;
-        state(key, complete, depth);
-        const uint32_t g = head_of(l, key);
-        const int li = list_of(i - g + 1, depth);
-        uint32_t slot = 0;
-#pragma unroll
-        for (int q = 0; q < kLists; q++) {
-            if (li == q) {
-                uint64_t &off = q < 4 ? off_lo : off_hi;
-                const int sh = 16 * (q & 3);
-                slot = s_base[q] + (uint32_t)((off >> sh) & 0xFFFFu);
-                off += 1ull << sh;
-            }
-        }
-        list_ptr(G, li, 0)[slot] = group_entry(g + shift_of(i), i - g + 1, depth);
+    if (threadIdx.x < kLists && s_cnt[threadIdx.x])
+        s_base[threadIdx.x] = atomicAdd(&G.ctr->n[threadIdx.x][0], s_cnt[threadIdx.x]);
+    __syncthreads();
+    const uint32_t np = s_npend;
+    for (uint32_t e = threadIdx.x; e < np; e += 256) {
+        uint4 ent = s_pend[e];
+        const int q = (int)(ent.w >> 16);
+        const uint32_t slot = s_base[q] + (ent.w & 0xFFFFu);
+        ent.w = 0;
+        list_ptr(G, q, 0)[slot] = ent;
     }
 }
 
@@ -1789,7 +1796,8 @@ __global__ void partition_check_kernel(const uint32_t *__restrict__ bucket_of,
 // every bucket contiguous and in suffix order up to the window, and the
 // usual refinement finishes each bucket (phase 4, src/ext_mem.rs:1745-2108).
 
-constexpr uint64_t kPfCmpCap = 1ull << 16;  // symbols an exact pivot comparison may read
+constexpr uint64_t kPfCmpCap = 1ull << 16;  // symbols an exact sample comparison may read
+constexpr uint64_t kPfPivotCap = 1ull << 12;  // symbols a suffix-vs-pivot comparison may read
 constexpr uint32_t kPfTieMax = 64;          // largest run of equal sample keys sorted exactly
 constexpr uint32_t kPfEllCap = 1u << 15;    // window offsets are capped (any prefix length works)
 
@@ -1939,8 +1947,10 @@ __global__ void __launch_bounds__(kKeyThreads)
             probes++;
             const uint64_t pk = sk[j];
             if (K != pk) return K > pk;
+            const uint32_t pj = __ldg(ppos + j);
+            if (pj == q) return false;  // the pivot itself
             const int c =
-                direct_cmp(P, q, lim, __ldg(ppos + j), __ldg(plim + j), 0, kPfCmpCap, lf);
+                direct_cmp(P, q, lim, pj, __ldg(plim + j), 0, kPfPivotCap, lf);
             if (c == 2) deep = true;
             return c == 1;
         };
@@ -2093,8 +2103,9 @@ struct PfRun {
 // count as the reference's sampler, as evenly spaced midpoints of the text)
 // sorted exactly, its pivots and their common prefixes, the learned model
 // (LEARNED), then the fused partition + record kernel over every position.
-// A sample run or pivot comparison deeper than kPfCmpCap symbols sets
-// pf->fell_back (one synchronisation after the fused kernel).
+// A sample run longer than kPfTieMax, a sample comparison deeper than
+// kPfCmpCap symbols or a pivot comparison deeper than kPfPivotCap sets
+// pf->fell_back (checked after the sample sort and after the fused kernel).
 template <typename S>
 capssa_status pf_keys(Ctx &c, const EngineArgs &a, const eng::Packed &P, const KeyGeom &geo,
                       int bucket_bits, int key_passes, uint64_t *keys, uint32_t *counts,
@@ -2145,6 +2156,13 @@ capssa_status pf_keys(Ctx &c, const EngineArgs &a, const eng::Packed &P, const K
     pf_sample_ties_kernel<<<grid_for(ns, 256), 256, 0, c.stream>>>(skeys, spos, ns, P, a.lim, lf,
                                                                    fb);
     CAPSSA_LAUNCHED(c);
+    int *h_fb = (int *)c.h_scratch;
+    CAPSSA_CUDA(c, cudaMemcpyAsync(h_fb, fb, 4, cudaMemcpyDeviceToHost, c.stream));
+    CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+    if (*h_fb) {  // a degenerate sample: sort first instead
+        pf->fell_back = true;
+        return CAPSSA_OK;
+    }
     // 2. pivots and the buckets' common prefixes
     pf_pivot_kernel<<<grid_for(p, 256), 256, 0, c.stream>>>(spos, ns, p, P, a.lim, lf, pkey,
                                                             ppos, plim);
@@ -2206,7 +2224,6 @@ capssa_status pf_keys(Ctx &c, const EngineArgs &a, const eng::Packed &P, const K
 #undef CAPSSA_PF_LAUNCH
     CAPSSA_LAUNCHED(c);
     cudaEventRecord(q1, c.stream);
-    int *h_fb = (int *)c.h_scratch;
     CAPSSA_CUDA(c, cudaMemcpyAsync(h_fb, fb, 4, cudaMemcpyDeviceToHost, c.stream));
     CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
     float pms = 0.0f;
