@@ -160,8 +160,8 @@ def hbm_peak():
 
 def profiled_traffic(n, item_bytes):
     """DRAM bytes per radix-pass launch from the committed ncu summary for
-    this record width, scaled by records per launch (traffic grows linearly
-    with the records)."""
+    this record width (captured at 2^26 records, input 4x L2), scaled by
+    records per launch (traffic grows linearly with the records)."""
     p = os.path.join(ROOT, "profiles", "radix_onesweep_pass_%dB.txt" % item_bytes)
     try:
         vals = {}

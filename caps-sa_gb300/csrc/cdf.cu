@@ -137,6 +137,37 @@ __global__ void to_bf16_kernel(const float *__restrict__ params, __nv_bfloat16 *
     for (int i = threadIdx.x; i < kParams; i += blockDim.x) w[i] = __float2bfloat16(params[i]);
 }
 
+// Data-dependent start for n samples sorted by prefix: the ReLU kinks sit on
+// f0 at 64 evenly spaced samples, and the output weights make the model the
+// piecewise-linear interpolant of the targets through those samples (flat
+// before the first and after the last); coinciding kinks get no slope.
+// Training then only has to refine it.
+__global__ void knot_init_kernel(const uint64_t *__restrict__ x, const float *__restrict__ t,
+                                 uint32_t n, float *__restrict__ params) {
+    __shared__ float c[kHidden], y[kHidden], m[kHidden];
+    const int h = threadIdx.x;
+    if (h < kHidden) {
+        const uint32_t i = (uint32_t)(((uint64_t)h * (n - 1)) / (kHidden - 1));
+        float f0, f1;
+        features(x[i], f0, f1);
+        c[h] = f0;
+        y[h] = t[i];
+    }
+    __syncthreads();
+    if (h < kHidden) {  // slope of the segment after kink h (0 after the last)
+        const float dx = h + 1 < kHidden ? c[h + 1] - c[h] : 0.0f;
+        m[h] = dx > 1e-6f ? (y[h + 1] - y[h]) / dx : 0.0f;
+    }
+    __syncthreads();
+    if (h < kHidden) {
+        params[2 * h] = 1.0f;
+        params[2 * h + 1] = 0.0f;
+        params[2 * kHidden + h] = -c[h];
+        params[3 * kHidden + h] = m[h] - (h > 0 ? m[h - 1] : 0.0f);
+        if (h == 0) params[4 * kHidden] = y[0];
+    }
+}
+
 // Workspace of one training: grad, m, v (kParams each), loss, loss_out, step.
 struct TrainState {
     float *grad, *m, *v, *loss, *loss_out;
@@ -166,7 +197,7 @@ capssa_status grad(Ctx &c, const float *params, const uint64_t *x, const float *
 }
 
 capssa_status train(Ctx &c, const uint64_t *x, const float *t, uint32_t n, int steps,
-                    float *params, __nv_bfloat16 *w_bf16, float *final_loss) {
+                    float *params, __nv_bfloat16 *w_bf16, float *final_loss, bool knot_start) {
     std::vector<float> h(kParams);
     init_params(h.data());
     float *st = (float *)ws_get(c, WS_CDF, (size_t)(4 * kParams + 16) * 4);
@@ -178,9 +209,15 @@ capssa_status train(Ctx &c, const uint64_t *x, const float *t, uint32_t n, int s
     CAPSSA_CUDA(c, cudaMemsetAsync(st, 0, (size_t)(4 * kParams + 16) * 4, c.stream));
     CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));  // h goes out of scope
     if (n == 0) return CAPSSA_OK;
+    if (knot_start && n >= 2) {
+        knot_init_kernel<<<1, kHidden, 0, c.stream>>>(x, t, n, params);
+        CAPSSA_LAUNCHED(c);
+    }
     const unsigned blocks = std::min<unsigned>(kGradBlocks, (n + kGradThreads - 1) / kGradThreads);
     auto step_launch = [&](int s) {
-        const float lr = s < steps * 3 / 4 ? 1e-2f : 2e-3f;
+        // from the interpolating start only small steps refine the fit
+        const float lr0 = knot_start ? 2e-4f : 1e-2f;
+        const float lr = s < steps * 3 / 4 ? lr0 : lr0 * 0.2f;
         grad_kernel<<<blocks, kGradThreads, 0, c.stream>>>(params, x, t, n, S.grad, S.loss);
         adam_kernel<<<1, 320, 0, c.stream>>>(params, S.grad, S.m, S.v, S.step, lr, S.loss,
                                              S.loss_out, n);

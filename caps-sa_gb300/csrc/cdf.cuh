@@ -50,9 +50,12 @@ capssa_status grad(Ctx &c, const float *params, const uint64_t *x, const float *
 // Trains params (device, kParams floats; initialised here) on n (prefix,
 // target) samples with `steps` full-batch Adam steps, replayed from a CUDA
 // graph; writes the BF16 copy to w_bf16 (device, kParams) and returns the
-// final mean loss in *final_loss.
+// final mean loss in *final_loss.  knot_start (samples sorted by prefix):
+// start from the piecewise-linear interpolant through 64 of the samples
+// instead of evenly spread kinks.
 capssa_status train(Ctx &c, const uint64_t *x, const float *t, uint32_t n, int steps,
-                    float *params, __nv_bfloat16 *w_bf16, float *final_loss);
+                    float *params, __nv_bfloat16 *w_bf16, float *final_loss,
+                    bool knot_start = false);
 
 // Deterministic initial parameters: ReLU kinks evenly spread over f0.
 void init_params(float *h_params);

@@ -530,17 +530,31 @@ __global__ void __launch_bounds__(256)
         const uint64_t k0 = keys[wbase] >> vshift;
         carry_start = carry_key == k0 ? run_head(keys, 0, wbase - 1, carry_key, vshift) : wbase;
     }
+    // every step's record first (16 loads in flight per lane), and the
+    // record after the warp's span for the last step's lane 31
+    uint64_t items[kInitSteps];
+#pragma unroll
+    for (int j = 0; j < kInitSteps; j++) {
+        const uint32_t i = wbase + (uint32_t)j * 32 + (uint32_t)lane;
+        items[j] = i < n ? keys[i] : 0ull;
+    }
+    const uint32_t after = wbase + kInitWarpSpan;
+    const uint64_t after_key = after < n ? keys[after] >> vshift : 0ull;
+#pragma unroll
     for (int j = 0; j < kInitSteps; j++) {
         const uint32_t sbase = wbase + (uint32_t)j * 32;
         if (sbase >= n) break;  // warp-uniform
         const uint32_t i = sbase + (uint32_t)lane;
         const bool valid = i < n;
-        const uint64_t item = valid ? keys[i] : 0ull;
+        const uint64_t item = items[j];
         const uint64_t key = item >> vshift;
         uint64_t prev = __shfl_up_sync(0xffffffffu, key, 1);
         uint64_t next = __shfl_down_sync(0xffffffffu, key, 1);
+        // lane 31's successor is lane 0 of the next step
+        uint64_t first_next = after_key;
+        if (j + 1 < kInitSteps) first_next = __shfl_sync(0xffffffffu, items[j + 1], 0) >> vshift;
         if (lane == 0) prev = carry_key;
-        if (lane == 31 && i + 1 < n) next = keys[i + 1] >> vshift;
+        if (lane == 31) next = first_next;
         const bool head = valid && (i == 0 || prev != key);
         const bool last = valid && (i + 1 >= n || next != key);
         const unsigned hm = __ballot_sync(0xffffffffu, head) & le_mask;
@@ -1799,7 +1813,9 @@ __global__ void partition_check_kernel(const uint32_t *__restrict__ bucket_of,
 constexpr uint64_t kPfCmpCap = 1ull << 16;  // symbols an exact sample comparison may read
 constexpr uint64_t kPfPivotCap = 1ull << 12;  // symbols a suffix-vs-pivot comparison may read
 constexpr uint32_t kPfTieMax = 64;          // largest run of equal sample keys sorted exactly
-constexpr uint32_t kPfEllCap = 1u << 15;    // window offsets are capped (any prefix length works)
+constexpr uint32_t kPfEllCap = 0xFFFFu;     // window offsets are capped (any prefix length works)
+constexpr uint32_t kPfTrainSamples = 16384;  // learned model: training samples (of the sorted sample)
+constexpr int kPfTrainSteps = 32;            // Adam steps after the interpolating start
 
 // Comparison key of a suffix on its first spw symbols: the packed window,
 // truncated at the limit and padded low (ShorterFirst) or high
@@ -1877,7 +1893,7 @@ __global__ void pf_pivot_kernel(const uint32_t *__restrict__ spos, uint32_t ns, 
 // Key-window offset of every bucket: the common prefix of its two pivots
 // (0 for the first and last buckets, which have one pivot), capped.
 __global__ void pf_ell_kernel(const uint32_t *__restrict__ ppos, const uint64_t *__restrict__ plim,
-                              uint32_t p, Packed P, uint32_t *__restrict__ ell) {
+                              uint32_t p, Packed P, uint16_t *__restrict__ ell) {
     for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < p; b += gridDim.x * blockDim.x) {
         uint64_t t = 0;
         if (b > 0 && b + 1 < p) {
@@ -1894,7 +1910,32 @@ __global__ void pf_ell_kernel(const uint32_t *__restrict__ ppos, const uint64_t 
             }
             if (t > lim) t = lim;
         }
-        ell[b] = (uint32_t)t;
+        ell[b] = (uint16_t)t;
+    }
+}
+
+// Top-bits index of the pivot keys: tbl[t] = the number of pivots whose
+// key's top kPfTableBits bits are below t (t = 0 .. 2^kPfTableBits), so the
+// pivots a key can fall between are [tbl[top], tbl[top + 1]).
+constexpr int kPfTableBits = 12;
+__global__ void pf_table_kernel(const uint64_t *__restrict__ pkey, uint32_t n_piv,
+                                uint16_t *__restrict__ tbl) {
+    const uint32_t nt = (1u << kPfTableBits) + 1;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = n_piv;
+        if (t >= (1u << kPfTableBits)) {
+            lo = n_piv;
+        } else {
+            const uint64_t key = (uint64_t)t << (64 - kPfTableBits);
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (pkey[mid] < key)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+        }
+        tbl[t] = (uint16_t)lo;
     }
 }
 
@@ -1913,22 +1954,26 @@ __global__ void __launch_bounds__(kKeyThreads)
     pf_key_kernel(Packed P, uint64_t n, DevLimits L, int k, int lbits, int flag_len, int vbits,
                   int lf, int n_passes, int bucket_shift, const uint64_t *__restrict__ pkey,
                   const uint32_t *__restrict__ ppos, const uint64_t *__restrict__ plim,
-                  const uint32_t *__restrict__ ell, uint32_t p, const __nv_bfloat16 *__restrict__ w,
+                  const uint16_t *__restrict__ ell, const uint16_t *__restrict__ tbl, uint32_t p,
+                  const __nv_bfloat16 *__restrict__ w,
                   uint64_t *__restrict__ keys, uint32_t *__restrict__ counts,
                   unsigned long long *__restrict__ sizes, unsigned long long *__restrict__ stats,
                   int *__restrict__ fallback) {
     extern __shared__ __align__(16) unsigned char pfs[];
     const uint32_t n_piv = p - 1;
-    uint64_t *sk = reinterpret_cast<uint64_t *>(pfs);    // n_piv pivot keys
-    uint32_t *sell = reinterpret_cast<uint32_t *>(sk + n_piv);  // p offsets
-    uint32_t *bh = sell + p;                              // p bucket counts
-    uint32_t *hist = bh + p;                              // 8 * 256 digit counts
-    __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(hist + 8 * 256);
+    constexpr uint32_t kTbl = (1u << kPfTableBits) + 1;
+    uint64_t *sk = reinterpret_cast<uint64_t *>(pfs);           // n_piv pivot keys
+    uint32_t *bh = reinterpret_cast<uint32_t *>(sk + n_piv);    // p bucket counts
+    uint32_t *hist = bh + p;                                     // 8 * 256 digit counts
+    uint16_t *sell = reinterpret_cast<uint16_t *>(hist + 8 * 256);  // p window offsets
+    uint16_t *stbl = sell + p;                                   // kTbl top-bits index
+    __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(stbl + kTbl + 1);
     for (uint32_t j = threadIdx.x; j < n_piv; j += kKeyThreads) sk[j] = pkey[j];
     for (uint32_t j = threadIdx.x; j < p; j += kKeyThreads) {
         sell[j] = ell[j];
         bh[j] = 0;
     }
+    for (uint32_t j = threadIdx.x; j < kTbl; j += kKeyThreads) stbl[j] = tbl[j];
     for (int i = threadIdx.x; i < 8 * 256; i += kKeyThreads) hist[i] = 0;
     if (LEARNED)
         for (int j = threadIdx.x; j < cdf::kParams; j += kKeyThreads) sw[j] = w[j];
@@ -1956,17 +2001,49 @@ __global__ void __launch_bounds__(kKeyThreads)
         };
         uint32_t bk;
         if (LEARNED) {
+            // the model's guess, checked against its two neighbouring pivots;
+            // a wrong guess gallops away from it and bisects the bracket
             const float y = cdf::infer_bf16(sw, K);
             float g = floorf(y * (float)p);
             g = g < 0.0f ? 0.0f : (g > (float)n_piv ? (float)n_piv : g);
-            bk = (uint32_t)g;
-            const uint32_t guess = bk;
-            while (bk > 0 && !greater(bk - 1)) bk--;
-            if (bk == guess)
-                while (bk < n_piv && greater(bk)) bk++;
+            const uint32_t guess = (uint32_t)g;
+            uint32_t lo, hi;  // the bucket lies in [lo, hi]
+            if (guess > 0 && !greater(guess - 1)) {  // below the guess
+                hi = guess - 1;
+                uint32_t d = 1;
+                for (;;) {
+                    if (hi < d) { lo = 0; break; }
+                    const uint32_t j = hi - d;  // pivot j: is the suffix above it?
+                    if (greater(j)) { lo = j + 1; break; }
+                    hi = j;
+                    d *= 2;
+                }
+            } else if (guess < n_piv && greater(guess)) {  // above the guess
+                lo = guess + 1;
+                uint32_t d = 1;
+                for (;;) {
+                    if (lo + d - 1 >= n_piv) { hi = n_piv; break; }
+                    const uint32_t j = lo + d - 1;
+                    if (!greater(j)) { hi = j; break; }
+                    lo = j + 1;
+                    d *= 2;
+                }
+            } else {
+                lo = hi = guess;
+            }
+            while (lo < hi) {  // first pivot the suffix is not above
+                const uint32_t mid = (lo + hi) >> 1;
+                if (greater(mid))
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            bk = lo;
             mis += bk != guess ? 1u : 0u;
         } else {
-            uint32_t lo = 0, hi = n_piv;
+            // binary search between the pivots that share the key's top bits
+            const uint32_t top = (uint32_t)(K >> (64 - kPfTableBits));
+            uint32_t lo = stbl[top], hi = stbl[top + 1];
             while (lo < hi) {
                 const uint32_t mid = (lo + hi) >> 1;
                 if (greater(mid))
@@ -2136,7 +2213,8 @@ capssa_status pf_keys(Ctx &c, const EngineArgs &a, const eng::Packed &P, const K
     uint64_t *pkey = (uint64_t *)carve((size_t)p * 8);
     uint32_t *ppos = (uint32_t *)carve((size_t)p * 4);
     uint64_t *plim = (uint64_t *)carve((size_t)p * 8);
-    uint32_t *ell = (uint32_t *)carve((size_t)p * 4);
+    uint16_t *ell = (uint16_t *)carve((size_t)p * 2);
+    uint16_t *tbl = (uint16_t *)carve(((size_t)1 << kPfTableBits) * 2 + 16);
     unsigned long long *sizes = (unsigned long long *)carve(((size_t)p + 4) * 8);
     uint64_t *tx = (uint64_t *)carve((size_t)65536 * 8);
     float *tt = (float *)carve((size_t)65536 * 4);
@@ -2169,9 +2247,12 @@ capssa_status pf_keys(Ctx &c, const EngineArgs &a, const eng::Packed &P, const K
     CAPSSA_LAUNCHED(c);
     pf_ell_kernel<<<grid_for(p, 256), 256, 0, c.stream>>>(ppos, plim, p, P, ell);
     CAPSSA_LAUNCHED(c);
+    pf_table_kernel<<<grid_for((1u << kPfTableBits) + 1, 256), 256, 0, c.stream>>>(pkey, p - 1,
+                                                                                    tbl);
+    CAPSSA_LAUNCHED(c);
     // 3. the learned CDF model on the sorted sample
     if (pf->learned) {
-        const uint32_t tn = std::min<uint32_t>(ns, 65536);
+        const uint32_t tn = std::min<uint32_t>(ns, kPfTrainSamples);
         const uint32_t stride = (ns + tn - 1) / tn;
         const uint32_t tn_eff = (ns + stride - 1) / stride;
         pf_train_set_kernel<<<grid_for(tn_eff, 256), 256, 0, c.stream>>>(
@@ -2182,7 +2263,7 @@ capssa_status pf_keys(Ctx &c, const EngineArgs &a, const eng::Packed &P, const K
         cudaEventCreate(&t1);
         cudaEventRecord(t0, c.stream);
         float loss = 0.0f;
-        s = cdf::train(c, tx, tt, tn_eff, 300, params, wbf, &loss);
+        s = cdf::train(c, tx, tt, tn_eff, kPfTrainSteps, params, wbf, &loss, /*knot_start=*/true);
         cudaEventRecord(t1, c.stream);
         cudaEventSynchronize(t1);
         float ms = 0.0f;
@@ -2198,7 +2279,8 @@ capssa_status pf_keys(Ctx &c, const EngineArgs &a, const eng::Packed &P, const K
     // histogram buffer: clear it for the records' digit counts)
     CAPSSA_CUDA(c, cudaMemsetAsync(counts, 0, radix::kMaxPasses * 256 * 4, c.stream));
     CAPSSA_CUDA(c, cudaMemsetAsync(sizes, 0, ((size_t)p + 4) * 8, c.stream));
-    const size_t smem = (size_t)(p - 1) * 8 + (size_t)p * 8 + 8 * 256 * 4 + cdf::kParams * 2 + 16;
+    const size_t smem = (size_t)(p - 1) * 8 + (size_t)p * 4 + 8 * 256 * 4 + (size_t)p * 2 +
+                        (((size_t)1 << kPfTableBits) + 2) * 2 + cdf::kParams * 2 + 16;
     const bool plain = !a.lim.segmented;
     const unsigned grid = std::min<unsigned>(grid_for(n, kKeyThreads), (unsigned)c.sm_count * 8);
     cudaEvent_t q0, q1;
@@ -2210,7 +2292,7 @@ capssa_status pf_keys(Ctx &c, const EngineArgs &a, const eng::Packed &P, const K
                              (int)smem);                                                          \
         pf_key_kernel<PL, LE><<<grid, kKeyThreads, smem, c.stream>>>(                             \
             P, n, a.lim, geo.k, geo.lbits, geo.flag_len, geo.vbits, lf, key_passes, geo.total,    \
-            pkey, ppos, plim, ell, p, wbf, keys, counts, sizes, sizes + p, fb);                    \
+            pkey, ppos, plim, ell, tbl, p, wbf, keys, counts, sizes, sizes + p, fb);               \
     } while (0)
     cudaEventRecord(q0, c.stream);
     if (plain && pf->learned)
