@@ -461,46 +461,58 @@ __global__ void short_write_kernel(const ShortList *__restrict__ S, uint32_t *__
     hd[S->slot[j]] = S->slot[j];
 }
 
-constexpr int kInitSteps = 16;                 // warp steps of 32 sorted records
-constexpr int kInitWarpSpan = 32 * kInitSteps;  // 512 consecutive records per warp
-constexpr int kInitTile = 8 * kInitWarpSpan;    // 4096 records per block of 256 threads
+constexpr int kInitPer = 16;  // sorted keys per thread in init_groups_kernel
+constexpr int kInitTile = 256 * kInitPer;
 
 // Group heads after the key sort, in SA order (hd[i] = first SA index of
 // i's group; equal heads == equal comparison so far); tied groups that need
 // more symbols become the first round's work (engine.cuh step 3 -> 4).
-// Each warp walks 512 consecutive sorted records, 32 at a time: neighbours
-// come by shuffles, group starts by a ballot of the heads (carried across
-// steps), so every record costs a fixed handful of instructions.  The
-// block's group ends are staged in shared memory and appended with one
-// global atomic per list.  The positions riding below the keys are unpacked
-// into sa_out (segment-local ones rebased), and the short suffixes of a
-// flagless sort shift every record after their insertion points.
+// A block stages its 256 * kInitPer sorted keys (and their neighbours) in
+// shared memory once, unpacks the positions when they ride below the keys,
+// and appends its groups with one atomic per list (per-list counts packed
+// as 16-bit fields, 4096 keys per block at most).
 __global__ void __launch_bounds__(256)
     init_groups_kernel(const uint64_t *__restrict__ keys, uint32_t n, int k, uint64_t lmask,
                        int lf, int flag_len, int vshift, uint32_t *__restrict__ hd,
                        uint32_t *__restrict__ sa_out, GroupLists G,
                        const ShortList *__restrict__ S, int seg_at,
                        const uint64_t *__restrict__ seg_ends) {
-    __shared__ uint4 s_pend[kInitTile / 2 + 1];  // (start, len, depth, list << 16 | index in list)
-    __shared__ uint32_t s_npend, s_cnt[kLists], s_base[kLists];
-    __shared__ uint32_t s_shift[2];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t bbase = blockIdx.x * (uint32_t)kInitTile;
-    const uint32_t bvalid = n - bbase < (uint32_t)kInitTile ? n - bbase : (uint32_t)kInitTile;
+    static_assert(kLists <= 8, "two packed words of four 16-bit counters");
+    __shared__ uint64_t sk[kInitTile + 2];  // sk[l + 1] = key of sorted index base + l
+    __shared__ uint32_t s_base[kLists];
+    const uint32_t base = blockIdx.x * (uint32_t)kInitTile;
+    const uint32_t valid = n - base < (uint32_t)kInitTile ? n - base : (uint32_t)kInitTile;
     const uint64_t vmask = (1ull << vshift) - 1;
     // SA index of sorted record i: i + (short suffixes inserted at or before
     // it), one shift for the whole block unless an insertion falls inside
+    __shared__ uint32_t s_shift[2];
     const uint32_t ns = S ? __ldg(&S->n) : 0u;
     if (threadIdx.x == 0) {
-        const uint32_t lo = ns ? short_shift(S, ns, bbase) : 0u;
+        const uint32_t lo = ns ? short_shift(S, ns, base) : 0u;
         s_shift[0] = lo;
-        s_shift[1] = !ns || short_shift(S, ns, bbase + bvalid - 1) == lo;
-        s_npend = 0;
+        s_shift[1] = !ns || short_shift(S, ns, base + valid - 1) == lo;
     }
-    if (threadIdx.x < kLists) s_cnt[threadIdx.x] = 0;
     __syncthreads();
     const uint32_t sh_lo = s_shift[0];
     const bool sh_flat = s_shift[1] != 0;
+    auto shift_of = [&](uint32_t i) { return sh_flat ? sh_lo : short_shift(S, ns, i); };
+    for (uint32_t l = threadIdx.x; l < valid; l += 256) {
+        const uint64_t item = keys[base + l];
+        sk[l + 1] = item >> vshift;
+        if (sa_out) {
+            // segment-local positions (seg_at > 0): the segment index above
+            // the key gives the segment's first position
+            uint64_t pos = item & vmask;
+            if (seg_at) {
+                const uint64_t sg = item >> seg_at;
+                pos += sg ? __ldg(seg_ends + sg - 1) : 0ull;
+            }
+            sa_out[base + l + shift_of(base + l)] = (uint32_t)pos;
+        }
+    }
+    if (threadIdx.x == 0) sk[0] = base > 0 ? keys[base - 1] >> vshift : 0ull;
+    if (threadIdx.x == 32) sk[valid + 1] = base + valid < n ? keys[base + valid] >> vshift : 0ull;
+    __syncthreads();
     // tie state of a key: complete (equal through both ends: nothing to
     // refine), and the depth its group's members are known to agree on
     // (0 for the early-ended suffixes of a flagged plain text)
@@ -518,121 +530,88 @@ __global__ void __launch_bounds__(256)
             depth = (uint64_t)k;
         }
     };
+    // first sorted index of the run of `key` that holds local index l
+    auto head_of = [&](uint32_t l, uint64_t key) -> uint32_t {
+        uint32_t m = l;
+        int steps = 0;
+        while (m > 0 && steps < 32 && sk[m] == key) {  // sk[m] = key of local m - 1
+            m--;
+            steps++;
+        }
+        if (steps < 32 && (m > 0 || base == 0 || sk[0] != key)) return base + m;
+        return run_head(keys, 0, base + m, key, vshift);  // long run or one that began earlier
+    };
+    uint64_t cnt_lo = 0, cnt_hi = 0;  // 16-bit counts: lists 0..3, lists 4..
+    uint32_t ends = 0;                 // bit j: key j ends a group that needs refining
     // only LongerFirst with a length field separates complete ties by position
     const bool lf_field = lf && !flag_len;
-    const uint32_t wbase = bbase + (uint32_t)warp * kInitWarpSpan;
-    const unsigned le_mask = 0xFFFFFFFFu >> (31 - lane);  // lanes <= this one
-    const unsigned lt_mask = (1u << lane) - 1u;
-    uint64_t carry_key = 0;   // key of the record before this step
-    uint32_t carry_start = 0;  // start of the group that record belongs to
-    if (wbase < n && wbase > 0) {
-        carry_key = keys[wbase - 1] >> vshift;
-        const uint64_t k0 = keys[wbase] >> vshift;
-        carry_start = carry_key == k0 ? run_head(keys, 0, wbase - 1, carry_key, vshift) : wbase;
-    }
-    // every step's record first (16 loads in flight per lane), and the
-    // record after the warp's span for the last step's lane 31
-    uint64_t items[kInitSteps];
-#pragma unroll
-    for (int j = 0; j < kInitSteps; j++) {
-        const uint32_t i = wbase + (uint32_t)j * 32 + (uint32_t)lane;
-        items[j] = i < n ? keys[i] : 0ull;
-    }
-    const uint32_t after = wbase + kInitWarpSpan;
-    const uint64_t after_key = after < n ? keys[after] >> vshift : 0ull;
-#pragma unroll
-    for (int j = 0; j < kInitSteps; j++) {
-        const uint32_t sbase = wbase + (uint32_t)j * 32;
-        if (sbase >= n) break;  // warp-uniform
-        const uint32_t i = sbase + (uint32_t)lane;
-        const bool valid = i < n;
-        const uint64_t item = items[j];
-        const uint64_t key = item >> vshift;
-        uint64_t prev = __shfl_up_sync(0xffffffffu, key, 1);
-        uint64_t next = __shfl_down_sync(0xffffffffu, key, 1);
-        // lane 31's successor is lane 0 of the next step
-        uint64_t first_next = after_key;
-        if (j + 1 < kInitSteps) first_next = __shfl_sync(0xffffffffu, items[j + 1], 0) >> vshift;
-        if (lane == 0) prev = carry_key;
-        if (lane == 31) next = first_next;
-        const bool head = valid && (i == 0 || prev != key);
-        const bool last = valid && (i + 1 >= n || next != key);
-        const unsigned hm = __ballot_sync(0xffffffffu, head) & le_mask;
-        const uint32_t start = hm ? sbase + (uint32_t)(31 - __clz((int)hm)) : carry_start;
-        carry_start = __shfl_sync(0xffffffffu, start, 31);
-        carry_key = __shfl_sync(0xffffffffu, key, 31);
-        const uint32_t sh = sh_flat ? sh_lo : (valid ? short_shift(S, ns, i) : 0u);
-        bool end_here = false;
-        uint4 ent = make_uint4(0, 0, 0, 0);
-        int li = -1;
-        if (valid) {
-            if (sa_out) {
-                // segment-local positions (seg_at > 0): the segment index
-                // above the key gives the segment's first position
-                uint64_t pos = item & vmask;
-                if (seg_at) {
-                    const uint64_t sg = item >> seg_at;
-                    pos += sg ? __ldg(seg_ends + sg - 1) : 0ull;
-                }
-                sa_out[i + sh] = (uint32_t)pos;
-            }
-            if (head && last) {
-                hd[i + sh] = i + sh;
+    // pass 1: heads, and the groups this thread ends (singletons, the bulk,
+    // take the shortest path)
+#pragma unroll 4
+    for (int j = 0; j < kInitPer; j++) {
+        const uint32_t l = j * 256 + threadIdx.x;
+        if (l >= valid) break;
+        const uint32_t i = base + l;
+        const uint64_t key = sk[l + 1];
+        const bool head = (i == 0) || sk[l] != key;
+        const bool last = (i == n - 1) || sk[l + 2] != key;
+        // an insertion point only ever falls on a group head, so a group
+        // moves by one shift
+        const uint32_t sh = shift_of(i);
+        if (head && last) {
+            hd[i + sh] = i + sh;
+            continue;
+        }
+        const uint32_t g = head ? i : head_of(l, key);
+        bool complete = false;
+        uint64_t depth = (uint64_t)k;
+        if (lf_field || (last && !head)) state(key, complete, depth);
+        hd[i + sh] = ((complete && lf) ? i : g) + sh;
+        if (!complete && last && !head) {
+            const int li = list_of(i - g + 1, depth);
+            if (li == kLists) {
+                append_big(G, 0, g + sh, i - g + 1);
             } else {
-                bool complete = false;
-                uint64_t depth = (uint64_t)k;
-                if (lf_field || last) state(key, complete, depth);
-                hd[i + sh] = ((complete && lf) ? i : start) + sh;
-                if (last && !complete) {
-                    // an insertion point only ever falls on a group head, so
-                    // a group moves by one shift
-                    const uint32_t len = i - start + 1;
-                    li = list_of(len, depth);
-                    if (li == kLists) {
-                        append_big(G, 0, start + sh, len);
-                        li = -1;
-                    } else {
-                        end_here = true;
-                        ent = group_entry(start + sh, len, depth);
-                    }
-                }
-            }
-        }
-        // stage this step's group ends: one shared atomic per warp and list
-        const unsigned em = __ballot_sync(0xffffffffu, end_here);
-        if (em) {
-            uint32_t pbase = 0;
-            if (lane == 0) pbase = atomicAdd(&s_npend, (uint32_t)__popc(em));
-            pbase = __shfl_sync(0xffffffffu, pbase, 0);
-            uint32_t lidx = 0;
-#pragma unroll
-            for (int q = 0; q < kLists; q++) {
-                const unsigned qm = __ballot_sync(0xffffffffu, li == q);
-                if (qm) {
-                    uint32_t qb = 0;
-                    const int leader = __ffs((int)qm) - 1;
-                    if (lane == leader) qb = atomicAdd(&s_cnt[q], (uint32_t)__popc(qm));
-                    qb = __shfl_sync(0xffffffffu, qb, leader);
-                    if (li == q) lidx = qb + (uint32_t)__popc(qm & lt_mask);
-                }
-            }
-            if (end_here) {
-                ent.w = ((uint32_t)li << 16) | lidx;
-                s_pend[pbase + (uint32_t)__popc(em & lt_mask)] = ent;
+                if (li < 4)
+                    cnt_lo += 1ull << (16 * li);
+                else
+                    cnt_hi += 1ull << (16 * (li - 4));
+                ends |= 1u << j;
             }
         }
     }
+    uint64_t off_lo, off_hi;
+    const uint64_t tot_lo = block_excl_scan64(cnt_lo, &off_lo);
+    const uint64_t tot_hi = block_excl_scan64(cnt_hi, &off_hi);
+    if (threadIdx.x < kLists) {
+        const int li = (int)threadIdx.x;
+        const uint32_t total =
+            (uint32_t)(((li < 4 ? tot_lo : tot_hi) >> (16 * (li & 3))) & 0xFFFFu);
+        if (total) s_base[li] = atomicAdd(&G.ctr->n[li][0], total);
+    }
     __syncthreads();
-    if (threadIdx.x < kLists && s_cnt[threadIdx.x])
-        s_base[threadIdx.x] = atomicAdd(&G.ctr->n[threadIdx.x][0], s_cnt[threadIdx.x]);
-    __syncthreads();
-    const uint32_t np = s_npend;
-    for (uint32_t e = threadIdx.x; e < np; e += 256) {
-        uint4 ent = s_pend[e];
-        const int q = (int)(ent.w >> 16);
-        const uint32_t slot = s_base[q] + (ent.w & 0xFFFFu);
-        ent.w = 0;
-        list_ptr(G, q, 0)[slot] = ent;
+    // pass 2: write the entries of the groups found in pass 1
+    for (; ends; ends &= ends - 1) {
+        const int j = __ffs((int)ends) - 1;
+        const uint32_t l = j * 256 + threadIdx.x;
+        const uint32_t i = base + l;
+        const uint64_t key = sk[l + 1];
+        bool complete;
+        uint64_t depth;
+        state(key, complete, depth);
+        const uint32_t g = head_of(l, key);
+        const int li = list_of(i - g + 1, depth);
+        uint32_t slot = 0;
+#pragma unroll
+        for (int q = 0; q < kLists; q++) {
+            if (li == q) {
+                uint64_t &off = q < 4 ? off_lo : off_hi;
+                const int sh = 16 * (q & 3);
+                slot = s_base[q] + (uint32_t)((off >> sh) & 0xFFFFu);
+                off += 1ull << sh;
+            }
+        }
+        list_ptr(G, li, 0)[slot] = group_entry(g + shift_of(i), i - g + 1, depth);
     }
 }
 
@@ -1982,102 +1961,150 @@ __global__ void __launch_bounds__(kKeyThreads)
     const int kbits = k * b;  // 1..63
     unsigned long long probes = 0, mis = 0;
     bool deep = false;
-    // consecutive threads take consecutive positions (coalesced record stores)
-    for (uint64_t q = (uint64_t)blockIdx.x * kKeyThreads + threadIdx.x; q < n;
-         q += (uint64_t)gridDim.x * kKeyThreads) {
-        const uint64_t lim = kPlain ? n - q : dev_lim_at(L, q);
-        const uint64_t K = prefix_key(P, q, lim, lf);
-        // suffix q > pivot j ?
-        auto greater = [&](uint32_t j) -> bool {
-            probes++;
-            const uint64_t pk = sk[j];
-            if (K != pk) return K > pk;
-            const uint32_t pj = __ldg(ppos + j);
-            if (pj == q) return false;  // the pivot itself
-            const int c =
-                direct_cmp(P, q, lim, pj, __ldg(plim + j), 0, kPfPivotCap, lf);
-            if (c == 2) deep = true;
-            return c == 1;
-        };
-        uint32_t bk;
-        if (LEARNED) {
-            // the model's guess, checked against its two neighbouring pivots;
-            // a wrong guess gallops away from it and bisects the bracket
-            const float y = cdf::infer_bf16(sw, K);
-            float g = floorf(y * (float)p);
-            g = g < 0.0f ? 0.0f : (g > (float)n_piv ? (float)n_piv : g);
-            const uint32_t guess = (uint32_t)g;
-            uint32_t lo, hi;  // the bucket lies in [lo, hi]
-            if (guess > 0 && !greater(guess - 1)) {  // below the guess
-                hi = guess - 1;
-                uint32_t d = 1;
-                for (;;) {
-                    if (hi < d) { lo = 0; break; }
-                    const uint32_t j = hi - d;  // pivot j: is the suffix above it?
-                    if (greater(j)) { lo = j + 1; break; }
-                    hi = j;
-                    d *= 2;
-                }
-            } else if (guess < n_piv && greater(guess)) {  // above the guess
-                lo = guess + 1;
-                uint32_t d = 1;
-                for (;;) {
-                    if (lo + d - 1 >= n_piv) { hi = n_piv; break; }
-                    const uint32_t j = lo + d - 1;
-                    if (!greater(j)) { hi = j; break; }
-                    lo = j + 1;
-                    d *= 2;
-                }
-            } else {
-                lo = hi = guess;
-            }
-            while (lo < hi) {  // first pivot the suffix is not above
-                const uint32_t mid = (lo + hi) >> 1;
-                if (greater(mid))
-                    lo = mid + 1;
-                else
-                    hi = mid;
-            }
-            bk = lo;
-            mis += bk != guess ? 1u : 0u;
-        } else {
-            // binary search between the pivots that share the key's top bits
-            const uint32_t top = (uint32_t)(K >> (64 - kPfTableBits));
-            uint32_t lo = stbl[top], hi = stbl[top + 1];
-            while (lo < hi) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (greater(mid))
-                    lo = mid + 1;
-                else
-                    hi = mid;
-            }
-            bk = lo;
-        }
-        atomicAdd(&bh[bk], 1u);
-        // window of k symbols after the bucket's common prefix
-        const uint64_t off = sell[bk];
-        const uint64_t rest = lim > off ? lim - off : 0;
-        const uint64_t bit = (q + off) * (uint64_t)b;
-        const uint64_t wi = bit >> 6;
-        const uint32_t sh = (uint32_t)(bit & 63);
-        const uint64_t w0 = __ldg(P.w + wi), w1 = __ldg(P.w + wi + 1);
-        uint64_t content = ((w0 << sh) | ((w1 >> 1) >> (63 - sh))) >> (64 - kbits);
-        int take = k;
-        if (rest < (uint64_t)k) {
-            take = (int)rest;
-            const uint64_t lowmask = (1ull << ((k - take) * b)) - 1;
-            content = lf ? (content | lowmask) : (content & ~lowmask);
-        }
-        const uint64_t field = flag_len ? (uint64_t)((take == k) != (lf != 0))
-                                        : (uint64_t)(lf ? k - take : take);
-        uint64_t rec =
-            (lbits ? (content << lbits) | field : content) | ((uint64_t)bk << bucket_shift);
-        const uint32_t rlo = (uint32_t)rec, rhi = (uint32_t)(rec >> 32);
+    // each thread takes kKeyPer consecutive positions, in three phases so
+    // that their loads overlap: prefix keys, buckets, then the windows after
+    // the buckets' common prefixes
+    for (uint64_t t0 = (uint64_t)blockIdx.x * kKeyTile; t0 < n;
+         t0 += (uint64_t)gridDim.x * kKeyTile) {
+        const uint64_t p0 = t0 + (uint64_t)threadIdx.x * kKeyPer;
+        if (p0 >= n) continue;
+        uint64_t K[kKeyPer], lim[kKeyPer];
 #pragma unroll
-        for (int ps = 0; ps < 8; ps++)
-            if (ps < n_passes)
-                atomicAdd(&hist[ps * 256 + (((ps < 4 ? rlo : rhi) >> (8 * (ps & 3))) & 255u)], 1u);
-        keys[q] = (rec << vbits) | q;
+        for (int e = 0; e < kKeyPer; e++) {
+            const uint64_t q = p0 + e < n ? p0 + e : n - 1;
+            lim[e] = kPlain ? n - q : dev_lim_at(L, q);
+            K[e] = prefix_key(P, q, lim[e], lf);
+        }
+        uint32_t bk[kKeyPer];
+#pragma unroll
+        for (int e = 0; e < kKeyPer; e++) {
+            const uint64_t q = p0 + e;
+            // suffix q > pivot j ?  (key order, an exact compare on key ties)
+            auto greater = [&](uint32_t j) -> bool {
+                probes++;
+                const uint64_t pk = sk[j];
+                if (K[e] != pk) return K[e] > pk;
+                const uint32_t pj = __ldg(ppos + j);
+                if (pj == q) return false;  // the pivot itself
+                const int c = direct_cmp(P, q, lim[e], pj, __ldg(plim + j), 0, kPfPivotCap, lf);
+                if (c == 2) deep = true;
+                return c == 1;
+            };
+            if (q >= n) {
+                bk[e] = 0;
+                continue;
+            }
+            if (LEARNED) {
+                // the model's guess, checked against its two neighbouring
+                // pivots; a wrong guess gallops away from it and bisects
+                const float y = cdf::infer_bf16(sw, K[e]);
+                float g = floorf(y * (float)p);
+                g = g < 0.0f ? 0.0f : (g > (float)n_piv ? (float)n_piv : g);
+                const uint32_t guess = (uint32_t)g;
+                uint32_t lo, hi;  // the bucket lies in [lo, hi]
+                if (guess > 0 && !greater(guess - 1)) {  // below the guess
+                    hi = guess - 1;
+                    uint32_t d = 1;
+                    for (;;) {
+                        if (hi < d) {
+                            lo = 0;
+                            break;
+                        }
+                        const uint32_t j = hi - d;
+                        if (greater(j)) {
+                            lo = j + 1;
+                            break;
+                        }
+                        hi = j;
+                        d *= 2;
+                    }
+                } else if (guess < n_piv && greater(guess)) {  // above the guess
+                    lo = guess + 1;
+                    uint32_t d = 1;
+                    for (;;) {
+                        if (lo + d - 1 >= n_piv) {
+                            hi = n_piv;
+                            break;
+                        }
+                        const uint32_t j = lo + d - 1;
+                        if (!greater(j)) {
+                            hi = j;
+                            break;
+                        }
+                        lo = j + 1;
+                        d *= 2;
+                    }
+                } else {
+                    lo = hi = guess;
+                }
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (greater(mid))
+                        lo = mid + 1;
+                    else
+                        hi = mid;
+                }
+                bk[e] = lo;
+                mis += lo != guess ? 1u : 0u;
+            } else {
+                // binary search between the pivots that share the key's top bits
+                const uint32_t top = (uint32_t)(K[e] >> (64 - kPfTableBits));
+                uint32_t lo = stbl[top], hi = stbl[top + 1];
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (greater(mid))
+                        lo = mid + 1;
+                    else
+                        hi = mid;
+                }
+                bk[e] = lo;
+            }
+        }
+        uint64_t out[kKeyPer];
+#pragma unroll
+        for (int e = 0; e < kKeyPer; e++) {
+            const uint64_t q = p0 + e;
+            uint64_t rec = 0;
+            if (q < n) {
+                atomicAdd(&bh[bk[e]], 1u);
+                // window of k symbols after the bucket's common prefix
+                const uint64_t off = sell[bk[e]];
+                const uint64_t rest = lim[e] > off ? lim[e] - off : 0;
+                const uint64_t bit = (q + off) * (uint64_t)b;
+                const uint64_t wi = bit >> 6;
+                const uint32_t sh = (uint32_t)(bit & 63);
+                const uint64_t w0 = __ldg(P.w + wi), w1 = __ldg(P.w + wi + 1);
+                uint64_t content = ((w0 << sh) | ((w1 >> 1) >> (63 - sh))) >> (64 - kbits);
+                int take = k;
+                if (rest < (uint64_t)k) {
+                    take = (int)rest;
+                    const uint64_t lowmask = (1ull << ((k - take) * b)) - 1;
+                    content = lf ? (content | lowmask) : (content & ~lowmask);
+                }
+                const uint64_t field = flag_len ? (uint64_t)((take == k) != (lf != 0))
+                                                : (uint64_t)(lf ? k - take : take);
+                rec = (lbits ? (content << lbits) | field : content) |
+                      ((uint64_t)bk[e] << bucket_shift);
+                const uint32_t rlo = (uint32_t)rec, rhi = (uint32_t)(rec >> 32);
+#pragma unroll
+                for (int ps = 0; ps < 8; ps++)
+                    if (ps < n_passes)
+                        atomicAdd(&hist[ps * 256 + (((ps < 4 ? rlo : rhi) >> (8 * (ps & 3))) & 255u)],
+                                  1u);
+                rec = (rec << vbits) | q;
+            }
+            out[e] = rec;
+        }
+        if (p0 + kKeyPer <= n) {
+            uint4 *dst = reinterpret_cast<uint4 *>(keys + p0);
+#pragma unroll
+            for (int e = 0; e < kKeyPer; e += 2)
+                dst[e / 2] = make_uint4((uint32_t)out[e], (uint32_t)(out[e] >> 32),
+                                        (uint32_t)out[e + 1], (uint32_t)(out[e + 1] >> 32));
+        } else {
+            for (int e = 0; e < kKeyPer; e++)
+                if (p0 + e < n) keys[p0 + e] = out[e];
+        }
     }
     if (deep) atomicExch(fallback, 1);
 #pragma unroll
@@ -2282,7 +2309,7 @@ capssa_status pf_keys(Ctx &c, const EngineArgs &a, const eng::Packed &P, const K
     const size_t smem = (size_t)(p - 1) * 8 + (size_t)p * 4 + 8 * 256 * 4 + (size_t)p * 2 +
                         (((size_t)1 << kPfTableBits) + 2) * 2 + cdf::kParams * 2 + 16;
     const bool plain = !a.lim.segmented;
-    const unsigned grid = std::min<unsigned>(grid_for(n, kKeyThreads), (unsigned)c.sm_count * 8);
+    const unsigned grid = std::min<unsigned>(grid_for(n, kKeyTile), (unsigned)c.sm_count * 8);
     cudaEvent_t q0, q1;
     cudaEventCreate(&q0);
     cudaEventCreate(&q1);
