@@ -116,7 +116,7 @@ class _Stats(C.Structure):
                 ("sort_pass_ms", C.c_double), ("partition_ms", C.c_double),
                 ("train_ms", C.c_double), ("partition_probes", C.c_uint64),
                 ("train_samples", C.c_uint32), ("model_loss", C.c_float),
-                ("radix_items", C.c_uint32), ("reserved1", C.c_uint32)]
+                ("radix_items", C.c_uint32), ("sparse_subset", C.c_uint32)]
 
 
 class _Packer(C.Structure):

@@ -234,6 +234,74 @@ __global__ void __launch_bounds__(kKeyThreads)
         if (hist[i]) atomicAdd(&counts[i], hist[i]);
 }
 
+// Composite key of each of m chosen positions (a subset sorted on its own):
+// the same record as key_kernel's, read at pos[i] (distinct, ascending,
+// < n), with the digit histograms of every radix pass.
+template <bool kPlain>
+__global__ void __launch_bounds__(kKeyThreads)
+    sparse_key_kernel(Packed P, uint64_t n, const uint32_t *__restrict__ pos, uint64_t m,
+                      DevLimits L, int k, int lbits, int flag_len, int vbits, int lf,
+                      int n_passes, uint64_t *__restrict__ keys, uint32_t *__restrict__ counts) {
+    __shared__ uint32_t hist[8 * 256];
+    for (int i = threadIdx.x; i < n_passes * 256; i += kKeyThreads) hist[i] = 0;
+    __syncthreads();
+    const int b = P.b;
+    const int kbits = k * b;
+    for (uint64_t i = blockIdx.x * (uint64_t)kKeyThreads + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * kKeyThreads) {
+        const uint64_t p = pos[i];
+        const uint64_t lim = kPlain ? n - p : dev_lim_at(L, p);
+        const uint64_t bit = p * (uint64_t)b;
+        const uint64_t wi = bit >> 6;
+        const uint32_t sh = (uint32_t)(bit & 63);
+        const uint64_t w0 = __ldg(P.w + wi), w1 = __ldg(P.w + wi + 1);
+        uint64_t content = ((w0 << sh) | ((w1 >> 1) >> (63 - sh))) >> (64 - kbits);
+        int take = k;
+        if (lim < (uint64_t)k) {
+            take = (int)lim;
+            const uint64_t lowmask = (1ull << ((k - take) * b)) - 1;
+            content = lf ? (content | lowmask) : (content & ~lowmask);
+        }
+        const uint64_t field = flag_len ? (uint64_t)((take == k) != (lf != 0))
+                                        : (uint64_t)(lf ? k - take : take);
+        uint64_t key = lbits ? (content << lbits) | field : content;
+        const uint32_t lo = (uint32_t)key, hi = (uint32_t)(key >> 32);
+#pragma unroll
+        for (int ps = 0; ps < 8; ps++)
+            if (ps < n_passes)
+                atomicAdd(&hist[ps * 256 + (((ps < 4 ? lo : hi) >> (8 * (ps & 3))) & 255u)], 1u);
+        if (vbits) key = (key << vbits) | p;
+        keys[i] = key;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n_passes * 256; i += kKeyThreads)
+        if (hist[i]) atomicAdd(&counts[i], hist[i]);
+}
+
+// Population count of every bitmap word (the chosen positions per word).
+__global__ void bits_popc_kernel(const uint32_t *__restrict__ bits, uint64_t nw,
+                                 uint32_t *__restrict__ cnt) {
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nw;
+         w += (uint64_t)gridDim.x * blockDim.x)
+        cnt[w] = (uint32_t)__popc(bits[w]);
+}
+
+// The set bits of the bitmap as ascending positions (incl = inclusive prefix
+// of the word counts).
+__global__ void bits_expand_kernel(const uint32_t *__restrict__ bits, uint64_t nw,
+                                   const uint32_t *__restrict__ incl, uint32_t *__restrict__ pos) {
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nw;
+         w += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t x = bits[w];
+        uint32_t o = incl[w] - (uint32_t)__popc(x);
+        while (x) {
+            const int j = __ffs((int)x) - 1;
+            pos[o++] = (uint32_t)(w * 32 + (uint64_t)j);
+            x &= x - 1;
+        }
+    }
+}
+
 // ---------------------------------------------------------------- groups
 
 // First index of the run of `key` that contains sorted index i.
@@ -2193,6 +2261,14 @@ inline int bits_for(uint64_t v) {  // bits to represent 0..v
     return b == 0 ? 1 : b;
 }
 
+// A subset sorted on its own (records for the m chosen positions only,
+// instead of the whole text): the positions, distinct and ascending.
+struct SparseRun {
+    const uint32_t *pos = nullptr;  // device, m positions < n
+    uint64_t m = 0;
+    bool fell_back = false;  // out: a tied group needs rank doubling; nothing returned
+};
+
 // Request and outcome of a partition-first core_sort (the sample sort's
 // buckets computed before the sort and leading its records).
 struct PfRun {
@@ -2352,7 +2428,7 @@ capssa_status pf_keys(Ctx &c, const EngineArgs &a, const eng::Packed &P, const K
 // records lead with the sample sort's bucket (partition first).
 template <typename S>
 capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Packed *pk_out,
-                        PfRun *pf = nullptr) {
+                        PfRun *pf = nullptr, SparseRun *sp = nullptr) {
     using namespace eng;
     const uint64_t n = a.n;
     const int lf = a.lim.longer_first;
@@ -2447,7 +2523,7 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     c.seg_major_done = a.seg_major && (seg_bits > 0 || a.lim.n_ends <= 1);
     // a ShorterFirst plain text may drop the early-end flag when that saves a
     // radix pass
-    const bool allow_flagless = !a.lim.segmented && !lf && n <= 0xFFFFFFFEull && !pf;
+    const bool allow_flagless = !a.lim.segmented && !lf && n <= 0xFFFFFFFEull && !pf && !sp;
     KeyGeom geo;
     if (pf) {  // the bucket index leads the record
         seg_bits = bits_for(pf->p - 1);
@@ -2457,24 +2533,28 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
             return CAPSSA_OK;
         }
     } else {
-        geo = key_geom(b, n, !a.lim.segmented, hbits, seg_bits, seg_bits ? a.seg_max_len : 0,
-                       allow_flagless);
+        geo = key_geom(b, n, !a.lim.segmented, hbits, seg_bits,
+                       seg_bits ? a.seg_max_len : (sp ? sp->m : 0), allow_flagless);
     }
     // records the radix sort orders: every suffix, or the full ones only
     const uint64_t n_short = geo.flagless ? (uint64_t)geo.k - 1 : 0;
-    const uint64_t n_rec = n - n_short;
+    // suffixes in the output: every position, or the chosen subset's
+    const uint64_t N = sp ? sp->m : n;
+    const uint64_t n_rec = N - n_short;
     const int sort_bits = geo.total + seg_bits;
     c.stats.key_symbols = geo.k;
     c.stats.key_bits_per_symbol = geo.b;
 
     // ---- 2+3. composite keys of every position, stable radix sort
-    const uint32_t nn = (uint32_t)n;
-    uint64_t *keys_a = (uint64_t *)ws_get(c, WS_KEYS_A, (size_t)n * 8);
-    uint64_t *keys_b = (uint64_t *)ws_get(c, WS_KEYS_B, (size_t)n * 8);
-    uint32_t *vals_a = (uint32_t *)ws_get(c, WS_VALS_A, (size_t)n * 4);
-    uint32_t *vals_b = (uint32_t *)ws_get(c, WS_VALS_B, (size_t)n * 4);
-    uint32_t *rank = (uint32_t *)ws_get(c, WS_RANK, (size_t)n * 4 + 64);
-    uint64_t *key2 = (uint64_t *)ws_get(c, WS_KEY2, (size_t)n * 8);
+    const uint32_t nn = (uint32_t)N;
+    uint64_t *keys_a = (uint64_t *)ws_get(c, WS_KEYS_A, (size_t)N * 8);
+    uint64_t *keys_b = (uint64_t *)ws_get(c, WS_KEYS_B, (size_t)N * 8);
+    uint32_t *vals_a = (uint32_t *)ws_get(c, WS_VALS_A, (size_t)N * 4);
+    uint32_t *vals_b = (uint32_t *)ws_get(c, WS_VALS_B, (size_t)N * 4);
+    // position-indexed ranks: only rank doubling reads them, which a subset
+    // sorted on its own never reaches
+    uint32_t *rank = (uint32_t *)ws_get(c, WS_RANK, (size_t)(sp ? 1 : n) * 4 + 64);
+    uint64_t *key2 = (uint64_t *)ws_get(c, WS_KEY2, (size_t)N * 8);
     if (!keys_a || !keys_b || !vals_a || !vals_b || !rank || !key2)
         return set_err(c, CAPSSA_ENOMEM, "suffix-sort workspace");
     Coder<S> coder{table, minv};
@@ -2507,6 +2587,20 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     if (pf) {
         capssa_status s0 = pf_keys<S>(c, a, P, geo, seg_bits, key_passes, keys_a, counts, pf);
         if (s0 != CAPSSA_OK || pf->fell_back) return s0;
+    } else if (sp) {
+        const unsigned sg = std::min<unsigned>(grid_for(N, kKeyThreads), c.sm_count * 8);
+        if (!a.lim.segmented)
+            sparse_key_kernel<true><<<sg, kKeyThreads, 0, c.stream>>>(
+                P, n, sp->pos, N, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf, key_passes,
+                keys_a, counts);
+        else
+            sparse_key_kernel<false><<<sg, kKeyThreads, 0, c.stream>>>(
+                P, n, sp->pos, N, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf, key_passes,
+                keys_a, counts);
+        CAPSSA_LAUNCHED(c);
+        if (!vbits)  // the record's value is its position
+            CAPSSA_CUDA(c, cudaMemcpyAsync(vals_a, sp->pos, (size_t)N * 4, cudaMemcpyDeviceToDevice,
+                                           c.stream));
     } else if (!a.lim.segmented && !seg_bits) {
         key_kernel<true><<<kgrid, kKeyThreads, 0, c.stream>>>(
             P, n, n_rec, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf, key_passes, 0, 0,
@@ -2524,7 +2618,7 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     capssa_status s =
         vbits ? radix::sort_keys(c, keys_a, keys_b, (uint32_t)n_rec, vbits, vbits + sort_bits,
                                  &in_b, &passes, /*hist_ready=*/true)
-              : radix::sort_pairs(c, keys_a, vals_a, keys_b, vals_b, nn, 0, sort_bits, true, 0,
+              : radix::sort_pairs(c, keys_a, vals_a, keys_b, vals_b, nn, 0, sort_bits, !sp, 0,
                                   &in_b, &passes, /*hist_ready=*/true);
     if (s != CAPSSA_OK) return s;
     c.stats.sort_passes = (uint32_t)passes;
@@ -2541,14 +2635,14 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
 
     // ---- 4. tied groups: direct comparison while shallow, rank doubling when deep
     // list capacities from the smallest group each list can hold
-    const size_t cap_of[kLists] = {(size_t)n / 2 + 2,  (size_t)n / 3 + 2, (size_t)n / 9 + 2,
-                                   (size_t)n / 33 + 2, (size_t)n / 2 + 2, (size_t)n / 5 + 2};
-    const size_t big_cap = (size_t)n / (kSmallMax + 1) + 2;
+    const size_t cap_of[kLists] = {(size_t)N / 2 + 2,  (size_t)N / 3 + 2, (size_t)N / 9 + 2,
+                                   (size_t)N / 33 + 2, (size_t)N / 2 + 2, (size_t)N / 5 + 2};
+    const size_t big_cap = (size_t)N / (kSmallMax + 1) + 2;
     size_t list_bytes = 256 + big_cap * 16 * 2;
     for (int l = 0; l < kLists; l++) list_bytes += cap_of[l] * 16 * 2;
     GroupLists G;
     char *gl = (char *)ws_get(c, WS_GROUPS_A, list_bytes);
-    uint32_t *hd = (uint32_t *)ws_get(c, WS_GROUPS_B, (size_t)n * 4 + 64);
+    uint32_t *hd = (uint32_t *)ws_get(c, WS_GROUPS_B, (size_t)N * 4 + 64);
     if (!gl || !hd) return set_err(c, CAPSSA_ENOMEM, "group lists");
     G.ctr = (Counters *)gl;
     uint4 *cursor = (uint4 *)(gl + 256);
@@ -2606,6 +2700,10 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
                          cnt[L_TINY], cnt[L_TINY8], cnt[L_SMALL], cnt[L_MEDIUM], cnt[L_DEEP],
                          nb, big_total);
         if (!any && !nb) break;
+        if (sp && (nb || cnt[L_DEEP])) {  // deep ties: the subset needs the whole text's ranks
+            sp->fell_back = true;
+            return CAPSSA_OK;
+        }
         if (c.stats.refine_rounds >= 70)
             return set_err(c, CAPSSA_EINVAL, "rank doubling did not converge");
         c.stats.refine_rounds++;
@@ -3018,6 +3116,84 @@ inline capssa_status pf_report(Ctx &c, const EngineArgs &a, const PfRun &pf) {
     return CAPSSA_OK;
 }
 
+// Subsets far smaller than the text (m * kSparseRatio <= n) are sorted on
+// their own: the distinct chosen positions become records of their own and
+// go through the same radix sort and refinement, so the work is O(m) plus
+// one n / 8-byte bitmap.  Repeated positions, deep ties (a group needing
+// rank doubling) or any other case leave *res null and the caller sorts the
+// whole text instead.  On success *res holds the m positions in order (the
+// empty suffix n first under ShorterFirst, last under LongerFirst).
+constexpr uint64_t kSparseRatio = 8;
+
+template <typename S>
+capssa_status sparse_subset(Ctx &c, const EngineArgs &a, const uint32_t **res) {
+    using namespace eng;
+    *res = nullptr;
+    const uint64_t n = a.n, m = a.m;
+    const int lf = a.lim.longer_first;
+    const uint64_t nw = n / 32 + 1;
+    uint32_t *bits = const_cast<uint32_t *>(a.keep_bits);
+    unsigned long long n_empty = 0;
+    if (!bits) {
+        bits = (uint32_t *)ws_get(c, WS_KEEP, nw * 4 + 64);
+        if (!bits) return set_err(c, CAPSSA_ENOMEM, "subset bitmap");
+        int *fl = c.d_flags + 1;  // [0] beyond the end, [1] repeated
+        unsigned long long *cnt = (unsigned long long *)(c.d_flags + 4);
+        CAPSSA_CUDA(c, cudaMemsetAsync(fl, 0, 12 + 8, c.stream));
+        CAPSSA_CUDA(c, cudaMemsetAsync(bits, 0, nw * 4, c.stream));
+        const unsigned gb = std::min<unsigned>(grid_for(m, 256), (unsigned)c.sm_count * 8);
+        if (a.pos_bytes == 4)
+            subset_bits_kernel<uint32_t><<<gb, 256, 0, c.stream>>>((const uint32_t *)a.positions, m,
+                                                                   n, bits, fl, cnt);
+        else
+            subset_bits_kernel<uint64_t><<<gb, 256, 0, c.stream>>>((const uint64_t *)a.positions, m,
+                                                                   n, bits, fl, cnt);
+        CAPSSA_LAUNCHED(c);
+        int *h = (int *)c.h_scratch;
+        unsigned long long *h_cnt = (unsigned long long *)c.h_scratch + 2;
+        CAPSSA_CUDA(c, cudaMemcpyAsync(h, fl, 8, cudaMemcpyDeviceToHost, c.stream));
+        CAPSSA_CUDA(c, cudaMemcpyAsync(h_cnt, cnt, 8, cudaMemcpyDeviceToHost, c.stream));
+        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+        if (h[0]) return set_err(c, CAPSSA_EINVAL, "a position lies beyond the end of the text");
+        if (h[1] || *h_cnt > 1) return CAPSSA_OK;  // repeated positions: the whole-text path
+        n_empty = *h_cnt;
+    }
+    const uint64_t count = m - n_empty;  // chosen positions below n
+    if (count == 0) return CAPSSA_OK;
+    // the chosen positions, ascending (a stable sort then keeps every tie
+    // class in ascending position, as the whole-text path does)
+    uint32_t *wc = (uint32_t *)ws_get(c, WS_MISC, nw * 4 + 64);
+    uint32_t *pos = (uint32_t *)ws_get(c, WS_MISC2, count * 4 + 64);
+    if (!wc || !pos) return set_err(c, CAPSSA_ENOMEM, "subset positions");
+    bits_popc_kernel<<<grid_for(nw, 256), 256, 0, c.stream>>>(bits, nw, wc);
+    CAPSSA_LAUNCHED(c);
+    capssa_status s = scan_u32(c, wc, wc, nw, /*max_op=*/false, /*inclusive=*/true);
+    if (s != CAPSSA_OK) return s;
+    bits_expand_kernel<<<grid_for(nw, 256), 256, 0, c.stream>>>(bits, nw, wc, pos);
+    CAPSSA_LAUNCHED(c);
+    SparseRun sp;
+    sp.pos = pos;
+    sp.m = count;
+    uint32_t *sa = nullptr;
+    Packed P{};
+    s = core_sort<S>(c, a, &sa, &P, nullptr, &sp);
+    if (s != CAPSSA_OK || sp.fell_back) return s;
+    uint32_t *sv = (uint32_t *)ws_get(c, WS_MISC3, (size_t)m * 8 + 64);
+    if (!sv) return set_err(c, CAPSSA_ENOMEM, "subset workspace");
+    const uint64_t off = (n_empty && !lf) ? 1 : 0;
+    CAPSSA_CUDA(c, cudaMemcpyAsync(sv + off, sa, count * 4, cudaMemcpyDeviceToDevice, c.stream));
+    if (n_empty) {
+        uint32_t *hv = (uint32_t *)c.h_scratch;
+        *hv = (uint32_t)n;
+        CAPSSA_CUDA(c, cudaMemcpyAsync(sv + (lf ? m - 1 : 0), hv, 4, cudaMemcpyHostToDevice,
+                                       c.stream));
+        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));  // the pinned word is reused
+    }
+    c.stats.sparse_subset = 1;
+    *res = sv;
+    return CAPSSA_OK;
+}
+
 template <typename S>
 capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
     using namespace eng;
@@ -3033,6 +3209,12 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
 
     uint32_t *sa = nullptr;
     eng::Packed P{};
+    // a small subset sorted on its own
+    const uint32_t *sparse_res = nullptr;
+    if (subset && !a.part_p && !bounded && n > 0 && m * kSparseRatio <= n) {
+        capssa_status s = sparse_subset<S>(c, a, &sparse_res);
+        if (s != CAPSSA_OK) return s;
+    }
     // the sample sort with its partition ahead of the sort (whole texts,
     // unbounded context, at least two buckets)
     bool part_done = false;
@@ -3048,7 +3230,7 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
             part_done = true;
         }
     }
-    if (n > 0 && !part_done) {
+    if (n > 0 && !part_done && !sparse_res) {
         capssa_status s = core_sort<S>(c, a, &sa, &P);
         if (s != CAPSSA_OK) return s;
         if (bounded) {
@@ -3083,9 +3265,9 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
     if (!sv) return set_err(c, CAPSSA_ENOMEM, "subset workspace");
     uint32_t *sv_b = sv + m;
     const unsigned gm = grid_for(m, 256);
-    const uint32_t *res = nullptr;
+    const uint32_t *res = sparse_res;
     if (a.keep_bits && a.part_p) return set_err(c, CAPSSA_EINVAL, "no partition plan for a kept-bit set");
-    if (!a.part_p && n > 0) {
+    if (!res && !a.part_p && n > 0) {
         // distinct positions: mark them in a bitmap (L2-sized: n / 8 bytes)
         // and compact the full order, instead of sorting them by rank
         uint32_t *bits = (uint32_t *)ws_get(c, WS_KEYS_A, (size_t)n * 8);

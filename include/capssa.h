@@ -147,7 +147,7 @@ typedef struct capssa_stats {
     float model_loss;           /* learned partition: final mean squared CDF error */
     uint32_t radix_items;       /* records per thread of the radix passes (the context's
                                    autotuner picks it on its first large sort of each kind) */
-    uint32_t reserved1;
+    uint32_t sparse_subset;     /* 1: a subset build sorted only its own positions */
 } capssa_stats;
 
 typedef struct capssa_ctx capssa_ctx;

@@ -83,6 +83,31 @@ def test_c4_learned_sample_sort_2p28_bit_exact(ctx, c2):
         assert np.array_equal(sz, osz[:k])
 
 
+def test_c2_small_subset_2p28_sorted_alone(ctx, c2):
+    """2^16 positions of the 2^28-symbol text: sorted on their own, bit-exact,
+    in a small fraction of the whole-text build's device time."""
+    import torch
+    t, _ = c2
+    rng = np.random.default_rng(65)
+    pos = np.sort(rng.choice(len(t), size=1 << 16, replace=False)).astype(np.uint32)
+    want = orc.build_in_memory(t, pos)
+    got = ctx.build_in_memory_for_positions(t, pos)
+    assert ctx.stats()["sparse_subset"] == 1
+    assert np.array_equal(got, want)
+    td = torch.from_numpy(t).cuda()
+    pd = torch.from_numpy(pos.view(np.int32)).cuda()
+    out = torch.empty(len(pos), dtype=torch.int32, device="cuda")
+    full = torch.empty(len(t), dtype=torch.int32, device="cuda")
+    ctx.build_in_memory_for_positions(td, pd, out=out)
+    ctx.build_in_memory(td, out=full)
+    ctx.build_in_memory_for_positions(td, pd, out=out)
+    sub_ms = ctx.stats()["device_ms"]
+    ctx.build_in_memory(td, out=full)
+    full_ms = ctx.stats()["device_ms"]
+    print("subset of 2^16: %.2f ms, whole text: %.2f ms" % (sub_ms, full_ms))
+    assert sub_ms < full_ms / 4
+
+
 def test_c3_segmented_filtered_2p29(ctx, c3):
     text, ends, pos = c3
     n = len(text)

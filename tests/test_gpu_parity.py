@@ -568,3 +568,62 @@ def test_flagless_with_context_bound_and_lcp(ctx):
     assert np.array_equal(lcp[1:], ctx.lcp(t, sa[:-1], sa[1:]))
     keep = np.nonzero(rng.random(n) < 0.5)[0]
     check_against_oracle(ctx, t, positions=keep, index=np.uint64)
+
+
+# ---------------------------------------------------------------- subsets sorted on their own
+
+def _subset(rng, n, m, with_empty=False):
+    pos = rng.choice(n, size=m, replace=False).astype(np.uint64)
+    if with_empty:
+        pos = np.concatenate([pos, [n]]).astype(np.uint64)
+    return pos
+
+
+@pytest.mark.parametrize("index", [np.uint32, np.uint64])
+def test_small_subset_sorted_alone_bit_exact(ctx, index):
+    """m <= n / 8 distinct positions: only those suffixes are sorted (O(m)
+    records), bit-exact against the oracle, the empty suffix included."""
+    from capssa import workloads
+    t = workloads.dna_with_repeats(1 << 21, seed=61)
+    rng = np.random.default_rng(62)
+    pos = _subset(rng, len(t), 1 << 15, with_empty=True).astype(index)
+    got = ctx.build_in_memory_for_positions(t, pos)
+    assert ctx.stats()["sparse_subset"] == 1
+    want = orc.build_in_memory(t, pos, index=index)
+    assert np.array_equal(got, want)
+    # inside repeats: positions clustered in copies and their sources
+    pos2 = np.unique(np.concatenate([np.arange(5000, 9000), np.arange(700000, 720000)]))
+    got2 = ctx.build_in_memory_for_positions(t, pos2.astype(index))
+    assert ctx.stats()["sparse_subset"] == 1
+    assert np.array_equal(got2, orc.build_in_memory(t, pos2.astype(index), index=index))
+
+
+def test_small_subset_segments_both_orders(ctx):
+    rng = np.random.default_rng(63)
+    t = rng.integers(0, 4, 300000).astype(np.uint8)
+    ends = np.unique(np.concatenate([rng.integers(1, len(t), 2000), [len(t)]]))
+    pos = _subset(rng, len(t), 30000, with_empty=True)
+    check_against_oracle(ctx, t, positions=pos, ends=ends.tolist(), longer_first=True,
+                         index=np.uint64)
+    assert ctx.stats()["sparse_subset"] == 1
+    check_against_oracle(ctx, t, positions=pos, ends=ends.tolist(), index=np.uint64)
+    assert ctx.stats()["sparse_subset"] == 1
+
+
+def test_small_subset_falls_back_when_needed(ctx):
+    """Repeated positions, and suffixes inside a 100,000-symbol run (ties
+    deeper than the direct comparisons reach), take the whole-text path:
+    same output."""
+    rng = np.random.default_rng(64)
+    t = rng.integers(0, 4, 1 << 21).astype(np.uint8)
+    pos = _subset(rng, len(t), 1000)
+    dup = np.concatenate([pos, pos[:10]]).astype(np.uint64)
+    got = ctx.build_in_memory_for_positions(t, dup)
+    assert ctx.stats()["sparse_subset"] == 0
+    assert np.array_equal(got, orc.build_in_memory(t, dup, index=np.uint64))
+    t2 = t.copy()
+    t2[100000:200000] = 1
+    deep = np.arange(100000, 120000, dtype=np.uint64)
+    got = ctx.build_in_memory_for_positions(t2, deep)
+    assert ctx.stats()["sparse_subset"] == 0
+    assert np.array_equal(got, orc.build_in_memory(t2, deep, index=np.uint64))
