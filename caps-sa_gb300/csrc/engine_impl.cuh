@@ -2032,16 +2032,24 @@ __global__ void __launch_bounds__(kKeyThreads)
     // each thread takes kKeyPer consecutive positions, in three phases so
     // that their loads overlap: prefix keys, buckets, then the windows after
     // the buckets' common prefixes
+    cdf::MmaWeights MW;
+    if (LEARNED) MW = cdf::mma_weights(sw);
     for (uint64_t t0 = (uint64_t)blockIdx.x * kKeyTile; t0 < n;
          t0 += (uint64_t)gridDim.x * kKeyTile) {
+        // every lane stays in the loop (the model runs warp-wide); lanes past
+        // the end work on the last position and store nothing
         const uint64_t p0 = t0 + (uint64_t)threadIdx.x * kKeyPer;
-        if (p0 >= n) continue;
         uint64_t K[kKeyPer], lim[kKeyPer];
 #pragma unroll
         for (int e = 0; e < kKeyPer; e++) {
             const uint64_t q = p0 + e < n ? p0 + e : n - 1;
             lim[e] = kPlain ? n - q : dev_lim_at(L, q);
             K[e] = prefix_key(P, q, lim[e], lf);
+        }
+        float yp[kKeyPer];
+        if (LEARNED) {
+#pragma unroll
+            for (int e = 0; e < kKeyPer; e++) yp[e] = cdf::infer_mma(MW, K[e]);
         }
         uint32_t bk[kKeyPer];
 #pragma unroll
@@ -2065,8 +2073,7 @@ __global__ void __launch_bounds__(kKeyThreads)
             if (LEARNED) {
                 // the model's guess, checked against its two neighbouring
                 // pivots; a wrong guess gallops away from it and bisects
-                const float y = cdf::infer_bf16(sw, K[e]);
-                float g = floorf(y * (float)p);
+                float g = floorf(yp[e] * (float)p);
                 g = g < 0.0f ? 0.0f : (g > (float)n_piv ? (float)n_piv : g);
                 const uint32_t guess = (uint32_t)g;
                 uint32_t lo, hi;  // the bucket lies in [lo, hi]
