@@ -2198,6 +2198,56 @@ __global__ void __launch_bounds__(kKeyThreads)
         if (bh[j]) atomicAdd(&sizes[j], (unsigned long long)bh[j]);
 }
 
+// Learned mode: the model's bucket for every sample of the exactly sorted
+// sample, evaluated exactly as the fused kernel evaluates suffixes (the
+// same tensor-core inference from the same BF16 weights).
+__global__ void __launch_bounds__(256)
+    pf_sample_bucket_kernel(const uint32_t *__restrict__ spos, uint32_t ns, Packed P, DevLimits L,
+                            int lf, uint32_t p, const __nv_bfloat16 *__restrict__ w,
+                            uint32_t *__restrict__ mb) {
+    __shared__ __nv_bfloat16 sw[cdf::kParams + 1];
+    for (int j = threadIdx.x; j < cdf::kParams; j += blockDim.x) sw[j] = w[j];
+    __syncthreads();
+    const cdf::MmaWeights MW = cdf::mma_weights(sw);
+    // whole warps step together (the model runs warp-wide)
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < ns; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t q = spos[i < ns ? i : ns - 1];
+        const uint64_t key = prefix_key(P, q, dev_lim_at(L, q), lf);
+        const float y = cdf::infer_mma(MW, key);
+        float g = floorf(y * (float)p);
+        g = g < 0.0f ? 0.0f : (g > (float)(p - 1) ? (float)(p - 1) : g);
+        if (i < ns) mb[i] = (uint32_t)g;
+    }
+}
+
+// Learned mode's pivots: pivot j - 1 (j = 1 .. p - 1) is the first sorted
+// sample whose running-maximum model bucket reaches j, so a suffix between
+// two samples of one predicted bucket is predicted exactly and only the
+// suffixes next to a bucket boundary can be one bucket off.  mx = inclusive
+// running maximum of the samples' buckets; pivots no sample reaches take the
+// last sample.
+__global__ void pf_model_pivot_kernel(const uint32_t *__restrict__ spos,
+                                      const uint32_t *__restrict__ mx, uint32_t ns, uint32_t p,
+                                      Packed P, DevLimits L, int lf, uint64_t *__restrict__ pkey,
+                                      uint32_t *__restrict__ ppos, uint64_t *__restrict__ plim) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
+        const uint32_t lo = i == 0 ? 0u : mx[i - 1];
+        uint32_t hi = mx[i];
+        if (i + 1 == ns) hi = p - 1;  // the last sample also takes every pivot above it
+        if (hi <= lo) continue;
+        const uint32_t q = spos[i];
+        const uint64_t lim = dev_lim_at(L, q);
+        const uint64_t key = prefix_key(P, q, lim, lf);
+        for (uint32_t j = lo + 1; j <= hi && j < p; j++) {
+            ppos[j - 1] = q;
+            plim[j - 1] = lim;
+            pkey[j - 1] = key;
+        }
+    }
+}
+
 // Training set of the learned model from the exactly sorted sample: every
 // stride-th sample's comparison key and its rank fraction.
 __global__ void pf_train_set_kernel(const uint32_t *__restrict__ spos,
@@ -2351,16 +2401,7 @@ capssa_status pf_keys(Ctx &c, const EngineArgs &a, const eng::Packed &P, const K
         pf->fell_back = true;
         return CAPSSA_OK;
     }
-    // 2. pivots and the buckets' common prefixes
-    pf_pivot_kernel<<<grid_for(p, 256), 256, 0, c.stream>>>(spos, ns, p, P, a.lim, lf, pkey,
-                                                            ppos, plim);
-    CAPSSA_LAUNCHED(c);
-    pf_ell_kernel<<<grid_for(p, 256), 256, 0, c.stream>>>(ppos, plim, p, P, ell);
-    CAPSSA_LAUNCHED(c);
-    pf_table_kernel<<<grid_for((1u << kPfTableBits) + 1, 256), 256, 0, c.stream>>>(pkey, p - 1,
-                                                                                    tbl);
-    CAPSSA_LAUNCHED(c);
-    // 3. the learned CDF model on the sorted sample
+    // 2. the learned CDF model on the sorted sample (learned mode)
     if (pf->learned) {
         const uint32_t tn = std::min<uint32_t>(ns, kPfTrainSamples);
         const uint32_t stride = (ns + tn - 1) / tn;
@@ -2385,6 +2426,29 @@ capssa_status pf_keys(Ctx &c, const EngineArgs &a, const eng::Packed &P, const K
         c.stats.model_loss = loss;
         c.stats.train_samples = tn_eff;
     }
+    // 3. pivots: samples[(j + 1) * ns / p] (splitters), or where the model's
+    // predicted bucket steps (learned); then the buckets' common prefixes
+    if (pf->learned) {
+        uint32_t *mb = (uint32_t *)ws_get(c, WS_MISC, (size_t)ns * 4 + 64);
+        if (!mb) return set_err(c, CAPSSA_ENOMEM, "model buckets");
+        pf_sample_bucket_kernel<<<grid_for(ns, 256), 256, 0, c.stream>>>(spos, ns, P, a.lim, lf, p,
+                                                                         wbf, mb);
+        CAPSSA_LAUNCHED(c);
+        s = scan_u32(c, mb, mb, ns, /*max_op=*/true, /*inclusive=*/true);
+        if (s != CAPSSA_OK) return s;
+        pf_model_pivot_kernel<<<grid_for(ns, 256), 256, 0, c.stream>>>(spos, mb, ns, p, P, a.lim,
+                                                                       lf, pkey, ppos, plim);
+        CAPSSA_LAUNCHED(c);
+    } else {
+        pf_pivot_kernel<<<grid_for(p, 256), 256, 0, c.stream>>>(spos, ns, p, P, a.lim, lf, pkey,
+                                                                ppos, plim);
+        CAPSSA_LAUNCHED(c);
+    }
+    pf_ell_kernel<<<grid_for(p, 256), 256, 0, c.stream>>>(ppos, plim, p, P, ell);
+    CAPSSA_LAUNCHED(c);
+    pf_table_kernel<<<grid_for((1u << kPfTableBits) + 1, 256), 256, 0, c.stream>>>(pkey, p - 1,
+                                                                                    tbl);
+    CAPSSA_LAUNCHED(c);
     // 4. the fused partition + record kernel (the sample's sort used the
     // histogram buffer: clear it for the records' digit counts)
     CAPSSA_CUDA(c, cudaMemsetAsync(counts, 0, radix::kMaxPasses * 256 * 4, c.stream));

@@ -57,23 +57,25 @@ def test_c2_bench_text_2p28_bit_exact(ctx, c2):
 
 
 def test_c4_learned_sample_sort_2p28_bit_exact(ctx, c2):
-    from test_gpu_partition import pf_expected_plan
+    from test_gpu_partition import pf_expected_plan, sizes_between
     t, want = c2
     opts = capssa.ExtMemOpts(subproblem_count=4096, partition=capssa.Partition.LEARNED)
     got = ctx.build_in_memory_sample_sort(t, opts)
     assert got.dtype == np.uint64
     assert np.array_equal(got, want.astype(np.uint64))
     del got
+    cmp = orc.adjacent_cmp(t, want, orc.Limits(len(t)))
     ends, sizes = pf_expected_plan(t, orc.Limits(len(t)), 4096, want)
-    for part in (capssa.Partition.LEARNED, capssa.Partition.SPLITTERS):
-        k, pv, sz = ctx.sample_sort_plan(t, capssa.ExtMemOpts(subproblem_count=4096,
-                                                              partition=part))
-        assert k == 4096
-        assert np.array_equal(sz.astype(np.int64), sizes)
-        pos_of = np.empty(len(t), dtype=np.int64)
-        pos_of[want] = np.arange(len(t))
-        assert np.array_equal(pos_of[pv.astype(np.int64)], ends)  # PlainText: no ties
-        del pos_of
+    k, pv, sz = ctx.sample_sort_plan(t, capssa.ExtMemOpts(subproblem_count=4096))
+    assert k == 4096
+    assert np.array_equal(sz.astype(np.int64), sizes)
+    assert np.array_equal(sizes_between(want, cmp, pv)[1], ends)  # the same pivots
+    k, pv, sz = ctx.sample_sort_plan(t, opts)  # learned: pivots where the model steps
+    st = ctx.stats()
+    assert k == 4096
+    assert np.array_equal(sz.astype(np.int64), sizes_between(want, cmp, pv)[0])
+    assert st["mispredicted"] < 0.1 * len(t)
+    del cmp
     _, kp, opv, osz = orc.sample_sort(t, subproblem_count=4096)
     for part in (capssa.Partition.LEARNED, capssa.Partition.SPLITTERS):
         k, pv, sz = ctx.sample_sort_plan(t, capssa.ExtMemOpts(
