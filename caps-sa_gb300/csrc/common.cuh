@@ -109,16 +109,8 @@ __device__ __forceinline__ unsigned warp_match_bits(uint32_t label) {
 __device__ __forceinline__ uint32_t warp_rank_digit(uint32_t *wh, uint32_t d, unsigned peers,
                                                     unsigned lt_mask, int lane) {
     const int leader = 31 - __clz(peers);
-    // the leader's shared atomic as one predicated instruction (no branch
-    // and reconvergence per item)
-    uint32_t old;
-    const uint32_t addr = (uint32_t)__cvta_generic_to_shared(wh + d);
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.eq.s32 p, %1, %2;\n\tmov.u32 %0, 0;\n\t"
-        "@p atom.shared.add.u32 %0, [%3], %4;\n\t}"
-        : "=r"(old)
-        : "r"(lane), "r"(leader), "r"(addr), "r"((uint32_t)__popc(peers))
-        : "memory");
+    uint32_t old = 0;
+    if (lane == leader) old = atomicAdd(&wh[d], (uint32_t)__popc(peers));
     old = __shfl_sync(0xffffffffu, old, leader);
     return old + __popc(peers & lt_mask);
 }

@@ -150,11 +150,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     uint32_t d[IT];
     uint32_t r[IT];
     const uint32_t wbase = base + warp * 32 * IT;
-    const bool full = valid == (uint32_t)TILE;  // every record of the tile is real
 #pragma unroll
     for (int j = 0; j < IT; j++) {
         uint32_t idx = wbase + j * 32 + lane;
-        if (full || idx < n) {
+        if (idx < n) {
             k[j] = keys_in[idx];
             if (MODE == kGenVals) v[j] = val_base + idx;
             if (MODE == kPairs) v[j] = vals_in[idx];
