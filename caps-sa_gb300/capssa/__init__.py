@@ -151,6 +151,7 @@ def _load():
     L.capssa_cdf_grad.argtypes = [vp, vp, vp, vp, u64, vp, vp]
     L.capssa_selftest_bounded_wait.argtypes = [vp, C.c_uint32]
     L.capssa_cdf_train.argtypes = [vp, vp, vp, u64, i32, vp, vp]
+    L.capssa_cdf_infer.argtypes = [vp, vp, vp, u64, vp]
     L.capssa_ctx_set_stream.argtypes = [vp, vp]
     L.capssa_opts_default.argtypes = [C.POINTER(_Opts)]
     for s in ("u8", "u16", "u32"):
@@ -648,6 +649,16 @@ class Context:
         self._check(lib.capssa_cdf_grad(self._h, params.ctypes.data, x.ctypes.data,
                                         t.ctypes.data, len(x), g.ctypes.data, C.byref(loss)))
         return float(loss.value), g
+
+    def cdf_infer(self, params, prefixes):
+        """The model's outputs as the learned partition evaluates them (BF16
+        weights, tensor-core layer 1, fp32 layer 2)."""
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        x = np.ascontiguousarray(prefixes, dtype=np.uint64)
+        y = np.zeros(len(x), dtype=np.float32)
+        self._check(lib.capssa_cdf_infer(self._h, params.ctypes.data, x.ctypes.data, len(x),
+                                         y.ctypes.data))
+        return y
 
     def cdf_train(self, prefixes, targets, steps=300):
         """(trained parameters, final loss) after `steps` Adam steps on the GPU."""

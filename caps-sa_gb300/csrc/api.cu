@@ -1106,6 +1106,23 @@ capssa_status capssa_cdf_grad(capssa_ctx *ctx, const float *params, const uint64
     return scope.finish(s);
 }
 
+capssa_status capssa_cdf_infer(capssa_ctx *ctx, const float *params, const uint64_t *prefixes,
+                               uint64_t n, float *out) {
+    CTX_OR_EINVAL(ctx);
+    if (!params || (n && (!prefixes || !out)))
+        return scope.finish(set_err(c, CAPSSA_EINVAL, "null model buffer"));
+    if (n > 0xFFFFFFFFull) return scope.finish(set_err(c, CAPSSA_EUNSUPPORTED, "2^32 samples"));
+    void *dp = nullptr, *dx = nullptr;
+    capssa_status s = stage_in(c, WS_MISC, params, cdf::kParams * 4, 64, &dp);
+    if (s == CAPSSA_OK) s = stage_in(c, WS_MISC2, prefixes, n * 8, 64, &dx);
+    if (s != CAPSSA_OK) return scope.finish(s);
+    float *dy = (float *)ws_get(c, WS_OUT2, n * 4 + 64);
+    if (!dy) return scope.finish(set_err(c, CAPSSA_ENOMEM, "model output"));
+    s = cdf::infer(c, (const float *)dp, (const uint64_t *)dx, (uint32_t)n, dy);
+    if (s == CAPSSA_OK) s = stage_out(c, out, dy, n * 4);
+    return scope.finish(s);
+}
+
 capssa_status capssa_cdf_train(capssa_ctx *ctx, const uint64_t *prefixes, const float *targets,
                                uint64_t n, int32_t steps, float *params, float *loss) {
     CTX_OR_EINVAL(ctx);

@@ -174,7 +174,36 @@ struct TrainState {
     int *step;
 };
 
+// Tensor-core inference (infer_mma) of n prefixes from BF16 weights:
+// whole warps step together, lanes past the end repeat the last prefix.
+__global__ void __launch_bounds__(256)
+    infer_kernel(const __nv_bfloat16 *__restrict__ w, const uint64_t *__restrict__ x, uint32_t n,
+                 float *__restrict__ y) {
+    __shared__ __nv_bfloat16 sw[kParams + 1];
+    for (int j = threadIdx.x; j < kParams; j += blockDim.x) sw[j] = w[j];
+    __syncthreads();
+    const MmaWeights W = mma_weights(sw);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const float v = infer_mma(W, x[i < n ? i : n - 1]);
+        if (i < n) y[i] = v;
+    }
+}
+
 }  // namespace
+
+capssa_status infer(Ctx &c, const float *params, const uint64_t *x, uint32_t n, float *y) {
+    if (n == 0) return CAPSSA_OK;
+    __nv_bfloat16 *wb = (__nv_bfloat16 *)ws_get(c, WS_CDF, (size_t)(4 * kParams + 16) * 4);
+    if (!wb) return set_err(c, CAPSSA_ENOMEM, "model weights");
+    to_bf16_kernel<<<1, 320, 0, c.stream>>>(params, wb);
+    CAPSSA_LAUNCHED(c);
+    infer_kernel<<<std::min<unsigned>((n + 255) / 256, (unsigned)c.sm_count * 8), 256, 0,
+                   c.stream>>>(wb, x, n, y);
+    CAPSSA_LAUNCHED(c);
+    return CAPSSA_OK;
+}
 
 void init_params(float *p) {
     for (int h = 0; h < kHidden; h++) {

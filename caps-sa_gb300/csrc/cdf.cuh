@@ -151,6 +151,10 @@ capssa_status train(Ctx &c, const uint64_t *x, const float *t, uint32_t n, int s
                     float *params, __nv_bfloat16 *w_bf16, float *final_loss,
                     bool knot_start = false);
 
+// The model's output for n prefixes as the learned partition evaluates it:
+// the FP32 parameters (device) rounded to BF16, then infer_mma.
+capssa_status infer(Ctx &c, const float *params, const uint64_t *x, uint32_t n, float *y);
+
 // Deterministic initial parameters: ReLU kinks evenly spread over f0.
 void init_params(float *h_params);
 

@@ -408,6 +408,11 @@ CAPSSA_DECL_PLAN(u32, uint32_t)
  * capssa_cdf_train: `steps` full-batch Adam steps from the built-in
  * initialisation (the training the learned partition runs); writes the
  * trained parameters and the final loss.
+ * capssa_cdf_infer: the model's output for n prefixes exactly as the
+ * learned partition evaluates it: the parameters rounded to BF16, layer 1 on
+ * the tensor cores (mma.sync m16n8k16, fp32 accumulation, each input split
+ * into a BF16 high part and the BF16 rounding of its remainder), layer 2 in
+ * fp32.
  * ------------------------------------------------------------------- */
 /* Failure-detection self-test (no reference counterpart): one kernel
  * waits on a device word that nothing sets, polling `polls` times (1..2^20)
@@ -420,6 +425,8 @@ capssa_status capssa_cdf_grad(capssa_ctx *ctx, const float *params, const uint64
                               const float *targets, uint64_t n, float *grad, float *loss);
 capssa_status capssa_cdf_train(capssa_ctx *ctx, const uint64_t *prefixes, const float *targets,
                                uint64_t n, int32_t steps, float *params, float *loss);
+capssa_status capssa_cdf_infer(capssa_ctx *ctx, const float *params, const uint64_t *prefixes,
+                               uint64_t n, float *out);
 
 /* ---------------------------------------------------------------------
  * On-disk formats and emit sinks.

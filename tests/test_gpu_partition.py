@@ -44,6 +44,36 @@ def test_cdf_grad_matches_oracle(ctx):
         assert abs(loss - want_loss) <= 1e-4 * max(1.0, want_loss)
 
 
+def _bf16(a):
+    """float32 values rounded to the nearest BF16 (ties to even)."""
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def test_cdf_tensor_core_inference_matches_oracle(ctx):
+    """The learned partition's inference (BF16 weights, layer 1 on the
+    tensor cores with every input split into two BF16 parts, fp32 layer 2)
+    against the oracle's double-precision forward pass of the same
+    BF16-rounded weights: within 1e-4 of the output scale, on prefixes
+    spread over the whole key range and on a trained CDF."""
+    rng = np.random.default_rng(14)
+    for scale in (0.3, 2.0):
+        params = _bf16(rng.normal(0, scale, capssa.CDF_PARAMS))
+        x = rng.integers(0, 2 ** 64 - 1, 5000, dtype=np.uint64)
+        got = ctx.cdf_infer(params, x)
+        want = orc.cdf_forward(params, x)
+        tol = 1e-4 * max(1.0, float(np.max(np.abs(want))))
+        assert np.max(np.abs(got - want)) <= tol, (scale, np.max(np.abs(got - want)))
+    xs = np.sort(rng.integers(0, 2 ** 64 - 1, 65536, dtype=np.uint64))
+    ts = ((np.arange(len(xs)) + 0.5) / len(xs)).astype(np.float32)
+    params, _ = ctx.cdf_train(xs, ts, steps=100)
+    params = _bf16(params)
+    got = ctx.cdf_infer(params, xs[::7])
+    want = orc.cdf_forward(params, xs[::7])
+    assert np.max(np.abs(got - want)) <= 1e-4
+
+
 def test_cdf_train_learns_a_cdf(ctx):
     """Trained on sorted prefixes with rank-fraction targets, the model's
     (oracle-evaluated) predictions land within a few buckets of 4096."""
