@@ -538,13 +538,17 @@ constexpr int kInitTile = 256 * kInitPer;
 // A block stages its 256 * kInitPer sorted keys (and their neighbours) in
 // shared memory once, unpacks the positions when they ride below the keys,
 // and appends its groups with one atomic per list (per-list counts packed
-// as 16-bit fields, 4096 keys per block at most).
+// as 16-bit fields, 4096 keys per block at most).  The key layout (the
+// length field's kind, whether positions ride below the keys and whether
+// they are segment-local) is fixed per instantiation.
+template <int FLAG_LEN, bool UNPACK, bool SEG>
 __global__ void __launch_bounds__(256)
     init_groups_kernel(const uint64_t *__restrict__ keys, uint32_t n, int k, uint64_t lmask,
-                       int lf, int flag_len, int vshift, uint32_t *__restrict__ hd,
+                       int lf, int vshift, uint32_t *__restrict__ hd,
                        uint32_t *__restrict__ sa_out, GroupLists G,
                        const ShortList *__restrict__ S, int seg_at,
                        const uint64_t *__restrict__ seg_ends) {
+    constexpr int flag_len = FLAG_LEN;
     static_assert(kLists <= 8, "two packed words of four 16-bit counters");
     __shared__ uint64_t sk[kInitTile + 2];  // sk[l + 1] = key of sorted index base + l
     __shared__ uint32_t s_base[kLists];
@@ -554,7 +558,8 @@ __global__ void __launch_bounds__(256)
     // SA index of sorted record i: i + (short suffixes inserted at or before
     // it), one shift for the whole block unless an insertion falls inside
     __shared__ uint32_t s_shift[2];
-    const uint32_t ns = S ? __ldg(&S->n) : 0u;
+    // short suffixes exist only in a flagless sort
+    const uint32_t ns = (FLAG_LEN == 2 && S) ? __ldg(&S->n) : 0u;
     if (threadIdx.x == 0) {
         const uint32_t lo = ns ? short_shift(S, ns, base) : 0u;
         s_shift[0] = lo;
@@ -567,11 +572,11 @@ __global__ void __launch_bounds__(256)
     for (uint32_t l = threadIdx.x; l < valid; l += 256) {
         const uint64_t item = keys[base + l];
         sk[l + 1] = item >> vshift;
-        if (sa_out) {
+        if (UNPACK) {
             // segment-local positions (seg_at > 0): the segment index above
             // the key gives the segment's first position
             uint64_t pos = item & vmask;
-            if (seg_at) {
+            if (SEG) {
                 const uint64_t sg = item >> seg_at;
                 pos += sg ? __ldg(seg_ends + sg - 1) : 0ull;
             }
@@ -1619,26 +1624,6 @@ __global__ void subset_bits_kernel(const PT *__restrict__ pos, uint64_t m, uint6
                 if ((old & mask) != 0u || __popc(mask) != __popc(peers)) atomicExch(&flags[1], 1);
             }
         }
-    }
-}
-
-// flag[j] = 1 when the suffix at SA index j was requested.
-__global__ void subset_flag_kernel(const uint32_t *__restrict__ sa, uint32_t n,
-                                   const uint32_t *__restrict__ bits, uint32_t *__restrict__ flag) {
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint32_t p = sa[j];
-        flag[j] = (__ldg(bits + (p >> 5)) >> (p & 31)) & 1u;
-    }
-}
-
-// The requested suffixes in SA order: slot incl[j] - 1 (+ off) for each
-// flagged j (incl = inclusive scan of the flags).
-__global__ void subset_compact_kernel(const uint32_t *__restrict__ sa, uint32_t n,
-                                      const uint32_t *__restrict__ incl, uint32_t off,
-                                      uint32_t *__restrict__ out) {
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint32_t c = incl[j], before = j ? incl[j - 1] : 0u;
-        if (c != before) out[c - 1 + off] = sa[j];
     }
 }
 
@@ -2737,9 +2722,29 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
         CAPSSA_LAUNCHED(c);
     }
     CAPSSA_CUDA(c, cudaMemsetAsync(G.ctr, 0, sizeof(Counters), c.stream));
-    init_groups_kernel<<<grid_for(n_rec, kInitTile), 256, 0, c.stream>>>(
-        skeys, (uint32_t)n_rec, geo.k, (1ull << geo.lbits) - 1, lf, geo.flag_len, vbits, hd,
-        vbits ? sa : nullptr, G, d_short, local_pos ? vbits + geo.total : 0, a.lim.ends);
+    {
+        const unsigned ig = grid_for(n_rec, kInitTile);
+        const uint64_t lm = (1ull << geo.lbits) - 1;
+        const int seg_at = local_pos ? vbits + geo.total : 0;
+#define CAPSSA_IG(FL, UN, SG)                                                                  \
+    init_groups_kernel<FL, UN, SG><<<ig, 256, 0, c.stream>>>(skeys, (uint32_t)n_rec, geo.k, lm, \
+                                                             lf, vbits, hd, sa, G, d_short,      \
+                                                             seg_at, a.lim.ends)
+        if (!vbits) {
+            if (geo.flag_len == 0) CAPSSA_IG(0, false, false);
+            else if (geo.flag_len == 1) CAPSSA_IG(1, false, false);
+            else CAPSSA_IG(2, false, false);
+        } else if (seg_at) {
+            if (geo.flag_len == 0) CAPSSA_IG(0, true, true);
+            else if (geo.flag_len == 1) CAPSSA_IG(1, true, true);
+            else CAPSSA_IG(2, true, true);
+        } else {
+            if (geo.flag_len == 0) CAPSSA_IG(0, true, false);
+            else if (geo.flag_len == 1) CAPSSA_IG(1, true, false);
+            else CAPSSA_IG(2, true, false);
+        }
+#undef CAPSSA_IG
+    }
     CAPSSA_LAUNCHED(c);
     if (n_short) {
         short_write_kernel<<<1, 64, 0, c.stream>>>(d_short, sa, hd);
@@ -2781,13 +2786,14 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
         const int nxt = cur ^ 1;
         // rank doubling reads position-ordered ranks; they are built from the
         // SA-ordered heads the first time a round needs them
+        kt.start(c.stream);
         if ((nb || cnt[L_DEEP]) && !ranks_ready) {
             rank_from_heads_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa, hd, nn, rank);
             CAPSSA_LAUNCHED(c);
             ranks_ready = true;
+            kt.mark(c.stream, "ranks");
         }
         uint32_t *rk = ranks_ready ? rank : nullptr;
-        kt.start(c.stream);
         for (int l = 0; l < kLists; l++)
             CAPSSA_CUDA(c, cudaMemsetAsync(&G.ctr->n[l][nxt], 0, 4, c.stream));
         CAPSSA_CUDA(c, cudaMemsetAsync(&G.ctr->big_packed[nxt], 0, 8, c.stream));
@@ -3342,8 +3348,7 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
         // distinct positions: mark them in a bitmap (L2-sized: n / 8 bytes)
         // and compact the full order, instead of sorting them by rank
         uint32_t *bits = (uint32_t *)ws_get(c, WS_KEYS_A, (size_t)n * 8);
-        uint32_t *flag = (uint32_t *)ws_get(c, WS_KEYS_B, (size_t)n * 8);
-        if (!bits || !flag) return set_err(c, CAPSSA_ENOMEM, "subset workspace");
+        if (!bits) return set_err(c, CAPSSA_ENOMEM, "subset workspace");
         unsigned long long n_empty = 0;
         bool distinct = true;
         if (a.keep_bits) {
@@ -3371,22 +3376,24 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
             distinct = !h[1];
         }
         if (distinct && n_empty <= 1) {
-            subset_flag_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa, (uint32_t)n, bits,
-                                                                        flag);
-            CAPSSA_LAUNCHED(c);
-            capssa_status s0 = scan_u32(c, flag, flag, n, /*max_op=*/false, /*inclusive=*/true);
-            if (s0 != CAPSSA_OK) return s0;
-            // the empty suffix n sorts first (ShorterFirst) or last
+            // one pass: the requested suffixes of the full order, in order,
+            // straight into the output (widened on the way) unless an LCP
+            // array is wanted too; the empty suffix n sorts first
+            // (ShorterFirst) or last
             const uint32_t off = (n_empty && !lf) ? 1u : 0u;
-            subset_compact_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa, (uint32_t)n, flag,
-                                                                           off, sv);
-            CAPSSA_LAUNCHED(c);
+            const bool direct = !a.out_lcp;
+            void *dst = direct ? a.out_sa : (void *)sv;
+            const int db = direct ? a.out_bytes : 4;
+            capssa_status s0 = select_bits(c, sa, n, bits, off, dst, db);
+            if (s0 != CAPSSA_OK) return s0;
             if (n_empty) {
-                const uint32_t nv = (uint32_t)n;
-                CAPSSA_CUDA(c, cudaMemcpyAsync(sv + (lf ? m - 1 : 0), &nv, 4,
-                                               cudaMemcpyHostToDevice, c.stream));
-                CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));  // nv is on this stack
+                uint64_t *hv = (uint64_t *)c.h_scratch;
+                *hv = n;  // little-endian: the low 4 bytes are the u32 value
+                CAPSSA_CUDA(c, cudaMemcpyAsync((char *)dst + (lf ? m - 1 : 0) * (uint64_t)db, hv,
+                                               db, cudaMemcpyHostToDevice, c.stream));
+                CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));  // the pinned word is reused
             }
+            if (direct) return CAPSSA_OK;
             res = sv;
         }
     }

@@ -10,4 +10,10 @@ namespace capssa {
 capssa_status scan_u32(Ctx &c, const uint32_t *in, uint32_t *out, uint64_t n, bool max_op,
                        bool inclusive);
 
+// out[off + r] = the r-th entry of sa[0..n) whose bit in `bits` is set (bit
+// v of the bitmap for entry value v), as u32 (out_bytes 4) or u64 (8); one
+// pass with a decoupled look-back over tile counts.
+capssa_status select_bits(Ctx &c, const uint32_t *sa, uint64_t n, const uint32_t *bits,
+                          uint64_t off, void *out, int out_bytes);
+
 }  // namespace capssa
