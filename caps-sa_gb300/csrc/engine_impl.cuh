@@ -586,6 +586,45 @@ __global__ void __launch_bounds__(256)
     if (threadIdx.x == 0) sk[0] = base > 0 ? keys[base - 1] >> vshift : 0ull;
     if (threadIdx.x == 32) sk[valid + 1] = base + valid < n ? keys[base + valid] >> vshift : 0ull;
     __syncthreads();
+    // run heads of the tile as a bitmap (bit l of the tile: local l heads a
+    // run), the last word at or before each word that holds a head, and the
+    // head of a run that entered the tile from an earlier one: every member
+    // then finds its head in O(1) however long its run is
+    __shared__ uint32_t s_hb[kInitTile / 32];
+    __shared__ int s_prev[kInitTile / 32];
+    __shared__ uint32_t s_carry;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll 4
+    for (int j = 0; j < kInitPer; j++) {
+        const uint32_t l = j * 256 + threadIdx.x;
+        const bool hb = l < valid && (base + l == 0 || sk[l] != sk[l + 1]);
+        const uint32_t word = __ballot_sync(0xffffffffu, hb);
+        if (lane == 0) s_hb[j * 8 + warp] = word;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        static_assert(kInitTile / 32 == 128, "four bitmap words per lane");
+        int lp[4], last = -1;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (s_hb[4 * lane + q]) last = 4 * lane + q;
+            lp[q] = last;
+        }
+        int x = last;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x = max(x, y);
+        }
+        int before = __shfl_up_sync(0xffffffffu, x, 1);
+        if (lane == 0) before = -1;
+#pragma unroll
+        for (int q = 0; q < 4; q++) s_prev[4 * lane + q] = max(lp[q], before);
+        if (lane == 0)
+            s_carry = (base > 0 && valid && sk[0] == sk[1]) ? run_head(keys, 0, base, sk[1], vshift)
+                                                            : base;
+    }
+    __syncthreads();
     // tie state of a key: complete (equal through both ends: nothing to
     // refine), and the depth its group's members are known to agree on
     // (0 for the early-ended suffixes of a flagged plain text)
@@ -603,16 +642,14 @@ __global__ void __launch_bounds__(256)
             depth = (uint64_t)k;
         }
     };
-    // first sorted index of the run of `key` that holds local index l
-    auto head_of = [&](uint32_t l, uint64_t key) -> uint32_t {
-        uint32_t m = l;
-        int steps = 0;
-        while (m > 0 && steps < 32 && sk[m] == key) {  // sk[m] = key of local m - 1
-            m--;
-            steps++;
-        }
-        if (steps < 32 && (m > 0 || base == 0 || sk[0] != key)) return base + m;
-        return run_head(keys, 0, base + m, key, vshift);  // long run or one that began earlier
+    // first sorted index of the run that holds local index l
+    auto head_of = [&](uint32_t l) -> uint32_t {
+        const uint32_t w = l >> 5;
+        const uint32_t x = s_hb[w] & (0xffffffffu >> (31 - (l & 31)));
+        if (x) return base + w * 32 + 31 - __clz(x);
+        const int w2 = w ? s_prev[w - 1] : -1;
+        if (w2 >= 0) return base + (uint32_t)w2 * 32 + 31 - __clz(s_hb[w2]);
+        return s_carry;
     };
     uint64_t cnt_lo = 0, cnt_hi = 0;  // 16-bit counts: lists 0..3, lists 4..
     uint32_t ends = 0;                 // bit j: key j ends a group that needs refining
@@ -635,7 +672,7 @@ __global__ void __launch_bounds__(256)
             hd[i + sh] = i + sh;
             continue;
         }
-        const uint32_t g = head ? i : head_of(l, key);
+        const uint32_t g = head ? i : head_of(l);
         bool complete = false;
         uint64_t depth = (uint64_t)k;
         if (lf_field || (last && !head)) state(key, complete, depth);
@@ -672,7 +709,7 @@ __global__ void __launch_bounds__(256)
         bool complete;
         uint64_t depth;
         state(key, complete, depth);
-        const uint32_t g = head_of(l, key);
+        const uint32_t g = head_of(l);
         const int li = list_of(i - g + 1, depth);
         uint32_t slot = 0;
 #pragma unroll
@@ -695,6 +732,92 @@ __global__ void rank_from_heads_kernel(const uint32_t *__restrict__ sa,
                                        uint32_t *__restrict__ rank) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         rank[sa[i]] = hd[i];
+}
+
+// The same ranks for a rank array far beyond L2.  rank[sa[i]] = hd[i] in SA
+// order is a random 4-byte scatter over the whole array, which runs at the
+// rate DRAM serves partial sectors (about 26 G writes/s: 20 ms for 2^29
+// positions).  Instead the (position, head) pairs are first distributed to at
+// most 256 windows of 2^wb positions (8 MB of ranks or more) and then applied
+// window by window, so every rank line is assembled in L2 and written back
+// whole.  The distribution is a counting sort of 4096-pair tiles: per-tile
+// window counts, one exclusive scan of them in window-major order, then each
+// tile writes its pairs, grouped by window in shared memory, after its slot
+// in every window.  Tiles run in index order, so the tiles in flight write
+// next to each other in every window (a handful of pages, not the whole
+// array: blocks that each own a long chunk were TLB-bound, 12 ms at 2^29).
+constexpr int kRankWinMin = 21;
+constexpr int kRankWinMax = 256;
+constexpr int kRankPer = 16;  // pairs per thread and tile
+constexpr int kRankTile = 256 * kRankPer;
+
+// hist[w * gridDim.x + t] = pairs of tile t in window w.
+__global__ void __launch_bounds__(256)
+    rank_win_count_kernel(const uint32_t *__restrict__ sa, uint32_t m, int wb,
+                          uint32_t *__restrict__ hist) {
+    __shared__ uint32_t h[kRankWinMax];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * (uint32_t)kRankTile;
+#pragma unroll
+    for (int j = 0; j < kRankPer; j++) {
+        const uint32_t i = base + j * 256 + threadIdx.x;
+        if (i < m) atomicAdd(&h[__ldg(sa + i) >> wb], 1u);
+    }
+    __syncthreads();
+    hist[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+}
+
+// (position << 32 | head) pairs of tile t into their windows, after the
+// tile's slot0[w * gridDim.x + t] in each; staged in shared memory in window
+// order so that consecutive threads write consecutive slots.
+__global__ void __launch_bounds__(256)
+    rank_win_scatter_kernel(const uint32_t *__restrict__ sa, const uint32_t *__restrict__ hd,
+                            uint32_t m, int wb, const uint32_t *__restrict__ slot0,
+                            uint64_t *__restrict__ pairs) {
+    __shared__ uint64_t st[kRankTile];
+    __shared__ uint32_t s_cnt[kRankWinMax], s_start[kRankWinMax], s_slot[kRankWinMax];
+    s_cnt[threadIdx.x] = 0;
+    s_slot[threadIdx.x] = slot0[(size_t)threadIdx.x * gridDim.x + blockIdx.x];
+    __syncthreads();
+    const uint32_t base = blockIdx.x * (uint32_t)kRankTile;
+    const uint32_t valid = m - base < (uint32_t)kRankTile ? m - base : (uint32_t)kRankTile;
+    uint64_t e[kRankPer];
+    uint32_t r[kRankPer];
+#pragma unroll
+    for (int j = 0; j < kRankPer; j++) {
+        const uint32_t l = j * 256 + threadIdx.x;
+        if (l < valid) {
+            const uint32_t p = __ldg(sa + base + l);
+            e[j] = ((uint64_t)p << 32) | __ldg(hd + base + l);
+            r[j] = atomicAdd(&s_cnt[p >> wb], 1u);
+        }
+    }
+    __syncthreads();
+    uint32_t start;
+    block_excl_scan(s_cnt[threadIdx.x], &start);
+    s_start[threadIdx.x] = start;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kRankPer; j++) {
+        const uint32_t l = j * 256 + threadIdx.x;
+        if (l < valid) st[s_start[(uint32_t)(e[j] >> 32) >> wb] + r[j]] = e[j];
+    }
+    __syncthreads();
+    for (uint32_t l = threadIdx.x; l < valid; l += 256) {
+        const uint64_t x = st[l];
+        const uint32_t w = (uint32_t)(x >> 32) >> wb;
+        pairs[s_slot[w] + (l - s_start[w])] = x;
+    }
+}
+
+// rank[position] = head, streaming the pairs window by window.
+__global__ void rank_win_apply_kernel(const uint64_t *__restrict__ pairs, uint32_t m,
+                                      uint32_t *__restrict__ rank) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        const uint64_t e = __ldg(pairs + i);
+        rank[e >> 32] = (uint32_t)e;
+    }
 }
 
 // Sort key of suffix p for a round at depth h: the rank of p + h, or the
@@ -2788,8 +2911,27 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
         // SA-ordered heads the first time a round needs them
         kt.start(c.stream);
         if ((nb || cnt[L_DEEP]) && !ranks_ready) {
-            rank_from_heads_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa, hd, nn, rank);
-            CAPSSA_LAUNCHED(c);
+            if (n > (1ull << 24)) {
+                // by window: the sorted keys are dead once the groups are
+                // listed, so their buffers hold the pairs and the counts
+                int wb = kRankWinMin;
+                while ((uint64_t)kRankWinMax << wb < n) wb++;
+                const uint32_t tiles = (uint32_t)((N + kRankTile - 1) / kRankTile);
+                uint32_t *hist = (uint32_t *)keys_b;  // kRankWinMax * tiles <= N / 16 counts
+                rank_win_count_kernel<<<tiles, 256, 0, c.stream>>>(sa, nn, wb, hist);
+                CAPSSA_LAUNCHED(c);
+                kt.mark(c.stream, "rank-count");
+                s = scan_u32(c, hist, hist, (uint64_t)kRankWinMax * tiles, false, false);
+                if (s != CAPSSA_OK) return s;
+                rank_win_scatter_kernel<<<tiles, 256, 0, c.stream>>>(sa, hd, nn, wb, hist, keys_a);
+                CAPSSA_LAUNCHED(c);
+                kt.mark(c.stream, "rank-scatter");
+                rank_win_apply_kernel<<<grid_for(nn, 256), 256, 0, c.stream>>>(keys_a, nn, rank);
+                CAPSSA_LAUNCHED(c);
+            } else {
+                rank_from_heads_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa, hd, nn, rank);
+                CAPSSA_LAUNCHED(c);
+            }
             ranks_ready = true;
             kt.mark(c.stream, "ranks");
         }

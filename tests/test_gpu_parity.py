@@ -456,6 +456,22 @@ def test_large_text_runs_and_period(ctx, dtype):
     assert np.array_equal(got, orc.build_in_memory(t))
 
 
+def test_rank_build_by_window_2p25(ctx):
+    """Past 2^24 symbols the position-ordered ranks that rank doubling reads
+    are built window by window (2^21 positions each, the last one partial):
+    a 2^25+ text whose run and periodic stretch need rank doubling, bit-exact
+    with and without segments."""
+    t = _runs_text((1 << 25) + 4321, seed=14).astype(np.uint8)
+    got = ctx.build_in_memory(t)
+    assert ctx.stats()["refine_rounds"] > 5
+    assert np.array_equal(got, orc.build_in_memory(t))
+    rng = np.random.default_rng(6)
+    ends = np.unique(np.concatenate([rng.integers(1, len(t), 200), [len(t)]])).tolist()
+    lp, lo = limits_pair(len(t), ends, True)  # LongerFirst: a total order
+    got = ctx.build_in_memory(t, lp)
+    assert np.array_equal(got, orc.build_in_memory(t, None, lo))
+
+
 def test_large_text_star_segments(ctx):
     t = _runs_text((1 << 22) + 777, seed=12).astype(np.uint8)
     rng = np.random.default_rng(5)
