@@ -89,6 +89,12 @@ class Sampling(enum.IntEnum):
     PARTITION_FIRST = 2
 
 
+class TieOrder(enum.IntEnum):
+    """capssa_tie_order: order inside a tie class (SegmentedText, ShorterFirst)."""
+    POSITION = 0   # ascending input order
+    REFERENCE = 1  # as the reference's in-memory merge sort emits it
+
+
 class _Limits(C.Structure):
     _fields_ = [("kind", C.c_int32), ("boundary", C.c_int32),
                 ("ends", C.c_void_p), ("n_ends", C.c_uint64)]
@@ -97,7 +103,7 @@ class _Limits(C.Structure):
 class _Opts(C.Structure):
     _fields_ = [("max_context", C.c_uint64), ("subproblem_count", C.c_uint64),
                 ("partition", C.c_int32), ("host_threads", C.c_int32),
-                ("flags", C.c_uint64), ("sampling", C.c_int32), ("reserved32", C.c_int32),
+                ("flags", C.c_uint64), ("sampling", C.c_int32), ("tie_order", C.c_int32),
                 ("reserved", C.c_uint64 * 4)]
 
 
@@ -116,7 +122,9 @@ class _Stats(C.Structure):
                 ("sort_pass_ms", C.c_double), ("partition_ms", C.c_double),
                 ("train_ms", C.c_double), ("partition_probes", C.c_uint64),
                 ("train_samples", C.c_uint32), ("model_loss", C.c_float),
-                ("radix_items", C.c_uint32), ("sparse_subset", C.c_uint32)]
+                ("radix_items", C.c_uint32), ("sparse_subset", C.c_uint32),
+                ("tie_classes", C.c_uint32), ("reserved_u32", C.c_uint32),
+                ("tie_order_ms", C.c_double)]
 
 
 class _Packer(C.Structure):
@@ -268,8 +276,10 @@ class SegmentedText:
 
 @dataclass
 class Opts:
-    """src/sample_sort.rs:70-85."""
+    """src/sample_sort.rs:70-85; tie_order picks the order inside tie classes
+    (the reference leaves it unpinned, src/sample_sort.rs:908-913)."""
     max_context: int = UNBOUNDED
+    tie_order: TieOrder = TieOrder.POSITION
 
 
 @dataclass
@@ -292,6 +302,7 @@ def _copts(o) -> _Opts:
         c.host_threads = int(getattr(o, "host_threads", 0))
         c.flags = 0
         c.sampling = int(getattr(o, "sampling", 0))
+        c.tie_order = int(getattr(o, "tie_order", 0))
     return c
 
 

@@ -349,8 +349,10 @@ capssa_status build_common(Ctx &c, const ST *text, uint64_t n, const void *posit
                            int pos_bytes, uint64_t m, const capssa_limits *lp,
                            const capssa_opts *opts, void *out_sa, int out_bytes, void *out_lcp,
                            const PartRequest *part = nullptr, uint64_t seg_major_len = 0,
-                           const uint32_t *keep_bits = nullptr) {
+                           const uint32_t *keep_bits = nullptr, bool in_memory = false) {
     if (!text && n) return set_err(c, CAPSSA_EINVAL, "null text");
+    if (opts && (opts->tie_order < CAPSSA_TIES_POSITION || opts->tie_order > CAPSSA_TIES_REFERENCE))
+        return set_err(c, CAPSSA_EINVAL, "unknown tie order");
     const bool chosen = positions || keep_bits;  // a subset, m suffixes
     if (!out_sa && (chosen ? m : n)) return set_err(c, CAPSSA_EINVAL, "null output");
     if (out_bytes == 4 && n > 0xFFFFFFFFull)
@@ -402,6 +404,8 @@ capssa_status build_common(Ctx &c, const ST *text, uint64_t n, const void *posit
         a.part_sizes = part->sizes;
         a.part_first = !opts || opts->sampling != CAPSSA_SAMPLING_REFERENCE ? 1 : 0;
     }
+    // the merge sort's tie order belongs to the in-memory builders
+    a.tie_ref = in_memory && opts && opts->tie_order == CAPSSA_TIES_REFERENCE ? 1 : 0;
     if (positions && m == 0) return CAPSSA_OK;
     s = engine_build(c, a);
     if (s != CAPSSA_OK) return s;
@@ -826,8 +830,8 @@ uint64_t capssa_ctx_workspace_bytes(const capssa_ctx *ctx) {
                                                    uint64_t n, const capssa_limits *lp,       \
                                                    const capssa_opts *opts, IT *out_sa) {     \
         CTX_OR_EINVAL(ctx);                                                                   \
-        return scope.finish(                                                                  \
-            build_common<ST>(c, text, n, nullptr, IB, 0, lp, opts, out_sa, IB, nullptr));    \
+        return scope.finish(build_common<ST>(c, text, n, nullptr, IB, 0, lp, opts, out_sa, IB, \
+                                             nullptr, nullptr, 0, nullptr, true));            \
     }                                                                                         \
     capssa_status capssa_build_in_memory_for_positions_##S##_##I(                             \
         capssa_ctx *ctx, const ST *text, uint64_t n, const IT *positions, uint64_t m,         \
@@ -836,7 +840,8 @@ uint64_t capssa_ctx_workspace_bytes(const capssa_ctx *ctx) {
         if (!positions && m) return scope.finish(set_err(c, CAPSSA_EINVAL, "null positions")); \
         return scope.finish(build_common<ST>(c, text, n, positions ? (const void *)positions   \
                                                                    : (const void *)out_sa,    \
-                                             IB, m, lp, opts, out_sa, IB, nullptr));          \
+                                             IB, m, lp, opts, out_sa, IB, nullptr, nullptr,   \
+                                             0, nullptr, true));                              \
     }                                                                                         \
     capssa_status capssa_build_in_memory_lcp_##S##_##I(                                       \
         capssa_ctx *ctx, const ST *text, uint64_t n, const IT *positions, uint64_t m,         \
@@ -844,7 +849,8 @@ uint64_t capssa_ctx_workspace_bytes(const capssa_ctx *ctx) {
         CTX_OR_EINVAL(ctx);                                                                   \
         if (!out_lcp) return scope.finish(set_err(c, CAPSSA_EINVAL, "null lcp output"));     \
         return scope.finish(build_common<ST>(c, text, n, positions, IB, positions ? m : 0, lp, \
-                                             opts, out_sa, IB, out_lcp));                     \
+                                             opts, out_sa, IB, out_lcp, nullptr, 0, nullptr,  \
+                                             true));                                          \
     }                                                                                         \
     capssa_status capssa_merge_##S##_##I(                                                     \
         capssa_ctx *ctx, const ST *text, uint64_t n, const capssa_limits *lp, const IT *x,    \

@@ -57,6 +57,7 @@ struct EngineArgs {
     uint64_t *part_pivots;   // host, part_p - 1 entries (out) or nullptr
     uint64_t *part_sizes;    // host, part_p entries (out) or nullptr
     int part_first;          // 1: partition before the sort (CAPSSA_SAMPLING_PARTITION_FIRST)
+    int tie_ref;             // 1: tie classes in the reference's merge order (ties.cu)
 };
 
 // Runs the whole sort; all buffers are device buffers.

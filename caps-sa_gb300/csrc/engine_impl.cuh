@@ -15,6 +15,7 @@
 #include "lcp.cuh"
 #include "radix.cuh"
 #include "scan.cuh"
+#include "ties.cuh"
 
 namespace capssa {
 namespace {  // every kernel and helper is private to its engine_*.cu unit
@@ -722,101 +723,6 @@ __global__ void __launch_bounds__(256)
             }
         }
         list_ptr(G, li, 0)[slot] = group_entry(g + shift_of(i), i - g + 1, depth);
-    }
-}
-
-// Position-ordered ranks from the SA-ordered heads; built once, the first
-// time a round needs rank doubling (rank[p + h] lookups).
-__global__ void rank_from_heads_kernel(const uint32_t *__restrict__ sa,
-                                       const uint32_t *__restrict__ hd, uint32_t n,
-                                       uint32_t *__restrict__ rank) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        rank[sa[i]] = hd[i];
-}
-
-// The same ranks for a rank array far beyond L2.  rank[sa[i]] = hd[i] in SA
-// order is a random 4-byte scatter over the whole array, which runs at the
-// rate DRAM serves partial sectors (about 26 G writes/s: 20 ms for 2^29
-// positions).  Instead the (position, head) pairs are first distributed to at
-// most 256 windows of 2^wb positions (8 MB of ranks or more) and then applied
-// window by window, so every rank line is assembled in L2 and written back
-// whole.  The distribution is a counting sort of 4096-pair tiles: per-tile
-// window counts, one exclusive scan of them in window-major order, then each
-// tile writes its pairs, grouped by window in shared memory, after its slot
-// in every window.  Tiles run in index order, so the tiles in flight write
-// next to each other in every window (a handful of pages, not the whole
-// array: blocks that each own a long chunk were TLB-bound, 12 ms at 2^29).
-constexpr int kRankWinMin = 21;
-constexpr int kRankWinMax = 256;
-constexpr int kRankPer = 16;  // pairs per thread and tile
-constexpr int kRankTile = 256 * kRankPer;
-
-// hist[w * gridDim.x + t] = pairs of tile t in window w.
-__global__ void __launch_bounds__(256)
-    rank_win_count_kernel(const uint32_t *__restrict__ sa, uint32_t m, int wb,
-                          uint32_t *__restrict__ hist) {
-    __shared__ uint32_t h[kRankWinMax];
-    h[threadIdx.x] = 0;
-    __syncthreads();
-    const uint32_t base = blockIdx.x * (uint32_t)kRankTile;
-#pragma unroll
-    for (int j = 0; j < kRankPer; j++) {
-        const uint32_t i = base + j * 256 + threadIdx.x;
-        if (i < m) atomicAdd(&h[__ldg(sa + i) >> wb], 1u);
-    }
-    __syncthreads();
-    hist[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
-}
-
-// (position << 32 | head) pairs of tile t into their windows, after the
-// tile's slot0[w * gridDim.x + t] in each; staged in shared memory in window
-// order so that consecutive threads write consecutive slots.
-__global__ void __launch_bounds__(256)
-    rank_win_scatter_kernel(const uint32_t *__restrict__ sa, const uint32_t *__restrict__ hd,
-                            uint32_t m, int wb, const uint32_t *__restrict__ slot0,
-                            uint64_t *__restrict__ pairs) {
-    __shared__ uint64_t st[kRankTile];
-    __shared__ uint32_t s_cnt[kRankWinMax], s_start[kRankWinMax], s_slot[kRankWinMax];
-    s_cnt[threadIdx.x] = 0;
-    s_slot[threadIdx.x] = slot0[(size_t)threadIdx.x * gridDim.x + blockIdx.x];
-    __syncthreads();
-    const uint32_t base = blockIdx.x * (uint32_t)kRankTile;
-    const uint32_t valid = m - base < (uint32_t)kRankTile ? m - base : (uint32_t)kRankTile;
-    uint64_t e[kRankPer];
-    uint32_t r[kRankPer];
-#pragma unroll
-    for (int j = 0; j < kRankPer; j++) {
-        const uint32_t l = j * 256 + threadIdx.x;
-        if (l < valid) {
-            const uint32_t p = __ldg(sa + base + l);
-            e[j] = ((uint64_t)p << 32) | __ldg(hd + base + l);
-            r[j] = atomicAdd(&s_cnt[p >> wb], 1u);
-        }
-    }
-    __syncthreads();
-    uint32_t start;
-    block_excl_scan(s_cnt[threadIdx.x], &start);
-    s_start[threadIdx.x] = start;
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < kRankPer; j++) {
-        const uint32_t l = j * 256 + threadIdx.x;
-        if (l < valid) st[s_start[(uint32_t)(e[j] >> 32) >> wb] + r[j]] = e[j];
-    }
-    __syncthreads();
-    for (uint32_t l = threadIdx.x; l < valid; l += 256) {
-        const uint64_t x = st[l];
-        const uint32_t w = (uint32_t)(x >> 32) >> wb;
-        pairs[s_slot[w] + (l - s_start[w])] = x;
-    }
-}
-
-// rank[position] = head, streaming the pairs window by window.
-__global__ void rank_win_apply_kernel(const uint64_t *__restrict__ pairs, uint32_t m,
-                                      uint32_t *__restrict__ rank) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-        const uint64_t e = __ldg(pairs + i);
-        rank[e >> 32] = (uint32_t)e;
     }
 }
 
@@ -2911,27 +2817,10 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
         // SA-ordered heads the first time a round needs them
         kt.start(c.stream);
         if ((nb || cnt[L_DEEP]) && !ranks_ready) {
-            if (n > (1ull << 24)) {
-                // by window: the sorted keys are dead once the groups are
-                // listed, so their buffers hold the pairs and the counts
-                int wb = kRankWinMin;
-                while ((uint64_t)kRankWinMax << wb < n) wb++;
-                const uint32_t tiles = (uint32_t)((N + kRankTile - 1) / kRankTile);
-                uint32_t *hist = (uint32_t *)keys_b;  // kRankWinMax * tiles <= N / 16 counts
-                rank_win_count_kernel<<<tiles, 256, 0, c.stream>>>(sa, nn, wb, hist);
-                CAPSSA_LAUNCHED(c);
-                kt.mark(c.stream, "rank-count");
-                s = scan_u32(c, hist, hist, (uint64_t)kRankWinMax * tiles, false, false);
-                if (s != CAPSSA_OK) return s;
-                rank_win_scatter_kernel<<<tiles, 256, 0, c.stream>>>(sa, hd, nn, wb, hist, keys_a);
-                CAPSSA_LAUNCHED(c);
-                kt.mark(c.stream, "rank-scatter");
-                rank_win_apply_kernel<<<grid_for(nn, 256), 256, 0, c.stream>>>(keys_a, nn, rank);
-                CAPSSA_LAUNCHED(c);
-            } else {
-                rank_from_heads_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(sa, hd, nn, rank);
-                CAPSSA_LAUNCHED(c);
-            }
+            // beyond L2 the sorted keys' buffers (dead once the groups are
+            // listed) hold the window pairs and counts
+            s = scatter_u32(c, sa, hd, nn, rank, n, keys_a, (uint32_t *)keys_b);
+            if (s != CAPSSA_OK) return s;
             ranks_ready = true;
             kt.mark(c.stream, "ranks");
         }
@@ -3462,6 +3351,33 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
         if (s != CAPSSA_OK) return s;
     }
     FinishTimer ft(c);
+    // the reference's order inside the comparator's tie classes (only
+    // SegmentedText under ShorterFirst has any); `key` marks the classes when
+    // the full order's group heads line up with the output
+    auto tie_pass = [&](const uint32_t *key) -> capssa_status {
+        if (!a.tie_ref || !a.lim.segmented || lf || a.part_p || a.seg_major || a.keep_bits)
+            return CAPSSA_OK;
+        TieArgs t{};
+        t.text = a.text;
+        t.sym_bytes = a.sym_bytes;
+        t.lim = a.lim;
+        t.max_ctx = a.max_ctx;
+        t.out = a.out_sa;
+        t.out_bytes = a.out_bytes;
+        t.m = m;
+        t.key = key;
+        t.positions = a.positions;
+        t.pos_bytes = a.pos_bytes;
+        cudaEventRecord(c.pev[6], c.stream);
+        capssa_status s0 = reference_tie_order(c, t);
+        if (s0 != CAPSSA_OK) return s0;
+        cudaEventRecord(c.pev[7], c.stream);
+        CAPSSA_CUDA(c, cudaEventSynchronize(c.pev[7]));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c.pev[6], c.pev[7]);
+        c.stats.tie_order_ms = ms;
+        return CAPSSA_OK;
+    };
     if (!subset) {
         if (a.out_bytes == 4) {
             if (sa != a.out_sa)
@@ -3477,7 +3393,10 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
                                            a.out_lcp, a.out_bytes);
             if (s != CAPSSA_OK) return s;
         }
-        return CAPSSA_OK;
+        // last: it reuses the sort's buffers (reordering inside a class
+        // leaves the LCP array as it is); the refinement's final group heads
+        // mark the classes of an unbounded sort
+        return tie_pass(bounded ? nullptr : (const uint32_t *)c.bufs[WS_GROUPS_B]);
     }
     // subset: order the requested positions by their index in the full SA
     uint32_t *sv = (uint32_t *)ws_get(c, WS_MISC3, (size_t)m * 8 + 64);
@@ -3535,7 +3454,7 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
                                                db, cudaMemcpyHostToDevice, c.stream));
                 CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));  // the pinned word is reused
             }
-            if (direct) return CAPSSA_OK;
+            if (direct) return tie_pass(nullptr);
             res = sv;
         }
     }
@@ -3584,7 +3503,7 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
                          a.out_bytes);
         if (s != CAPSSA_OK) return s;
     }
-    return CAPSSA_OK;
+    return tie_pass(nullptr);
 }
 
 }  // namespace

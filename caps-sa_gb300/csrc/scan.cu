@@ -190,6 +190,121 @@ __global__ void __launch_bounds__(kScanThreads)
         if ((keep >> j) & 1u) out[o++] = (OT)v[j];
 }
 
+
+// ---------------------------------------------------------------- scatter
+
+// dst[idx[i]] = val(i) for a destination far beyond L2.  Done directly, a
+// random 4-byte scatter over the whole array runs at the rate DRAM serves
+// partial sectors (about 26 G writes/s: 20 ms for 2^29 entries).  Instead
+// the (index, value) pairs are first distributed to at most 256 windows of
+// 2^wb destination entries (8 MB or more) and then applied window by window,
+// so every destination line is assembled in L2 and written back whole.  The
+// distribution is a counting sort of 4096-pair tiles: per-tile window counts,
+// one exclusive scan of them in window-major order, then each tile writes its
+// pairs, grouped by window in shared memory, after its slot in every window.
+// Tiles run in index order, so the tiles in flight write next to each other in
+// every window (a handful of pages, not the whole pair array: blocks that
+// each owned a long chunk were TLB-bound, 12 ms at 2^29).
+constexpr int kWinMin = 21;
+constexpr int kWinMax = 256;
+constexpr int kWinPer = 16;  // pairs per thread and tile
+constexpr int kWinTile = 256 * kWinPer;
+
+__device__ __forceinline__ uint32_t pair_val(const uint32_t *vals, uint32_t i) {
+    return vals ? __ldg(vals + i) : i;
+}
+
+__global__ void scatter_direct_kernel(const uint32_t *__restrict__ idx,
+                                      const uint32_t *__restrict__ vals, uint32_t m,
+                                      uint32_t *__restrict__ dst) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+        dst[idx[i]] = pair_val(vals, i);
+}
+
+// hist[w * gridDim.x + t] = pairs of tile t in window w.
+__global__ void __launch_bounds__(256)
+    win_count_kernel(const uint32_t *__restrict__ idx, uint32_t m, int wb,
+                     uint32_t *__restrict__ hist) {
+    __shared__ uint32_t h[kWinMax];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * (uint32_t)kWinTile;
+#pragma unroll
+    for (int j = 0; j < kWinPer; j++) {
+        const uint32_t i = base + j * 256 + threadIdx.x;
+        if (i < m) atomicAdd(&h[__ldg(idx + i) >> wb], 1u);
+    }
+    __syncthreads();
+    hist[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive block-wide prefix of one u32 per thread (256 threads).
+__device__ __forceinline__ uint32_t block_excl_256(uint32_t v) {
+    __shared__ uint32_t s_w[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    uint32_t before = 0;
+    for (int w = 0; w < warp; w++) before += s_w[w];
+    return before + x - v;
+}
+
+// (index << 32 | value) pairs of tile t into their windows, after the tile's
+// slot0[w * gridDim.x + t] in each; staged in shared memory in window order
+// so that consecutive threads write consecutive slots.
+__global__ void __launch_bounds__(256)
+    win_scatter_kernel(const uint32_t *__restrict__ idx, const uint32_t *__restrict__ vals,
+                       uint32_t m, int wb, const uint32_t *__restrict__ slot0,
+                       uint64_t *__restrict__ pairs) {
+    __shared__ uint64_t st[kWinTile];
+    __shared__ uint32_t s_cnt[kWinMax], s_start[kWinMax], s_slot[kWinMax];
+    s_cnt[threadIdx.x] = 0;
+    s_slot[threadIdx.x] = slot0[(size_t)threadIdx.x * gridDim.x + blockIdx.x];
+    __syncthreads();
+    const uint32_t base = blockIdx.x * (uint32_t)kWinTile;
+    const uint32_t valid = m - base < (uint32_t)kWinTile ? m - base : (uint32_t)kWinTile;
+    uint64_t e[kWinPer];
+    uint32_t r[kWinPer];
+#pragma unroll
+    for (int j = 0; j < kWinPer; j++) {
+        const uint32_t l = j * 256 + threadIdx.x;
+        if (l < valid) {
+            const uint32_t p = __ldg(idx + base + l);
+            e[j] = ((uint64_t)p << 32) | pair_val(vals, base + l);
+            r[j] = atomicAdd(&s_cnt[p >> wb], 1u);
+        }
+    }
+    __syncthreads();
+    s_start[threadIdx.x] = block_excl_256(s_cnt[threadIdx.x]);
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kWinPer; j++) {
+        const uint32_t l = j * 256 + threadIdx.x;
+        if (l < valid) st[s_start[(uint32_t)(e[j] >> 32) >> wb] + r[j]] = e[j];
+    }
+    __syncthreads();
+    for (uint32_t l = threadIdx.x; l < valid; l += 256) {
+        const uint64_t x = st[l];
+        const uint32_t w = (uint32_t)(x >> 32) >> wb;
+        pairs[s_slot[w] + (l - s_start[w])] = x;
+    }
+}
+
+// dst[index] = value, streaming the pairs window by window.
+__global__ void win_apply_kernel(const uint64_t *__restrict__ pairs, uint32_t m,
+                                 uint32_t *__restrict__ dst) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        const uint64_t e = __ldg(pairs + i);
+        dst[e >> 32] = (uint32_t)e;
+    }
+}
+
 }  // namespace
 
 capssa_status select_bits(Ctx &c, const uint32_t *sa, uint64_t n, const uint32_t *bits,
@@ -232,6 +347,36 @@ capssa_status scan_u32(Ctx &c, const uint32_t *in, uint32_t *out, uint64_t n, bo
     else
         scan_kernel<false, false><<<(unsigned)tiles, kScanThreads, 0, c.stream>>>(
             in, out, n, status, counter, c.d_flags);
+    CAPSSA_LAUNCHED(c);
+    return CAPSSA_OK;
+}
+
+
+size_t scatter_hist_words(uint64_t m) {
+    return (size_t)kWinMax * ((m + kWinTile - 1) / kWinTile) + 64;
+}
+
+capssa_status scatter_u32(Ctx &c, const uint32_t *idx, const uint32_t *vals, uint64_t m,
+                          uint32_t *dst, uint64_t n_dst, uint64_t *pairs, uint32_t *hist) {
+    if (m == 0) return CAPSSA_OK;
+    if (m > 0xFFFFFFFFull || n_dst > 0x100000000ull)
+        return set_err(c, CAPSSA_EUNSUPPORTED, "scatter beyond 2^32 entries");
+    const uint32_t mm = (uint32_t)m;
+    if (n_dst <= (1ull << 24) || !pairs || !hist) {  // the destination fits L2
+        scatter_direct_kernel<<<grid_for(m, 256), 256, 0, c.stream>>>(idx, vals, mm, dst);
+        CAPSSA_LAUNCHED(c);
+        return CAPSSA_OK;
+    }
+    int wb = kWinMin;
+    while ((uint64_t)kWinMax << wb < n_dst) wb++;
+    const uint32_t tiles = (uint32_t)((m + kWinTile - 1) / kWinTile);
+    win_count_kernel<<<tiles, 256, 0, c.stream>>>(idx, mm, wb, hist);
+    CAPSSA_LAUNCHED(c);
+    capssa_status s = scan_u32(c, hist, hist, (uint64_t)kWinMax * tiles, false, false);
+    if (s != CAPSSA_OK) return s;
+    win_scatter_kernel<<<tiles, 256, 0, c.stream>>>(idx, vals, mm, wb, hist, pairs);
+    CAPSSA_LAUNCHED(c);
+    win_apply_kernel<<<grid_for(m, 256), 256, 0, c.stream>>>(pairs, mm, dst);
     CAPSSA_LAUNCHED(c);
     return CAPSSA_OK;
 }

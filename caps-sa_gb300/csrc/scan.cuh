@@ -16,4 +16,11 @@ capssa_status scan_u32(Ctx &c, const uint32_t *in, uint32_t *out, uint64_t n, bo
 capssa_status select_bits(Ctx &c, const uint32_t *sa, uint64_t n, const uint32_t *bits,
                           uint64_t off, void *out, int out_bytes);
 
+// dst[idx[i]] = vals ? vals[i] : i for i < m (idx distinct, < n_dst).
+// Destinations beyond L2 go window by window through `pairs` (m words) and
+// `hist` (scatter_hist_words(m) words); either null scatters directly.
+size_t scatter_hist_words(uint64_t m);
+capssa_status scatter_u32(Ctx &c, const uint32_t *idx, const uint32_t *vals, uint64_t m,
+                          uint32_t *dst, uint64_t n_dst, uint64_t *pairs, uint32_t *hist);
+
 }  // namespace capssa

@@ -1,0 +1,503 @@
+// ties.cu — the reference's order inside comparator tie classes.
+//
+// Under SegmentedText with the ShorterFirst boundary order, suffixes that are
+// equal up to their (equal) limits compare Equal, and the reference emits
+// them in whatever order its merge sort produces: recursive halves at
+// mid = len / 2 of the input positions (src/sample_sort.rs:221-266), merged
+// by merge_body! (src/sample_sort.rs:430-497), which on Equal outputs from the
+// stream it did not output from last.  Inside one merge the members of a
+// class therefore alternate between the two halves, beginning with the half
+// that did not output the element just before the class (the left half when
+// nothing came before it: the right half goes first), and the longer half's
+// remaining members follow.  Nodes whose class members all sit in one half
+// keep their order.
+//
+// The engine emits each class in ascending input order.  This pass computes,
+// for every class and every merge-tree node with class members in both
+// halves (a split node), which half output last before the class:
+//   * the predecessor of the class among the node's inputs is the input with
+//     the largest suffix-order slot below the class start.  A block walks
+//     back from the class start through the slots, and each slot marks the
+//     split nodes of the class on its input's root-to-leaf path (first hit =
+//     largest slot); nodes the walk did not reach within its budget scan
+//     their input range instead;
+//   * if the predecessor belongs to another tie class with members in both
+//     halves of the node, that class's last output decides: its longer half,
+//     or, with equal halves, the half it did not begin with there (a link to
+//     that class's own split node, followed afterwards);
+// then places every member by composing the alternations from its leaf up to
+// the root.  The model was checked against the oracle's merge sort (which
+// restates the reference's) on random segmented texts, subsets, repeated
+// positions and finite contexts.
+#include <algorithm>
+
+#include "common.cuh"
+#include "lcp.cuh"
+#include "radix.cuh"
+#include "scan.cuh"
+#include "ties.cuh"
+
+namespace capssa {
+namespace {
+
+constexpr int kMaxDepth = 40;            // merge-tree depth for up to 2^32 inputs, with slack
+constexpr uint32_t kWalkSlots = 1u << 16;  // slots a class walks back before scanning
+constexpr uint32_t kChaseLimit = 1u << 24;  // links followed from one split node
+enum : uint32_t { kWalkDone = 0, kWalkExhausted = 1, kWalkBudget = 2 };
+
+inline int bits_upto(uint64_t v) {  // bits to represent 0..v
+    int b = 1;
+    while (b < 64 && (v >> b) != 0) b++;
+    return b;
+}
+
+__device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *__restrict__ a, uint32_t lo,
+                                                    uint32_t hi, uint64_t x) {
+    while (lo < hi) {
+        const uint32_t mid = lo + ((hi - lo) >> 1);
+        if ((uint64_t)__ldg(a + mid) < x)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// tie[r] = 1 when slot r - 1 and r compare Equal; pos32 = the positions.
+template <typename OT>
+__global__ void tie_flag_kernel(const OT *__restrict__ out, uint32_t m,
+                                const uint32_t *__restrict__ key,
+                                const uint8_t *__restrict__ text, int sym_bytes, DevLimits L,
+                                uint64_t max_ctx, uint32_t *__restrict__ pos32,
+                                uint32_t *__restrict__ tie) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        const uint32_t b = (uint32_t)out[r];
+        pos32[r] = b;
+        uint32_t t = 0;
+        if (r > 0) {
+            if (key) {
+                t = key[r] == key[r - 1];
+            } else {  // suffix_cmp_with Equal: same limit, same symbols up to it (or max_ctx)
+                const uint32_t a = (uint32_t)out[r - 1];
+                const uint64_t la = dev_lim_at(L, a), lb = dev_lim_at(L, b);
+                if (la == lb) {
+                    const uint64_t lim = la < max_ctx ? la : max_ctx;
+                    const uint64_t k = (uint64_t)sym_bytes;
+                    t = thread_lcp_bytes(text, (uint64_t)a * k, (uint64_t)b * k, lim * k) >=
+                        lim * k;
+                }
+            }
+        }
+        tie[r] = t;
+    }
+}
+
+// Class starts and members as 0/1 (scanned afterwards).
+__global__ void class_mark_kernel(const uint32_t *__restrict__ tie, uint32_t m,
+                                  uint32_t *__restrict__ start, uint32_t *__restrict__ mem) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        const uint32_t nx = r + 1 < m ? tie[r + 1] : 0u;
+        start[r] = (!tie[r] && nx) ? 1u : 0u;
+        mem[r] = (tie[r] || nx) ? 1u : 0u;
+    }
+}
+
+// cstart / moff per class, (class << 32 | input index) and position per
+// member (cs, ms: exclusive scans of the start and member marks).
+__global__ void class_emit_kernel(const uint32_t *__restrict__ tie, uint32_t m,
+                                  const uint32_t *__restrict__ cs, const uint32_t *__restrict__ ms,
+                                  const uint32_t *__restrict__ idxf,
+                                  const uint32_t *__restrict__ pos32,
+                                  uint32_t *__restrict__ cstart, uint32_t *__restrict__ moff,
+                                  uint64_t *__restrict__ mkey, uint32_t *__restrict__ melem) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        const uint32_t nx = r + 1 < m ? tie[r + 1] : 0u;
+        const bool st = !tie[r] && nx;
+        if (st) {
+            cstart[cs[r]] = r;
+            moff[cs[r]] = ms[r];
+        }
+        if (tie[r] || nx) {
+            const uint32_t ord = st ? cs[r] : cs[r] - 1;
+            mkey[ms[r]] = ((uint64_t)ord << 32) | idxf[r];
+            melem[ms[r]] = pos32[r];
+        }
+    }
+}
+
+struct Classes {
+    uint32_t C, M;               // classes, members
+    uint64_t N;                  // merge-tree inputs
+    const uint32_t *cstart;      // first slot of each class (ascending)
+    const uint32_t *moff;        // first member of each class
+    const uint64_t *mkey;        // (class << 32 | input index), by class then input index
+    const uint32_t *midx;        // input index of each member
+    __device__ __forceinline__ uint32_t size(uint32_t c) const {
+        return (c + 1 < C ? __ldg(moff + c + 1) : M) - __ldg(moff + c);
+    }
+};
+
+__global__ void member_idx_kernel(const uint64_t *__restrict__ mkey, uint32_t M,
+                                  uint32_t *__restrict__ midx) {
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < M; u += gridDim.x * blockDim.x)
+        midx[u] = (uint32_t)mkey[u];
+}
+
+// Split node of consecutive members u, u + 1 (id u - class): their lowest
+// common merge-tree node.
+__global__ void split_info_kernel(Classes K, uint32_t *__restrict__ slo, uint32_t *__restrict__ shi,
+                                  uint32_t *__restrict__ scls, uint32_t *__restrict__ pred) {
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < K.M; u += gridDim.x * blockDim.x) {
+        const uint32_t c = (uint32_t)(K.mkey[u] >> 32);
+        if (u + 1 >= K.moff[c] + K.size(c)) continue;  // the class's last member
+        const uint64_t x = K.midx[u], y = K.midx[u + 1];
+        uint64_t lo = 0, hi = K.N;
+        for (int d = 0; d < kMaxDepth; d++) {
+            const uint64_t mid = lo + (hi - lo) / 2;
+            if (y < mid)
+                hi = mid;
+            else if (x >= mid)
+                lo = mid;
+            else
+                break;
+        }
+        const uint32_t t = u - c;
+        slo[t] = (uint32_t)lo;
+        shi[t] = (uint32_t)(hi - 1);  // inclusive: hi may be 2^32
+        scls[t] = c;
+        pred[t] = 0;
+    }
+}
+
+// One block per class: walk back from the class start; every slot marks the
+// split nodes on its input's path (pred = slot + 1, the largest wins).
+__global__ void __launch_bounds__(256)
+    walk_kernel(Classes K, const uint32_t *__restrict__ idxf, uint32_t *__restrict__ pred,
+                uint32_t *__restrict__ cstate) {
+    __shared__ uint32_t s_found;
+    for (uint32_t c = blockIdx.x; c < K.C; c += gridDim.x) {
+        const uint32_t s = K.cstart[c], mb = K.moff[c], k = K.size(c);
+        if (threadIdx.x == 0) s_found = 0;
+        __syncthreads();
+        uint32_t walked = 0, state = kWalkDone;
+        for (;;) {
+            if (walked >= s) {
+                state = kWalkExhausted;
+                break;
+            }
+            if (walked >= kWalkSlots) {
+                state = kWalkBudget;
+                break;
+            }
+            const uint32_t top = s - walked;  // slots [top - 256, top)
+            if (threadIdx.x < top) {
+                const uint32_t q = top - 1 - threadIdx.x;
+                const uint64_t j = idxf[q];
+                uint32_t a = mb, b = mb + k;
+                uint64_t lo = 0, hi = K.N;
+                for (int d = 0; d < kMaxDepth && b - a >= 2; d++) {
+                    const uint64_t mid = lo + (hi - lo) / 2;
+                    const uint32_t cm = lower_bound_u32(K.midx, a, b, mid);
+                    if (a < cm && cm < b) {
+                        const uint32_t old = atomicMax(&pred[cm - 1 - c], q + 1);
+                        if (old == 0) atomicAdd(&s_found, 1u);
+                    }
+                    if (j < mid) {
+                        b = cm;
+                        hi = mid;
+                    } else {
+                        a = cm;
+                        lo = mid;
+                    }
+                }
+            }
+            walked += 256;
+            __syncthreads();
+            const bool done = s_found == k - 1;
+            __syncthreads();
+            if (done) break;
+        }
+        if (threadIdx.x == 0) cstate[c] = state;
+        __syncthreads();
+    }
+}
+
+// Split nodes the walk did not reach: one warp scans the node's inputs for
+// the largest slot below the class start.
+__global__ void brute_kernel(Classes K, uint32_t S, const uint32_t *__restrict__ slo,
+                             const uint32_t *__restrict__ shi, const uint32_t *__restrict__ scls,
+                             const uint32_t *__restrict__ cstate,
+                             const uint32_t *__restrict__ slot_of, uint32_t *__restrict__ pred) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < S; t += warps) {
+        const uint32_t c = scls[t];
+        if (pred[t] != 0 || cstate[c] != kWalkBudget) continue;
+        const uint32_t s = K.cstart[c];
+        uint32_t best = 0;
+        for (uint64_t j = (uint64_t)slo[t] + lane; j <= shi[t]; j += 32) {
+            const uint32_t q = __ldg(slot_of + j);
+            if (q < s && q + 1 > best) best = q + 1;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+        if (lane == 0) pred[t] = best;
+    }
+}
+
+// Which half goes first at each split node (start: 0 left, 1 right), or a
+// link (dep = split id + 1) to the split node of the preceding class whose
+// last output decides.
+__global__ void resolve_kernel(Classes K, uint32_t S, const uint32_t *__restrict__ slo,
+                               const uint32_t *__restrict__ shi, const uint32_t *__restrict__ pred,
+                               const uint32_t *__restrict__ idxf, uint32_t *__restrict__ start,
+                               uint32_t *__restrict__ dep) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < S; t += gridDim.x * blockDim.x) {
+        const uint64_t lo = slo[t], hi = (uint64_t)shi[t] + 1, mid = lo + (hi - lo) / 2;
+        dep[t] = 0;
+        if (pred[t] == 0) {  // nothing before the class: the left half was "last"
+            start[t] = 1;
+            continue;
+        }
+        const uint32_t q = pred[t] - 1;
+        // the tie class holding slot q, if any
+        uint32_t c2 = 0;
+        {
+            uint32_t a = 0, b = K.C;  // first class starting after q
+            while (a < b) {
+                const uint32_t md = a + ((b - a) >> 1);
+                if (K.cstart[md] <= q)
+                    a = md + 1;
+                else
+                    b = md;
+            }
+            c2 = a;  // classes [0, a) start at or before q
+        }
+        uint32_t last;
+        if (c2 > 0 && q < K.cstart[c2 - 1] + K.size(c2 - 1)) {
+            const uint32_t cc = c2 - 1, mb = K.moff[cc], me = mb + K.size(cc);
+            const uint32_t a = lower_bound_u32(K.midx, mb, me, lo);
+            const uint32_t md = lower_bound_u32(K.midx, a, me, mid);
+            const uint32_t b = lower_bound_u32(K.midx, md, me, hi);
+            const uint32_t cl = md - a, cr = b - md;
+            if (cr == 0)
+                last = 0;
+            else if (cl == 0)
+                last = 1;
+            else if (cl != cr)
+                last = cl > cr ? 0u : 1u;
+            else {  // equal halves: it ended on the half it did not begin with
+                dep[t] = (md - 1 - cc) + 1;
+                continue;
+            }
+        } else {
+            last = (uint64_t)idxf[q] >= mid ? 1u : 0u;
+        }
+        start[t] = 1u - last;
+    }
+}
+
+// start[t] = start of the end of t's link chain (chains run to earlier
+// classes, so they end).
+__global__ void chase_kernel(uint32_t S, const uint32_t *__restrict__ dep,
+                             uint32_t *__restrict__ start, int *__restrict__ err) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < S; t += gridDim.x * blockDim.x) {
+        if (!dep[t]) continue;
+        uint32_t x = dep[t] - 1, steps = 0;
+        while (dep[x] && steps < kChaseLimit) {
+            x = dep[x] - 1;
+            steps++;
+        }
+        if (dep[x]) {
+            atomicCAS(err, DEV_OK, DEV_LOOKBACK_TIMEOUT);
+            continue;
+        }
+        start[t] = start[x];
+    }
+}
+
+// Every member's place in its class: descend to its leaf recording the split
+// nodes on the way, then compose the alternations upwards.
+template <typename OT>
+__global__ void place_kernel(Classes K, const uint32_t *__restrict__ start,
+                             const uint32_t *__restrict__ melem, OT *__restrict__ out) {
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < K.M; u += gridDim.x * blockDim.x) {
+        const uint32_t c = (uint32_t)(K.mkey[u] >> 32);
+        const uint32_t mb = K.moff[c], k = K.size(c);
+        const uint64_t x = K.midx[u];
+        uint32_t pt[kMaxDepth], cl[kMaxDepth], cr[kMaxDepth];
+        uint64_t side = 0;  // bit d: the member is in the right half of split d
+        int depth = 0;
+        uint32_t a = mb, b = mb + k;
+        uint64_t lo = 0, hi = K.N;
+        for (int d = 0; d < kMaxDepth && b - a >= 2; d++) {
+            const uint64_t mid = lo + (hi - lo) / 2;
+            const uint32_t cm = lower_bound_u32(K.midx, a, b, mid);
+            if (a < cm && cm < b) {
+                pt[depth] = cm - 1 - c;
+                cl[depth] = cm - a;
+                cr[depth] = b - cm;
+                if (x >= mid) side |= 1ull << depth;
+                depth++;
+            }
+            if (x < mid) {
+                b = cm;
+                hi = mid;
+            } else {
+                a = cm;
+                lo = mid;
+            }
+        }
+        uint32_t r = 0;
+        for (int d = depth - 1; d >= 0; d--) {
+            const uint32_t sd = (uint32_t)(side >> d) & 1u;
+            const uint32_t p = cl[d] < cr[d] ? cl[d] : cr[d];
+            r = r < p ? 2 * r + (sd == start[pt[d]] ? 0u : 1u) : p + r;
+        }
+        out[K.cstart[c] + r] = (OT)melem[u];
+    }
+}
+
+template <typename PT>
+__global__ void pos_key_kernel(const PT *__restrict__ pos, uint32_t m, uint64_t *__restrict__ key) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+        key[i] = (uint64_t)pos[i];
+}
+
+__global__ void widen_u32_kernel(const uint32_t *__restrict__ v, uint32_t m,
+                                 uint64_t *__restrict__ key) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+        key[i] = v[i];
+}
+
+}  // namespace
+
+capssa_status reference_tie_order(Ctx &c, const TieArgs &t) {
+    const uint64_t m = t.m;
+    if (m < 2) return CAPSSA_OK;
+    if (m > 0xFFFFFFFFull) return set_err(c, CAPSSA_EUNSUPPORTED, "tie order beyond 2^32-1 slots");
+    const uint32_t mm = (uint32_t)m;
+    const size_t m4 = (size_t)m * 4 + 64, m8 = (size_t)m * 8 + 64;
+    uint32_t *pos32 = (uint32_t *)ws_get(c, WS_MISC, 2 * m4);
+    uint32_t *cs = (uint32_t *)ws_get(c, WS_MISC2, 2 * m4);
+    uint32_t *maps = (uint32_t *)ws_get(c, WS_MISC3, 2 * m4);
+    uint64_t *ka = (uint64_t *)ws_get(c, WS_KEYS_A, m8);
+    uint64_t *kb = (uint64_t *)ws_get(c, WS_KEYS_B, std::max(m8, scatter_hist_words(m) * 4));
+    uint32_t *va = (uint32_t *)ws_get(c, WS_VALS_A, m4);
+    uint32_t *vb = (uint32_t *)ws_get(c, WS_VALS_B, m4);
+    if (!pos32 || !cs || !maps || !ka || !kb || !va || !vb)
+        return set_err(c, CAPSSA_ENOMEM, "tie order workspace");
+    uint32_t *tie = pos32 + m4 / 4, *ms = cs + m4 / 4;
+    uint32_t *idxf = maps, *slot_of = maps + m4 / 4;
+    const unsigned g = grid_for(m, 256);
+    // 1. classes: adjacent Equal pairs
+    if (t.out_bytes == 8)
+        tie_flag_kernel<uint64_t><<<g, 256, 0, c.stream>>>((const uint64_t *)t.out, mm, t.key,
+                                                           (const uint8_t *)t.text, t.sym_bytes,
+                                                           t.lim, t.max_ctx, pos32, tie);
+    else
+        tie_flag_kernel<uint32_t><<<g, 256, 0, c.stream>>>((const uint32_t *)t.out, mm, t.key,
+                                                           (const uint8_t *)t.text, t.sym_bytes,
+                                                           t.lim, t.max_ctx, pos32, tie);
+    CAPSSA_LAUNCHED(c);
+    class_mark_kernel<<<g, 256, 0, c.stream>>>(tie, mm, cs, ms);
+    CAPSSA_LAUNCHED(c);
+    capssa_status s = scan_u32(c, cs, cs, m, false, false);
+    if (s != CAPSSA_OK) return s;
+    s = scan_u32(c, ms, ms, m, false, false);
+    if (s != CAPSSA_OK) return s;
+    uint32_t *h = (uint32_t *)c.h_scratch;
+    CAPSSA_CUDA(c, cudaMemcpyAsync(h, cs + (m - 1), 4, cudaMemcpyDeviceToHost, c.stream));
+    CAPSSA_CUDA(c, cudaMemcpyAsync(h + 1, ms + (m - 1), 4, cudaMemcpyDeviceToHost, c.stream));
+    CAPSSA_CUDA(c, cudaMemcpyAsync(h + 2, tie + (m - 1), 4, cudaMemcpyDeviceToHost, c.stream));
+    CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+    const uint32_t C = h[0], M = h[1] + h[2];
+    c.stats.tie_classes = C;
+    if (C == 0) return CAPSSA_OK;
+    // 2. input index of every slot and slot of every input index
+    if (!t.positions) {  // a whole text: the input index is the position
+        idxf = pos32;
+        s = scatter_u32(c, pos32, nullptr, m, slot_of, m, ka, (uint32_t *)kb);
+        if (s != CAPSSA_OK) return s;
+    } else {
+        // inputs and slots, each sorted by position (stably): the j-th of
+        // both name the same suffix (repeated positions pair up in order)
+        if (t.pos_bytes == 8)
+            pos_key_kernel<uint64_t><<<g, 256, 0, c.stream>>>((const uint64_t *)t.positions, mm,
+                                                              ka);
+        else
+            pos_key_kernel<uint32_t><<<g, 256, 0, c.stream>>>((const uint32_t *)t.positions, mm,
+                                                              ka);
+        CAPSSA_LAUNCHED(c);
+        const int pbits = bits_upto(t.lim.n);
+        bool in_b = false;
+        s = radix::sort_pairs(c, ka, va, kb, vb, mm, 0, pbits, true, 0, &in_b);
+        if (s != CAPSSA_OK) return s;
+        uint32_t *inp = in_b ? vb : va;  // input indices by position
+        uint32_t *spare = in_b ? va : vb;
+        // slots by position: keys in kb (or ka), values in `spare` and idxf
+        uint64_t *kx = in_b ? ka : kb, *ky = in_b ? kb : ka;
+        widen_u32_kernel<<<g, 256, 0, c.stream>>>(pos32, mm, kx);
+        CAPSSA_LAUNCHED(c);
+        s = radix::sort_pairs(c, kx, spare, ky, slot_of, mm, 0, pbits, true, 0, &in_b);
+        if (s != CAPSSA_OK) return s;
+        uint32_t *slots = in_b ? slot_of : spare;
+        // idxf[slot] = input; then slot_of[input] = slot (sorted keys are dead:
+        // they hold the window pairs and counts)
+        uint32_t *sl = slots;
+        if (slots == slot_of) {  // keep slot_of free for its own scatter
+            CAPSSA_CUDA(c, cudaMemcpyAsync(spare, slots, m * 4, cudaMemcpyDeviceToDevice,
+                                           c.stream));
+            sl = spare;
+        }
+        s = scatter_u32(c, sl, inp, m, idxf, m, ka, (uint32_t *)kb);
+        if (s != CAPSSA_OK) return s;
+        s = scatter_u32(c, inp, sl, m, slot_of, m, ka, (uint32_t *)kb);
+        if (s != CAPSSA_OK) return s;
+        // pos32 still holds the slots' positions; `inp` and `sl` are dead
+    }
+    // 3. members by class, then by input index
+    const size_t c4 = (size_t)C * 4 + 64, s4 = (size_t)(M - C) * 4 + 64;
+    char *w = (char *)ws_get(c, WS_PART, 3 * c4 + 6 * s4 + (size_t)M * 4 + 64);
+    if (!w) return set_err(c, CAPSSA_ENOMEM, "tie order workspace");
+    uint32_t *cstart = (uint32_t *)w, *moff = cstart + c4 / 4, *cstate = moff + c4 / 4;
+    uint32_t *slo = cstate + c4 / 4, *shi = slo + s4 / 4, *scls = shi + s4 / 4;
+    uint32_t *pred = scls + s4 / 4, *start = pred + s4 / 4, *dep = start + s4 / 4;
+    uint32_t *midx = dep + s4 / 4;
+    // members into ka / va (the maps above no longer need them)
+    class_emit_kernel<<<g, 256, 0, c.stream>>>(tie, mm, cs, ms, idxf, pos32, cstart, moff, ka, va);
+    CAPSSA_LAUNCHED(c);
+    bool in_b = false;
+    s = radix::sort_pairs(c, ka, va, kb, vb, M, 0, 32 + bits_upto(C - 1), false, 0, &in_b);
+    if (s != CAPSSA_OK) return s;
+    const uint64_t *mkey = in_b ? kb : ka;
+    const uint32_t *melem = in_b ? vb : va;
+    const unsigned gM = grid_for(M, 256);
+    member_idx_kernel<<<gM, 256, 0, c.stream>>>(mkey, M, midx);
+    CAPSSA_LAUNCHED(c);
+    Classes K{C, M, m, cstart, moff, mkey, midx};
+    const uint32_t S = M - C;
+    split_info_kernel<<<gM, 256, 0, c.stream>>>(K, slo, shi, scls, pred);
+    CAPSSA_LAUNCHED(c);
+    // 4. predecessors: walk, then scan what the walk left
+    walk_kernel<<<std::min<uint32_t>(C, (uint32_t)c.sm_count * 16), 256, 0, c.stream>>>(
+        K, idxf, pred, cstate);
+    CAPSSA_LAUNCHED(c);
+    brute_kernel<<<grid_for((uint64_t)S * 32, 256, (unsigned)c.sm_count * 32), 256, 0,
+                   c.stream>>>(K, S, slo, shi, scls, cstate, slot_of, pred);
+    CAPSSA_LAUNCHED(c);
+    // 5. first halves, links, places
+    const unsigned gS = grid_for(S, 256);
+    resolve_kernel<<<gS, 256, 0, c.stream>>>(K, S, slo, shi, pred, idxf, start, dep);
+    CAPSSA_LAUNCHED(c);
+    chase_kernel<<<gS, 256, 0, c.stream>>>(S, dep, start, c.d_flags);
+    CAPSSA_LAUNCHED(c);
+    if (t.out_bytes == 8)
+        place_kernel<uint64_t><<<gM, 256, 0, c.stream>>>(K, start, melem, (uint64_t *)t.out);
+    else
+        place_kernel<uint32_t><<<gM, 256, 0, c.stream>>>(K, start, melem, (uint32_t *)t.out);
+    CAPSSA_LAUNCHED(c);
+    return CAPSSA_OK;
+}
+
+}  // namespace capssa

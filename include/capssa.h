@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define CAPSSA_ABI_VERSION 4
+#define CAPSSA_ABI_VERSION 5
 
 typedef enum capssa_status {
     CAPSSA_OK = 0,
@@ -95,6 +95,20 @@ typedef enum {
     CAPSSA_SAMPLING_PARTITION_FIRST = 2
 } capssa_sampling;
 
+/* Order inside a tie class: suffixes the comparator calls Equal, which only
+ * SegmentedText under ShorterFirst has (equal symbols up to equal limits).
+ * The reference leaves it unpinned (src/sample_sort.rs:908-913); its merge
+ * sort emits each class in a fixed order all the same. */
+typedef enum {
+    /* ascending input order (position for a whole text, index in the
+     * positions array for a subset) */
+    CAPSSA_TIES_POSITION = 0,
+    /* the order the reference's in-memory merge sort emits
+     * (build_in_memory* and build_in_memory_for_positions*:
+     * src/sample_sort.rs:221-266, 430-497); the in-memory builders only */
+    CAPSSA_TIES_REFERENCE = 1
+} capssa_tie_order;
+
 /* Opts{max_context} (src/sample_sort.rs:70-85) and the in-memory subset of
  * ExtMemOpts (src/ext_mem.rs:60-118).  Zero-initialise, then set
  * max_context = CAPSSA_UNBOUNDED for the reference default. */
@@ -107,7 +121,7 @@ typedef struct capssa_opts {
     int32_t host_threads;      /* thread count the auto p rule assumes; 0 = all cores */
     uint64_t flags;            /* no flags are defined: 0 */
     int32_t sampling;          /* capssa_sampling (sample-sort builders and plans) */
-    int32_t reserved32;
+    int32_t tie_order;         /* capssa_tie_order (in-memory builders) */
     uint64_t reserved[4];
 } capssa_opts;
 
@@ -148,6 +162,9 @@ typedef struct capssa_stats {
     uint32_t radix_items;       /* records per thread of the radix passes (the context's
                                    autotuner picks it on its first large sort of each kind) */
     uint32_t sparse_subset;     /* 1: a subset build sorted only its own positions */
+    uint32_t tie_classes;       /* tie classes of the output (CAPSSA_TIES_REFERENCE) */
+    uint32_t reserved_u32;
+    double tie_order_ms;        /* device time of the reference tie order */
 } capssa_stats;
 
 typedef struct capssa_ctx capssa_ctx;

@@ -62,7 +62,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_defaults(lib):
-    assert lib.capssa_abi_version() == 4
+    assert lib.capssa_abi_version() == 5
 
     class Opts(ctypes.Structure):
         _fields_ = [("max_context", ctypes.c_uint64), ("subproblem_count", ctypes.c_uint64),

@@ -9,8 +9,9 @@
   C3  n = 2^29 segmented text, the positions with text[p] < 4, u64:
       ShorterFirst equal after canonicalising each tie class (the reference
       leaves the order inside a class unpinned, src/sample_sort.rs:908-934),
-      with the GPU's classes in ascending position; the same positions under
-      the STAR LongerFirst order (a total order): bit-exact.
+      with the GPU's classes in ascending position; with the reference tie
+      order requested, bit-exact; the same positions under the STAR
+      LongerFirst order (a total order): bit-exact.
   C5  8,192 texts sorted in one batched call: every 8th text and the longest
       one bit-exact against the oracle, text by text.
 
@@ -47,6 +48,13 @@ def c2():
 def c3():
     from capssa import workloads
     return workloads.segmented_filtered(1 << 29)
+
+
+@pytest.fixture(scope="module")
+def c3_want(c3):
+    """The oracle's ShorterFirst order of C3 (the reference's, ties included)."""
+    text, ends, pos = c3
+    return orc.build_in_memory(text, pos, orc.Limits(len(text), ends), index=np.uint64)
 
 
 def test_c2_bench_text_2p28_bit_exact(ctx, c2):
@@ -110,23 +118,37 @@ def test_c2_small_subset_2p28_sorted_alone(ctx, c2):
     assert sub_ms < full_ms / 4
 
 
-def test_c3_segmented_filtered_2p29(ctx, c3):
+def test_c3_segmented_filtered_2p29(ctx, c3, c3_want):
     text, ends, pos = c3
     n = len(text)
     lp = capssa.SegmentedText(n, ends)
     lo = orc.Limits(n, ends)
     got = ctx.build_in_memory_for_positions(text, pos, lp)
     assert got.dtype == np.uint64 and len(got) == len(pos)
-    want = orc.build_in_memory(text, pos, lo, index=np.uint64)
+    want = c3_want
     cw = orc.adjacent_cmp(text, want, lo)
     assert (cw <= 0).all()
     canon = orc.canonical_ties(want, cw)
     assert np.array_equal(orc.canonical_ties(got, cw), canon)
     assert np.array_equal(got, canon)  # GPU tie classes in ascending position
-    del want, canon
+    del canon
     # the filter source gives the same order
     f = ctx.build_in_memory_for_filter(text, 0, 4, lp=lp, index=np.uint64)
     assert np.array_equal(f, got)
+
+
+def test_c3_reference_tie_order_2p29_bit_exact(ctx, c3, c3_want):
+    """The same positions in the reference's own tie order: the output equals
+    the oracle's merge sort element for element."""
+    text, ends, pos = c3
+    lp = capssa.SegmentedText(len(text), ends)
+    opts = capssa.Opts(tie_order=capssa.TieOrder.REFERENCE)
+    got = ctx.build_in_memory_for_positions(text, pos, lp, opts)
+    st = ctx.stats()
+    print("C3 tie classes %d, reference tie order %.2f ms of %.2f ms" %
+          (st["tie_classes"], st["tie_order_ms"], st["device_ms"]))
+    assert st["tie_classes"] > 0
+    assert np.array_equal(got, c3_want)
 
 
 def test_c3_star_order_2p29_bit_exact(ctx, c3):
