@@ -339,6 +339,11 @@ def run_forms(ctx, t_dev, n):
     lp3 = capssa.SegmentedText(len(text3), ends3)
     ctx.build_in_memory_for_positions(t3, p3, lp3, out=o3)  # warm
     s_ms = _timed(lambda: ctx.build_in_memory_for_positions(t3, p3, lp3, out=o3), 2)
+    # the same with every tie class in the reference's merge order
+    ref_ties = capssa.Opts(tie_order=capssa.TieOrder.REFERENCE)
+    ctx.build_in_memory_for_positions(t3, p3, lp3, ref_ties, out=o3)  # warm
+    r_ms = _timed(lambda: ctx.build_in_memory_for_positions(t3, p3, lp3, ref_ties, out=o3), 2)
+    r_st = ctx.stats()
     # the same through the GPU filter source (positions selected on the device)
     ctx.build_in_memory_for_filter(t3, 0, 4, lp3, out=o3)
     f_ms = _timed(lambda: ctx.build_in_memory_for_filter(t3, 0, 4, lp3, out=o3), 2)
@@ -358,6 +363,11 @@ def run_forms(ctx, t_dev, n):
     out["segmented_filtered_2p29"] = {"value": len(pos3) / (s_ms / 1e3) / 1e6,
                                       "unit": "Msuffixes/s", "ms": s_ms,
                                       "positions": int(len(pos3)), "segments": int(len(ends3)),
+                                      "reference_tie_order": {
+                                          "value": len(pos3) / (r_ms / 1e3) / 1e6,
+                                          "unit": "Msuffixes/s", "ms": r_ms,
+                                          "tie_order_ms": r_st["tie_order_ms"],
+                                          "tie_classes": int(r_st["tie_classes"])},
                                       "filter_source": {"value": len(pos3) / (f_ms / 1e3) / 1e6,
                                                         "unit": "Msuffixes/s", "ms": f_ms},
                                       "ext_mem_for_filter": {

@@ -7,6 +7,8 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <cstdio>
+#include <cstdlib>
 
 #include <string>
 #include <vector>
@@ -177,5 +179,51 @@ inline unsigned grid_for(uint64_t n, unsigned block, unsigned cap = 1u << 30) {
     if (g > cap) g = cap;
     return (unsigned)g;
 }
+
+// CAPSSA_PROFILE in the environment turns on per-phase / per-round lines on
+// stderr, like the reference's CAPS_SA_PROFILE profile_log
+// (src/ext_mem.rs:42-51).
+inline bool profile_on() {
+    static const bool on = std::getenv("CAPSSA_PROFILE") != nullptr;
+    return on;
+}
+
+// Per-kernel device times of one phase (a refinement round, the tie
+// order), printed on one line when CAPSSA_PROFILE is set (events only then).
+struct KernelTimes {
+    static constexpr int kMax = 12;
+    cudaEvent_t ev[kMax + 1] = {};
+    const char *name[kMax] = {};
+    int used = 0;
+    bool on = false;
+    explicit KernelTimes(bool enable) : on(enable) {
+        if (on)
+            for (auto &e : ev) cudaEventCreate(&e);
+    }
+    ~KernelTimes() {
+        if (on)
+            for (auto &e : ev) cudaEventDestroy(e);
+    }
+    void start(cudaStream_t s) {
+        used = 0;
+        if (on) cudaEventRecord(ev[0], s);
+    }
+    void mark(cudaStream_t s, const char *what) {
+        if (!on || used >= kMax) return;
+        name[used] = what;
+        cudaEventRecord(ev[++used], s);
+    }
+    void print() {
+        if (!on || !used) return;
+        cudaEventSynchronize(ev[used]);
+        std::fprintf(stderr, "capssa profile    kernels:");
+        for (int i = 0; i < used; i++) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+            std::fprintf(stderr, " %s %.3f ms", name[i], ms);
+        }
+        std::fprintf(stderr, "\n");
+    }
+};
 
 }  // namespace capssa

@@ -2280,52 +2280,6 @@ __global__ void pf_train_set_kernel(const uint32_t *__restrict__ spos,
 
 // ---------------------------------------------------------------- host
 
-// CAPSSA_PROFILE in the environment turns on per-phase / per-round lines on
-// stderr, like the reference's CAPS_SA_PROFILE profile_log
-// (src/ext_mem.rs:42-51).
-inline bool profile_on() {
-    static const bool on = std::getenv("CAPSSA_PROFILE") != nullptr;
-    return on;
-}
-
-// Per-kernel device times of one refinement round, printed with the
-// round's line when CAPSSA_PROFILE is set (events only in that case).
-struct KernelTimes {
-    static constexpr int kMax = 12;
-    cudaEvent_t ev[kMax + 1] = {};
-    const char *name[kMax] = {};
-    int used = 0;
-    bool on = false;
-    explicit KernelTimes(bool enable) : on(enable) {
-        if (on)
-            for (auto &e : ev) cudaEventCreate(&e);
-    }
-    ~KernelTimes() {
-        if (on)
-            for (auto &e : ev) cudaEventDestroy(e);
-    }
-    void start(cudaStream_t s) {
-        used = 0;
-        if (on) cudaEventRecord(ev[0], s);
-    }
-    void mark(cudaStream_t s, const char *what) {
-        if (!on || used >= kMax) return;
-        name[used] = what;
-        cudaEventRecord(ev[++used], s);
-    }
-    void print() {
-        if (!on || !used) return;
-        cudaEventSynchronize(ev[used]);
-        std::fprintf(stderr, "capssa profile    kernels:");
-        for (int i = 0; i < used; i++) {
-            float ms = 0;
-            cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
-            std::fprintf(stderr, " %s %.3f ms", name[i], ms);
-        }
-        std::fprintf(stderr, "\n");
-    }
-};
-
 inline int bits_for(uint64_t v) {  // bits to represent 0..v
     int b = 0;
     while (b < 64 && (v >> b) != 0) b++;

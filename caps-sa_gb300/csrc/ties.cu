@@ -70,8 +70,15 @@ __global__ void tie_flag_kernel(const OT *__restrict__ out, uint32_t m,
                                 const uint8_t *__restrict__ text, int sym_bytes, DevLimits L,
                                 uint64_t max_ctx, uint32_t *__restrict__ pos32,
                                 uint32_t *__restrict__ tie) {
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
-        const uint32_t b = (uint32_t)out[r];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t r0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); r0 < m; r0 += stride) {
+        // whole warps step together: a slot's limit is its left neighbour's too
+        const uint32_t lane = threadIdx.x & 31, r = r0 + lane;
+        const bool in = r < m;
+        const uint32_t b = in ? (uint32_t)out[r] : 0u;
+        const uint64_t lb = key || !in ? 0ull : dev_lim_at(L, b);
+        const uint64_t lup = __shfl_up_sync(0xffffffffu, lb, 1);
+        if (!in) continue;
         pos32[r] = b;
         uint32_t t = 0;
         if (r > 0) {
@@ -79,7 +86,7 @@ __global__ void tie_flag_kernel(const OT *__restrict__ out, uint32_t m,
                 t = key[r] == key[r - 1];
             } else {  // suffix_cmp_with Equal: same limit, same symbols up to it (or max_ctx)
                 const uint32_t a = (uint32_t)out[r - 1];
-                const uint64_t la = dev_lim_at(L, a), lb = dev_lim_at(L, b);
+                const uint64_t la = lane ? lup : dev_lim_at(L, a);
                 if (la == lb) {
                     const uint64_t lim = la < max_ctx ? la : max_ctx;
                     const uint64_t k = (uint64_t)sym_bytes;
@@ -92,36 +99,46 @@ __global__ void tie_flag_kernel(const OT *__restrict__ out, uint32_t m,
     }
 }
 
-// Class starts and members as 0/1 (scanned afterwards).
-__global__ void class_mark_kernel(const uint32_t *__restrict__ tie, uint32_t m,
-                                  uint32_t *__restrict__ start, uint32_t *__restrict__ mem) {
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
-        const uint32_t nx = r + 1 < m ? tie[r + 1] : 0u;
-        start[r] = (!tie[r] && nx) ? 1u : 0u;
-        mem[r] = (tie[r] || nx) ? 1u : 0u;
-    }
+// Member marks (0/1, scanned afterwards): slots tied to a neighbour.
+__global__ void member_mark_kernel(const uint32_t *__restrict__ tie, uint32_t m,
+                                   uint32_t *__restrict__ mem) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x)
+        mem[r] = (tie[r] || (r + 1 < m && tie[r + 1])) ? 1u : 0u;
+}
+
+// The members' slots, in slot order (ms: exclusive scan of the marks).
+__global__ void member_list_kernel(const uint32_t *__restrict__ tie, uint32_t m,
+                                   const uint32_t *__restrict__ ms, uint32_t *__restrict__ slot) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x)
+        if (tie[r] || (r + 1 < m && tie[r + 1])) slot[ms[r]] = r;
+}
+
+// Class-start marks over the member list (a member not tied to its left).
+__global__ void start_mark_kernel(const uint32_t *__restrict__ tie, const uint32_t *__restrict__ slot,
+                                  uint32_t M, uint32_t *__restrict__ st) {
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < M; u += gridDim.x * blockDim.x)
+        st[u] = tie[slot[u]] ? 0u : 1u;
 }
 
 // cstart / moff per class, (class << 32 | input index) and position per
-// member (cs, ms: exclusive scans of the start and member marks).
-__global__ void class_emit_kernel(const uint32_t *__restrict__ tie, uint32_t m,
-                                  const uint32_t *__restrict__ cs, const uint32_t *__restrict__ ms,
+// member (cs: exclusive scan of the start marks over the member list).
+__global__ void class_emit_kernel(const uint32_t *__restrict__ tie,
+                                  const uint32_t *__restrict__ slot, uint32_t M,
+                                  const uint32_t *__restrict__ cs,
                                   const uint32_t *__restrict__ idxf,
                                   const uint32_t *__restrict__ pos32,
                                   uint32_t *__restrict__ cstart, uint32_t *__restrict__ moff,
                                   uint64_t *__restrict__ mkey, uint32_t *__restrict__ melem) {
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
-        const uint32_t nx = r + 1 < m ? tie[r + 1] : 0u;
-        const bool st = !tie[r] && nx;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < M; u += gridDim.x * blockDim.x) {
+        const uint32_t r = slot[u];
+        const bool st = !tie[r];
+        const uint32_t ord = st ? cs[u] : cs[u] - 1;
         if (st) {
-            cstart[cs[r]] = r;
-            moff[cs[r]] = ms[r];
+            cstart[ord] = r;
+            moff[ord] = u;
         }
-        if (tie[r] || nx) {
-            const uint32_t ord = st ? cs[r] : cs[r] - 1;
-            mkey[ms[r]] = ((uint64_t)ord << 32) | idxf[r];
-            melem[ms[r]] = pos32[r];
-        }
+        mkey[u] = ((uint64_t)ord << 32) | idxf[r];
+        melem[u] = pos32[r];
     }
 }
 
@@ -358,6 +375,48 @@ __global__ void place_kernel(Classes K, const uint32_t *__restrict__ start,
     }
 }
 
+// err[0] = 1 unless the positions strictly ascend.
+template <typename PT>
+__global__ void ascending_kernel(const PT *__restrict__ pos, uint32_t m, uint32_t *__restrict__ err) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i + 1 < m;
+         i += gridDim.x * blockDim.x)
+        if (pos[i] >= pos[i + 1]) *err = 1;
+}
+
+// One bit per chosen position.  Positions ascend, so a warp's lanes mostly
+// share words: the lanes of one word combine their bits and one of them
+// writes the word.
+template <typename PT>
+__global__ void pos_bits_kernel(const PT *__restrict__ pos, uint32_t m, uint32_t *__restrict__ bits) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < m; i0 += stride) {
+        const uint32_t i = i0 + (threadIdx.x & 31);
+        const uint64_t p = i < m ? (uint64_t)pos[i] : ~0ull;
+        const uint32_t w = (uint32_t)(p >> 5);  // past the end: a word no position has
+        const unsigned peers = __match_any_sync(0xffffffffu, w);
+        const uint32_t v = __reduce_or_sync(peers, i < m ? 1u << (p & 31) : 0u);
+        if (i < m && (threadIdx.x & 31) == (uint32_t)(__ffs((int)peers) - 1)) atomicOr(&bits[w], v);
+    }
+}
+
+__global__ void popc_words_kernel(const uint32_t *__restrict__ bits, uint64_t nw,
+                                  uint32_t *__restrict__ wc) {
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nw;
+         w += (uint64_t)gridDim.x * blockDim.x)
+        wc[w] = __popc(bits[w]);
+}
+
+// Input index of each slot for ascending positions: the rank of its position
+// among them (words' prefix counts + the bits below it in its word).
+__global__ void pos_rank_kernel(const uint32_t *__restrict__ pos32, uint32_t m,
+                                const uint32_t *__restrict__ bits,
+                                const uint32_t *__restrict__ wc, uint32_t *__restrict__ idxf) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        const uint32_t p = pos32[r];
+        idxf[r] = wc[p >> 5] + __popc(bits[p >> 5] & ((1u << (p & 31)) - 1u));
+    }
+}
+
 template <typename PT>
 __global__ void pos_key_kernel(const PT *__restrict__ pos, uint32_t m, uint64_t *__restrict__ key) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
@@ -390,6 +449,8 @@ capssa_status reference_tie_order(Ctx &c, const TieArgs &t) {
     uint32_t *tie = pos32 + m4 / 4, *ms = cs + m4 / 4;
     uint32_t *idxf = maps, *slot_of = maps + m4 / 4;
     const unsigned g = grid_for(m, 256);
+    KernelTimes kt(profile_on());
+    kt.start(c.stream);
     // 1. classes: adjacent Equal pairs
     if (t.out_bytes == 8)
         tie_flag_kernel<uint64_t><<<g, 256, 0, c.stream>>>((const uint64_t *)t.out, mm, t.key,
@@ -400,24 +461,74 @@ capssa_status reference_tie_order(Ctx &c, const TieArgs &t) {
                                                            (const uint8_t *)t.text, t.sym_bytes,
                                                            t.lim, t.max_ctx, pos32, tie);
     CAPSSA_LAUNCHED(c);
-    class_mark_kernel<<<g, 256, 0, c.stream>>>(tie, mm, cs, ms);
+    kt.mark(c.stream, "flags");
+    // members (slots tied to a neighbour) listed in slot order into `cs`,
+    // then class starts numbered over that list in `ms`
+    member_mark_kernel<<<g, 256, 0, c.stream>>>(tie, mm, ms);
     CAPSSA_LAUNCHED(c);
-    capssa_status s = scan_u32(c, cs, cs, m, false, false);
-    if (s != CAPSSA_OK) return s;
-    s = scan_u32(c, ms, ms, m, false, false);
+    capssa_status s = scan_u32(c, ms, ms, m, false, false);
     if (s != CAPSSA_OK) return s;
     uint32_t *h = (uint32_t *)c.h_scratch;
-    CAPSSA_CUDA(c, cudaMemcpyAsync(h, cs + (m - 1), 4, cudaMemcpyDeviceToHost, c.stream));
-    CAPSSA_CUDA(c, cudaMemcpyAsync(h + 1, ms + (m - 1), 4, cudaMemcpyDeviceToHost, c.stream));
-    CAPSSA_CUDA(c, cudaMemcpyAsync(h + 2, tie + (m - 1), 4, cudaMemcpyDeviceToHost, c.stream));
+    uint32_t *h_err = (uint32_t *)(c.d_flags + 1);  // a scratch device word
+    CAPSSA_CUDA(c, cudaMemcpyAsync(h, ms + (m - 1), 4, cudaMemcpyDeviceToHost, c.stream));
+    CAPSSA_CUDA(c, cudaMemcpyAsync(h + 1, tie + (m - 1), 4, cudaMemcpyDeviceToHost, c.stream));
     CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
-    const uint32_t C = h[0], M = h[1] + h[2];
+    const uint32_t M = h[0] + h[1];  // the last slot is a member iff tied to its left
+    c.stats.tie_classes = 0;
+    if (M == 0) return CAPSSA_OK;
+    uint32_t *mslot = cs;
+    member_list_kernel<<<g, 256, 0, c.stream>>>(tie, mm, ms, mslot);
+    CAPSSA_LAUNCHED(c);
+    const unsigned gM = grid_for(M, 256);
+    uint32_t *cord = ms;  // the member scan is dead once the list is written
+    start_mark_kernel<<<gM, 256, 0, c.stream>>>(tie, mslot, M, cord);
+    CAPSSA_LAUNCHED(c);
+    s = scan_u32(c, cord, cord, M, false, false);
+    if (s != CAPSSA_OK) return s;
+    CAPSSA_CUDA(c, cudaMemcpyAsync(h, cord + (M - 1), 4, cudaMemcpyDeviceToHost, c.stream));
+    CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+    const uint32_t C = h[0];  // an exclusive count: the last member never starts a class
     c.stats.tie_classes = C;
-    if (C == 0) return CAPSSA_OK;
+    kt.mark(c.stream, "classes");
     // 2. input index of every slot and slot of every input index
+    bool ascending = false;
+    if (t.positions) {  // strictly ascending positions (a filter's) rank through a bitmap
+        CAPSSA_CUDA(c, cudaMemsetAsync(h_err, 0, 4, c.stream));
+        if (t.pos_bytes == 8)
+            ascending_kernel<uint64_t><<<g, 256, 0, c.stream>>>((const uint64_t *)t.positions, mm,
+                                                                h_err);
+        else
+            ascending_kernel<uint32_t><<<g, 256, 0, c.stream>>>((const uint32_t *)t.positions, mm,
+                                                                h_err);
+        CAPSSA_LAUNCHED(c);
+        CAPSSA_CUDA(c, cudaMemcpyAsync(h, h_err, 4, cudaMemcpyDeviceToHost, c.stream));
+        CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+        ascending = h[0] == 0;
+    }
     if (!t.positions) {  // a whole text: the input index is the position
         idxf = pos32;
         s = scatter_u32(c, pos32, nullptr, m, slot_of, m, ka, (uint32_t *)kb);
+        if (s != CAPSSA_OK) return s;
+    } else if (ascending) {
+        const uint64_t nw = (t.lim.n + 1) / 32 + 1;  // position n included
+        uint32_t *bits = (uint32_t *)ws_get(c, WS_KEEP, nw * 4 + 64);
+        uint32_t *wc = (uint32_t *)ws_get(c, WS_RANK, nw * 4 + 64);
+        if (!bits || !wc) return set_err(c, CAPSSA_ENOMEM, "tie order workspace");
+        CAPSSA_CUDA(c, cudaMemsetAsync(bits, 0, nw * 4, c.stream));
+        if (t.pos_bytes == 8)
+            pos_bits_kernel<uint64_t><<<g, 256, 0, c.stream>>>((const uint64_t *)t.positions, mm,
+                                                               bits);
+        else
+            pos_bits_kernel<uint32_t><<<g, 256, 0, c.stream>>>((const uint32_t *)t.positions, mm,
+                                                               bits);
+        CAPSSA_LAUNCHED(c);
+        popc_words_kernel<<<grid_for(nw, 256), 256, 0, c.stream>>>(bits, nw, wc);
+        CAPSSA_LAUNCHED(c);
+        s = scan_u32(c, wc, wc, nw, false, false);
+        if (s != CAPSSA_OK) return s;
+        pos_rank_kernel<<<g, 256, 0, c.stream>>>(pos32, mm, bits, wc, idxf);
+        CAPSSA_LAUNCHED(c);
+        s = scatter_u32(c, idxf, nullptr, m, slot_of, m, ka, (uint32_t *)kb);
         if (s != CAPSSA_OK) return s;
     } else {
         // inputs and slots, each sorted by position (stably): the j-th of
@@ -456,6 +567,7 @@ capssa_status reference_tie_order(Ctx &c, const TieArgs &t) {
         if (s != CAPSSA_OK) return s;
         // pos32 still holds the slots' positions; `inp` and `sl` are dead
     }
+    kt.mark(c.stream, "maps");
     // 3. members by class, then by input index
     const size_t c4 = (size_t)C * 4 + 64, s4 = (size_t)(M - C) * 4 + 64;
     char *w = (char *)ws_get(c, WS_PART, 3 * c4 + 6 * s4 + (size_t)M * 4 + 64);
@@ -465,27 +577,30 @@ capssa_status reference_tie_order(Ctx &c, const TieArgs &t) {
     uint32_t *pred = scls + s4 / 4, *start = pred + s4 / 4, *dep = start + s4 / 4;
     uint32_t *midx = dep + s4 / 4;
     // members into ka / va (the maps above no longer need them)
-    class_emit_kernel<<<g, 256, 0, c.stream>>>(tie, mm, cs, ms, idxf, pos32, cstart, moff, ka, va);
+    class_emit_kernel<<<gM, 256, 0, c.stream>>>(tie, mslot, M, cord, idxf, pos32, cstart, moff,
+                                                ka, va);
     CAPSSA_LAUNCHED(c);
     bool in_b = false;
     s = radix::sort_pairs(c, ka, va, kb, vb, M, 0, 32 + bits_upto(C - 1), false, 0, &in_b);
     if (s != CAPSSA_OK) return s;
     const uint64_t *mkey = in_b ? kb : ka;
     const uint32_t *melem = in_b ? vb : va;
-    const unsigned gM = grid_for(M, 256);
     member_idx_kernel<<<gM, 256, 0, c.stream>>>(mkey, M, midx);
     CAPSSA_LAUNCHED(c);
     Classes K{C, M, m, cstart, moff, mkey, midx};
     const uint32_t S = M - C;
     split_info_kernel<<<gM, 256, 0, c.stream>>>(K, slo, shi, scls, pred);
     CAPSSA_LAUNCHED(c);
+    kt.mark(c.stream, "members");
     // 4. predecessors: walk, then scan what the walk left
     walk_kernel<<<std::min<uint32_t>(C, (uint32_t)c.sm_count * 16), 256, 0, c.stream>>>(
         K, idxf, pred, cstate);
     CAPSSA_LAUNCHED(c);
+    kt.mark(c.stream, "walk");
     brute_kernel<<<grid_for((uint64_t)S * 32, 256, (unsigned)c.sm_count * 32), 256, 0,
                    c.stream>>>(K, S, slo, shi, scls, cstate, slot_of, pred);
     CAPSSA_LAUNCHED(c);
+    kt.mark(c.stream, "scan");
     // 5. first halves, links, places
     const unsigned gS = grid_for(S, 256);
     resolve_kernel<<<gS, 256, 0, c.stream>>>(K, S, slo, shi, pred, idxf, start, dep);
@@ -497,6 +612,11 @@ capssa_status reference_tie_order(Ctx &c, const TieArgs &t) {
     else
         place_kernel<uint32_t><<<gM, 256, 0, c.stream>>>(K, start, melem, (uint32_t *)t.out);
     CAPSSA_LAUNCHED(c);
+    kt.mark(c.stream, "place");
+    if (profile_on())
+        std::fprintf(stderr, "capssa profile  tie order: %u classes, %u members, %u split nodes\n",
+                     C, M, S);
+    kt.print();
     return CAPSSA_OK;
 }
 
