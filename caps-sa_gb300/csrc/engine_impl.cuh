@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <type_traits>
 #include <vector>
 
 #include "engine.cuh"
@@ -570,20 +571,33 @@ __global__ void __launch_bounds__(256)
     const uint32_t sh_lo = s_shift[0];
     const bool sh_flat = s_shift[1] != 0;
     auto shift_of = [&](uint32_t i) { return sh_flat ? sh_lo : short_shift(S, ns, i); };
-    for (uint32_t l = threadIdx.x; l < valid; l += 256) {
-        const uint64_t item = keys[base + l];
-        sk[l + 1] = item >> vshift;
-        if (UNPACK) {
-            // segment-local positions (seg_at > 0): the segment index above
-            // the key gives the segment's first position
-            uint64_t pos = item & vmask;
-            if (SEG) {
-                const uint64_t sg = item >> seg_at;
-                pos += sg ? __ldg(seg_ends + sg - 1) : 0ull;
+    // the bulk of the tiles: full, neither the first nor the last, one shift
+    // for all records; they take loops without bounds, edge or shift checks
+    const bool fast = base > 0 && base + (uint32_t)kInitTile < n && sh_flat;
+    auto stage = [&](auto fast_c) {
+        constexpr bool FAST = decltype(fast_c)::value;
+#pragma unroll 4
+        for (int j = 0; j < kInitPer; j++) {
+            const uint32_t l = j * 256 + threadIdx.x;
+            if (!FAST && l >= valid) break;
+            const uint64_t item = keys[base + l];
+            sk[l + 1] = item >> vshift;
+            if (UNPACK) {
+                // segment-local positions (seg_at > 0): the segment index
+                // above the key gives the segment's first position
+                uint64_t pos = item & vmask;
+                if (SEG) {
+                    const uint64_t sg = item >> seg_at;
+                    pos += sg ? __ldg(seg_ends + sg - 1) : 0ull;
+                }
+                sa_out[base + l + (FAST ? sh_lo : shift_of(base + l))] = (uint32_t)pos;
             }
-            sa_out[base + l + shift_of(base + l)] = (uint32_t)pos;
         }
-    }
+    };
+    if (fast)
+        stage(std::true_type{});
+    else
+        stage(std::false_type{});
     if (threadIdx.x == 0) sk[0] = base > 0 ? keys[base - 1] >> vshift : 0ull;
     if (threadIdx.x == 32) sk[valid + 1] = base + valid < n ? keys[base + valid] >> vshift : 0ull;
     __syncthreads();
@@ -595,13 +609,21 @@ __global__ void __launch_bounds__(256)
     __shared__ int s_prev[kInitTile / 32];
     __shared__ uint32_t s_carry;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    auto heads = [&](auto fast_c) {
+        constexpr bool FAST = decltype(fast_c)::value;
 #pragma unroll 4
-    for (int j = 0; j < kInitPer; j++) {
-        const uint32_t l = j * 256 + threadIdx.x;
-        const bool hb = l < valid && (base + l == 0 || sk[l] != sk[l + 1]);
-        const uint32_t word = __ballot_sync(0xffffffffu, hb);
-        if (lane == 0) s_hb[j * 8 + warp] = word;
-    }
+        for (int j = 0; j < kInitPer; j++) {
+            const uint32_t l = j * 256 + threadIdx.x;
+            const bool hb = FAST ? sk[l] != sk[l + 1]
+                                 : l < valid && (base + l == 0 || sk[l] != sk[l + 1]);
+            const uint32_t word = __ballot_sync(0xffffffffu, hb);
+            if (lane == 0) s_hb[j * 8 + warp] = word;
+        }
+    };
+    if (fast)
+        heads(std::true_type{});
+    else
+        heads(std::false_type{});
     __syncthreads();
     if (warp == 0) {
         static_assert(kInitTile / 32 == 128, "four bitmap words per lane");
@@ -658,39 +680,46 @@ __global__ void __launch_bounds__(256)
     const bool lf_field = lf && !flag_len;
     // pass 1: heads, and the groups this thread ends (singletons, the bulk,
     // take the shortest path)
+    auto pass1 = [&](auto fast_c) {
+        constexpr bool FAST = decltype(fast_c)::value;
 #pragma unroll 4
-    for (int j = 0; j < kInitPer; j++) {
-        const uint32_t l = j * 256 + threadIdx.x;
-        if (l >= valid) break;
-        const uint32_t i = base + l;
-        const uint64_t key = sk[l + 1];
-        const bool head = (i == 0) || sk[l] != key;
-        const bool last = (i == n - 1) || sk[l + 2] != key;
-        // an insertion point only ever falls on a group head, so a group
-        // moves by one shift
-        const uint32_t sh = shift_of(i);
-        if (head && last) {
-            hd[i + sh] = i + sh;
-            continue;
-        }
-        const uint32_t g = head ? i : head_of(l);
-        bool complete = false;
-        uint64_t depth = (uint64_t)k;
-        if (lf_field || (last && !head)) state(key, complete, depth);
-        hd[i + sh] = ((complete && lf) ? i : g) + sh;
-        if (!complete && last && !head) {
-            const int li = list_of(i - g + 1, depth);
-            if (li == kLists) {
-                append_big(G, 0, g + sh, i - g + 1);
-            } else {
-                if (li < 4)
-                    cnt_lo += 1ull << (16 * li);
-                else
-                    cnt_hi += 1ull << (16 * (li - 4));
-                ends |= 1u << j;
+        for (int j = 0; j < kInitPer; j++) {
+            const uint32_t l = j * 256 + threadIdx.x;
+            if (!FAST && l >= valid) break;
+            const uint32_t i = base + l;
+            const uint64_t key = sk[l + 1];
+            const bool head = (!FAST && i == 0) || sk[l] != key;
+            const bool last = (!FAST && i == n - 1) || sk[l + 2] != key;
+            // an insertion point only ever falls on a group head, so a group
+            // moves by one shift
+            const uint32_t sh = FAST ? sh_lo : shift_of(i);
+            if (head && last) {
+                hd[i + sh] = i + sh;
+                continue;
+            }
+            const uint32_t g = head ? i : head_of(l);
+            bool complete = false;
+            uint64_t depth = (uint64_t)k;
+            if (lf_field || (last && !head)) state(key, complete, depth);
+            hd[i + sh] = ((complete && lf) ? i : g) + sh;
+            if (!complete && last && !head) {
+                const int li = list_of(i - g + 1, depth);
+                if (li == kLists) {
+                    append_big(G, 0, g + sh, i - g + 1);
+                } else {
+                    if (li < 4)
+                        cnt_lo += 1ull << (16 * li);
+                    else
+                        cnt_hi += 1ull << (16 * (li - 4));
+                    ends |= 1u << j;
+                }
             }
         }
-    }
+    };
+    if (fast)
+        pass1(std::true_type{});
+    else
+        pass1(std::false_type{});
     uint64_t off_lo, off_hi;
     const uint64_t tot_lo = block_excl_scan64(cnt_lo, &off_lo);
     const uint64_t tot_hi = block_excl_scan64(cnt_hi, &off_hi);
