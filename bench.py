@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the secondary forms (sample sort with splitter / learned "
                          "partition, batched texts, segmented filtered subset)")
+    ap.add_argument("--form", choices=FORMS,
+                    help="run this secondary form alone (no bench step) and print its "
+                         "JSON; for profiling one workload")
     return ap.parse_args()
 
 
@@ -267,18 +270,29 @@ def _timed(fn, reps):
     return statistics.median(ts)
 
 
-def run_forms(ctx, t_dev, n):
+FORMS = ("sample_sort", "batched", "segmented_filtered")
+
+
+def run_forms(ctx, t_dev, n, only=FORMS):
     """The secondary forms of the metric, each on its own workload:
     sample sort of the bench text with p = 4096 partitions found by splitter
     binary search vs the learned CDF model (65,536 training samples); 8,192
     independent texts sorted in one batched call vs a per-text loop; the
-    segmented, filtered subset build (n = 2^29, u64 index)."""
-    import torch
-
-    import capssa
-    from capssa import workloads
-
+    segmented, filtered subset build (n = 2^29, u64 index).  `only` picks
+    some of them (bench.py --form)."""
     out = {}
+    if "sample_sort" in only:
+        out["sample_sort_p4096"] = form_sample_sort(ctx, t_dev, n)
+    if "batched" in only:
+        out["batched_8192_texts"] = form_batched(ctx)
+    if "segmented_filtered" in only:
+        out["segmented_filtered_2p29"] = form_segmented_filtered(ctx)
+    return out
+
+
+def form_sample_sort(ctx, t_dev, n):
+    import capssa
+
     # ---- sample sort: splitter vs learned partition (plan = SA + partition),
     # bucketed before the sort; and the reference's sampling rule, whose
     # chunk order comes from a full sort first
@@ -305,7 +319,14 @@ def run_forms(ctx, t_dev, n):
                     "refine_ms": st["refine_ms"], "sort_passes": st["sort_passes"],
                     "sizes_sha": hash(sz.tobytes()) & 0xFFFFFFFF}
     ss["same_partition"] = ss["splitters"]["sizes_sha"] == ss["learned"]["sizes_sha"]
-    out["sample_sort_p4096"] = ss
+    return ss
+
+
+def form_batched(ctx):
+    import torch
+
+    from capssa import workloads
+
     # ---- batched: 8,192 texts, log-uniform 2^10..2^20, 10% repeats
     cat, offs = workloads.batched_texts()
     c_dev = torch.from_numpy(cat).to("cuda")
@@ -324,13 +345,22 @@ def run_forms(ctx, t_dev, n):
 
     loop()
     l_ms = _timed(loop, 1)
-    out["batched_8192_texts"] = {
+    res = {
         "value": total / (b_ms / 1e3) / 1e6, "unit": "Msuffixes/s", "ms": b_ms,
         "symbols": total,
         "per_text_loop": {"value": sample_syms / (l_ms / 1e3) / 1e6, "unit": "Msuffixes/s",
                           "sample": "every 16th text (%d texts, %d symbols)"
                                     % (len(idx), sample_syms)}}
     del c_dev, o_dev
+    return res
+
+
+def form_segmented_filtered(ctx):
+    import torch
+
+    import capssa
+    from capssa import workloads
+
     # ---- segmented, filtered subset: n = 2^29, lognormal segments, symbol < 4 kept
     text3, ends3, pos3 = workloads.segmented_filtered(1 << 29)
     t3 = torch.from_numpy(text3).to("cuda")
@@ -360,7 +390,7 @@ def run_forms(ctx, t_dev, n):
     ctx.try_build_ext_mem(text3, None, sink, lp3, keep=(0, 4))
     e_ms = (time.perf_counter() - t0) * 1e3
     assert sent[0] == len(pos3)
-    out["segmented_filtered_2p29"] = {"value": len(pos3) / (s_ms / 1e3) / 1e6,
+    res = {"value": len(pos3) / (s_ms / 1e3) / 1e6,
                                       "unit": "Msuffixes/s", "ms": s_ms,
                                       "positions": int(len(pos3)), "segments": int(len(ends3)),
                                       "reference_tie_order": {
@@ -379,7 +409,7 @@ def run_forms(ctx, t_dev, n):
                                                    "streamed emit)"}}
     del t3, p3, o3
     torch.cuda.synchronize()
-    return out
+    return res
 
 
 def run_ours(args):
@@ -504,10 +534,29 @@ def run_ours(args):
     return 0
 
 
+def run_form(args):
+    """One secondary form alone on cuda:0 (no bench step, no contract line)."""
+    import torch
+
+    import capssa
+
+    torch.cuda.set_device(0)
+    ctx = capssa.Context(0)
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    t_dev, n = None, 0
+    if args.form == "sample_sort":
+        n = 1 << args.log2n
+        t_dev = torch.from_numpy(workload(args.log2n)).to("cuda")
+    print(json.dumps({"form": args.form, **run_forms(ctx, t_dev, n, only=(args.form,))}))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.form:
+        return run_form(args)
     return run_ours(args)
 
 

@@ -123,7 +123,7 @@ enum Slot : int {
     WS_KEYS_A, WS_KEYS_B, WS_VALS_A, WS_VALS_B,
     WS_RANK, WS_KEY2, WS_GROUPS_A, WS_GROUPS_B, WS_COUNTERS,
     WS_RADIX_STATUS, WS_RADIX_HIST, WS_SCAN, WS_CODES, WS_MISC, WS_MISC2, WS_MISC3,
-    WS_PACKED, WS_CDF, WS_PART, WS_SAMPLE, WS_KEEP, WS_NSLOTS
+    WS_PACKED, WS_CDF, WS_PART, WS_SAMPLE, WS_KEEP, WS_RUNS, WS_NSLOTS
 };
 
 struct Ctx {

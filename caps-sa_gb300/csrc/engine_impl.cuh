@@ -31,7 +31,8 @@ constexpr int kKeyPer = 8;          // positions per thread in the key kernel
 constexpr int kKeyTile = kKeyThreads * kKeyPer;
 
 struct BigGroup {
-    uint32_t start, len, toff, pad;
+    uint32_t start, len, toff;
+    uint32_t depth;  // symbols its members are known to agree on (saturated)
 };
 
 // Work lists of one refinement round, by group size and depth.
@@ -355,19 +356,24 @@ __device__ __forceinline__ int list_of(uint32_t len, uint64_t depth) {
     return kLists;
 }
 
+// A pair entry that carries its two positions: (start, position at start,
+// depth | kPairPos, position at start + 1), so the pair kernel reads no SA
+// entries (group init writes these; pair depths stay below kDirectMaxH).
+constexpr uint32_t kPairPos = 0x80000000u;
+
 __device__ __forceinline__ uint4 group_entry(uint32_t start, uint32_t len, uint64_t depth) {
     return make_uint4(start, len, depth > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)depth, 0u);
 }
 
 __device__ __forceinline__ void append_big(const GroupLists &G, int nxt, uint32_t start,
-                                           uint32_t len) {
+                                           uint32_t len, uint64_t depth) {
     unsigned long long old = atomicAdd(&G.ctr->big_packed[nxt], kBigOrdUnit | len);
     uint32_t ord = (uint32_t)(old >> 40);
     BigGroup g;
     g.start = start;
     g.len = len;
     g.toff = (uint32_t)(old & kBigTotMask);
-    g.pad = 0;
+    g.depth = depth > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)depth;
     big_ptr(G, nxt)[ord] = g;
 }
 
@@ -391,7 +397,7 @@ __device__ __forceinline__ void append_group(const GroupLists &G, int nxt, uint3
                                              uint32_t len, uint64_t depth) {
     int l = list_of(len, depth);
     if (l == kLists) {
-        append_big(G, nxt, start, len);
+        append_big(G, nxt, start, len, depth);
         return;
     }
     uint32_t idx = warp_append(&G.ctr->n[l][nxt]);
@@ -414,7 +420,7 @@ __device__ __forceinline__ void block_append(const GroupLists &G, int nxt, bool 
         s_base[threadIdx.x] = atomicAdd(&G.ctr->n[threadIdx.x][nxt], s_cnt[threadIdx.x]);
     __syncthreads();
     if (l >= 0 && l < kLists) list_ptr(G, l, nxt)[s_base[l] + local] = group_entry(start, len, depth);
-    if (l == kLists) append_big(G, nxt, start, len);
+    if (l == kLists) append_big(G, nxt, start, len, depth);
 }
 
 // Exclusive block-wide prefix of one u32 per thread; returns the block total.
@@ -705,7 +711,7 @@ __global__ void __launch_bounds__(256)
             if (!complete && last && !head) {
                 const int li = list_of(i - g + 1, depth);
                 if (li == kLists) {
-                    append_big(G, 0, g + sh, i - g + 1);
+                    append_big(G, 0, g + sh, i - g + 1, depth);
                 } else {
                     if (li < 4)
                         cnt_lo += 1ull << (16 * li);
@@ -751,7 +757,20 @@ __global__ void __launch_bounds__(256)
                 off += 1ull << sh;
             }
         }
-        list_ptr(G, li, 0)[slot] = group_entry(g + shift_of(i), i - g + 1, depth);
+        uint4 entry = group_entry(g + shift_of(i), i - g + 1, depth);
+        if (UNPACK && li == L_PAIR) {  // the positions ride along (see kPairPos)
+            auto pos_of = [&](uint32_t r) -> uint32_t {
+                const uint64_t item = keys[r];
+                uint64_t pos = item & vmask;
+                if (SEG) {
+                    const uint64_t sg = item >> seg_at;
+                    pos += sg ? __ldg(seg_ends + sg - 1) : 0ull;
+                }
+                return (uint32_t)pos;
+            };
+            entry = make_uint4(entry.x, pos_of(g), entry.z | kPairPos, pos_of(i));
+        }
+        list_ptr(G, li, 0)[slot] = entry;
     }
 }
 
@@ -775,9 +794,10 @@ __global__ void gather_small_kernel(const uint4 *__restrict__ groups, uint32_t c
     for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < count;
          gi += gridDim.x * blockDim.x) {
         uint4 g = groups[gi];
+        const uint64_t d = g.z > h ? (uint64_t)g.z : h;  // the group's own depth if deeper
         for (uint32_t t = 0; t < g.y; t++) {
             uint32_t i = g.x + t;
-            key2[i] = doubling_key(L, rank, sa[i], h, lf, empty_lf);
+            key2[i] = doubling_key(L, rank, sa[i], d, lf, empty_lf);
         }
     }
 }
@@ -786,10 +806,46 @@ __global__ void gather_small_kernel(const uint4 *__restrict__ groups, uint32_t c
 // (a single group can hold millions: runs of one symbol): member t belongs
 // to the group whose flattened offset range holds it (groups' offsets grow
 // with their ordinals).
+// Runs of one symbol (ShorterFirst).  A tied group whose members all start
+// with c^h (c repeated through the depth h) is a run group: its members are
+// ordered at once by how their runs end instead of by doubling through the
+// run (a run of length L would take log2(L / h) rounds, each re-sorting the
+// whole group).  Member p with run length rr = min(run of c from p, lim):
+//   * ends at rr (the suffix is c^rr): below every continuation of c^rr;
+//   * continues with x != c at rr: c^rr x.. < c^rr' .. for rr < rr' when
+//     x < c, and > when x > c;
+// so the order is class A (x < c, or ended), ascending rr; then the members
+// whose run reaches the key's cap; then class B (x > c), descending rr; and
+// inside equal (class, rr) the rank of the suffix p + rr (0: ended).  Equal
+// keys then agree on rr + h symbols (ranks are exact to the round depth h),
+// the depth their subgroup is queued with; a group deeper than h is sorted
+// by the rank at its own depth d, and its subgroups agree on d + h.
+// runs_s: the inclusive max-scan of "last index of a run" over the reversed
+// text, from which the run from p ends at n - 1 - runs_s[n - 1 - p].
+struct RunKeys {
+    const uint32_t *runs_s;  // null: no run keys this round
+    Packed P;
+    uint64_t n;
+    int rbits;               // bits of the run-length field (cap 2^rbits - 1)
+};
+
+__device__ __forceinline__ uint32_t code_at(const Packed &P, uint64_t q) {
+    const uint64_t bit = q * (uint64_t)P.b;
+    const uint32_t sh = (uint32_t)(bit & 63);
+    const uint64_t w0 = __ldg(P.w + (bit >> 6));
+    const uint64_t w1 = __ldg(P.w + (bit >> 6) + 1);
+    const uint64_t v = sh ? (w0 << sh) | (w1 >> (64 - sh)) : w0;
+    return (uint32_t)(v >> (64 - P.b));
+}
+
+__device__ __forceinline__ uint64_t run_from(const RunKeys &R, uint64_t p) {
+    return R.n - 1 - (uint64_t)__ldg(R.runs_s + (R.n - 1 - p)) - p + 1;
+}
+
 __global__ void gather_big_kernel(const BigGroup *__restrict__ groups, uint32_t nb,
                                   uint32_t total, const uint32_t *__restrict__ sa,
                                   const uint32_t *__restrict__ rank, DevLimits L, uint64_t h,
-                                  int lf, uint64_t empty_lf, int k2bits,
+                                  int lf, uint64_t empty_lf, int k2bits, RunKeys R,
                                   uint64_t *__restrict__ tkeys, uint32_t *__restrict__ tvals) {
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += gridDim.x * blockDim.x) {
@@ -803,9 +859,50 @@ __global__ void gather_big_kernel(const BigGroup *__restrict__ groups, uint32_t 
         }
         const BigGroup g = groups[lo];
         const uint32_t p = sa[g.start + (t - g.toff)];
-        const uint64_t k2 = doubling_key(L, rank, p, h, lf, empty_lf);
-        tkeys[t] = ((uint64_t)lo << k2bits) | k2;
+        // the group's own depth when it is known to be deeper than the round's
+        const uint64_t d = g.depth > h ? (uint64_t)g.depth : h;
+        uint64_t key;
+        // a run group (see RunKeys); its members agree on d symbols only when
+        // the group's own depth reaches the round's
+        if (R.runs_s && g.depth >= h && run_from(R, sa[g.start]) >= d) {
+            const uint64_t cap = (1ull << R.rbits) - 1;
+            const uint64_t lim = dev_lim_at(L, p);
+            const uint64_t rl = run_from(R, p);
+            const uint64_t rr = rl < lim ? rl : lim;
+            uint64_t cls, rq, k2;
+            if (rr >= cap) {  // past the cap: between the two classes, by the
+                cls = 0;      // doubling key at offset cap (lim >= rr >= cap)
+                rq = cap;
+                k2 = lim > cap ? (uint64_t)__ldcg(rank + p + cap) + 1 : 0ull;
+            } else if (rr == lim) {  // ends inside the run
+                cls = 0;
+                rq = rr;
+                k2 = 0;
+            } else {
+                const uint32_t c = code_at(R.P, p), x = code_at(R.P, p + rr);
+                cls = x < c ? 0 : 1;
+                rq = x < c ? rr : cap - 1 - rr;
+                k2 = (uint64_t)__ldcg(rank + p + rr) + 1;
+            }
+            key = ((((((uint64_t)lo << 1) | cls) << R.rbits) | rq) << k2bits) | k2;
+        } else {
+            const uint64_t k2 = doubling_key(L, rank, p, d, lf, empty_lf);
+            key = ((uint64_t)lo << (R.runs_s ? k2bits + 1 + R.rbits : k2bits)) | k2;
+        }
+        tkeys[t] = key;
         tvals[t] = p;
+    }
+}
+
+// runs_s input: rev[r] = r where text position n - 1 - r ends a run of one
+// symbol (the next symbol differs, or the text ends), else 0.
+__global__ void run_ends_kernel(const void *__restrict__ text, int sym_bytes, uint64_t n,
+                                uint32_t *__restrict__ rev) {
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n;
+         r += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t q = n - 1 - r;
+        const bool end = q == n - 1 || sym_at(text, sym_bytes, q) != sym_at(text, sym_bytes, q + 1);
+        rev[r] = end ? (uint32_t)r : 0u;
     }
 }
 
@@ -814,10 +911,11 @@ __global__ void gather_big_kernel(const BigGroup *__restrict__ groups, uint32_t 
 __global__ void sort_small_kernel(const uint4 *__restrict__ groups, uint32_t count,
                                   uint32_t *__restrict__ sa, const uint64_t *__restrict__ key2,
                                   uint32_t *__restrict__ hd, uint32_t *__restrict__ rank, int lf,
-                                  uint64_t empty, uint64_t next_depth, GroupLists G, int nxt) {
+                                  uint64_t empty, uint64_t h, GroupLists G, int nxt) {
     for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < count;
          gi += gridDim.x * blockDim.x) {
         uint4 g = groups[gi];
+        const uint64_t next_depth = (g.z > h ? (uint64_t)g.z : h) + h;
         uint64_t kk[kSmallMax];
         uint32_t pp[kSmallMax];
         for (uint32_t t = 0; t < g.y; t++) {
@@ -1044,11 +1142,13 @@ __global__ void __launch_bounds__(256)
     bool again = false;
     uint4 g = make_uint4(0, 0, 0, 0);
     uint64_t cap = 0;
+    uint64_t o = 0;
     if (gi < count) {
         g = groups[gi];
-        const uint64_t o = g.z;
+        const bool carried = (g.z & kPairPos) != 0;  // positions in the entry
+        o = g.z & ~kPairPos;
         cap = o > kDirectCap ? o : kDirectCap;
-        uint32_t p0 = sa[g.x], p1 = sa[g.x + 1];
+        uint32_t p0 = carried ? g.y : sa[g.x], p1 = carried ? g.w : sa[g.x + 1];
         uint64_t l0 = dev_lim_at(L, p0), l1 = dev_lim_at(L, p1);
         int r = direct_cmp<kPairBurst>(P, p0, l0, p1, l1, o, cap, lf);
         if (r == 1 || ((r == 0 || r == 2) && p0 > p1)) {
@@ -1068,7 +1168,7 @@ __global__ void __launch_bounds__(256)
         }
         again = r == 2;
     }
-    block_append(G, nxt, again, g.x, 2, (uint64_t)g.z + cap);
+    block_append(G, nxt, again, g.x, 2, o + cap);
 }
 
 // Four consecutive windows of the packed text from symbol p (five word
@@ -1503,15 +1603,15 @@ __global__ void __launch_bounds__(kMedThreads)
 __global__ void split_big_kernel(const uint64_t *__restrict__ tkeys,
                                  const uint32_t *__restrict__ tvals, uint32_t total,
                                  const BigGroup *__restrict__ groups, uint32_t n_groups,
-                                 int k2bits,
+                                 int k2bits, int ord_shift, RunKeys R,
                                  uint32_t *__restrict__ sa, uint32_t *__restrict__ hd,
                                  uint32_t *__restrict__ rank, int lf,
-                                 uint64_t empty, uint64_t next_depth, GroupLists G, int nxt) {
+                                 uint64_t empty, uint64_t h, GroupLists G, int nxt) {
     const uint64_t k2mask = (k2bits >= 64) ? ~0ull : ((1ull << k2bits) - 1);
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += gridDim.x * blockDim.x) {
         uint64_t key = tkeys[t];
-        uint32_t ord = (uint32_t)(key >> k2bits);
+        uint32_t ord = (uint32_t)(key >> ord_shift);
         if (ord >= n_groups) continue;  // unreachable unless a sort step failed (flagged)
         BigGroup g = groups[ord];
         uint32_t local = t - g.toff;
@@ -1525,8 +1625,18 @@ __global__ void split_big_kernel(const uint64_t *__restrict__ tkeys,
         hd[g.start + local] = r;
         rank[p] = r;
         bool last = (t == g.toff + g.len - 1) || tkeys[t + 1] != key;
-        if (!ended && last && t > h0)
+        if (!ended && last && t > h0) {
+            // the depth the subgroup's members now agree on (see RunKeys)
+            const uint64_t d = g.depth > h ? (uint64_t)g.depth : h;
+            uint64_t next_depth = d + h;
+            if (R.runs_s && g.depth >= h && run_from(R, tvals[g.toff]) >= d) {
+                const uint64_t cap = (1ull << R.rbits) - 1;
+                const uint64_t rq = (key >> k2bits) & cap;
+                const bool cls_b = (key >> (k2bits + R.rbits)) & 1ull;
+                next_depth = (cls_b ? cap - 1 - rq : rq) + h;
+            }
             append_group(G, nxt, g.start + (h0 - g.toff), t - h0 + 1, next_depth);
+        }
     }
 }
 
@@ -2769,6 +2879,7 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
     const uint64_t empty_lf = (1ull << k2bits) - 1;  // above every rank
     const uint64_t empty = lf ? empty_lf : 0ull;
     bool ranks_ready = false;
+    uint32_t *runs_s = nullptr;  // run ends, for the run keys of deep rounds
     int cur = 0;
     Counters *hc = (Counters *)c.h_scratch;
     for (;;) {
@@ -2852,26 +2963,44 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
                 G.list[L_DEEP][cur], cnt[L_DEEP], sa, rank, a.lim, h, lf, empty_lf, key2);
             CAPSSA_LAUNCHED(c);
             sort_small_kernel<<<grid_for(cnt[L_DEEP], 128), 128, 0, c.stream>>>(
-                G.list[L_DEEP][cur], cnt[L_DEEP], sa, key2, hd, rank, lf, empty, 2 * h, G, nxt);
+                G.list[L_DEEP][cur], cnt[L_DEEP], sa, key2, hd, rank, lf, empty, h, G, nxt);
             CAPSSA_LAUNCHED(c);
             kt.mark(c.stream, "deep");
         }
         const int ord_bits = nb > 1 ? bits_for(nb - 1) : 1;
         if (nb) {
+            // run keys for ShorterFirst whole texts, when a run-length field
+            // of at least 12 bits fits beside the ordinal and the rank
+            RunKeys R{nullptr, P, n, 0};
+            const int rbits = std::min(24, 64 - ord_bits - 1 - k2bits);
+            if (!lf && !sp && rbits >= 12 && h >= 2 * (uint64_t)geo.k) {
+                if (!runs_s) {  // built once, the first deep round that can use it
+                    runs_s = (uint32_t *)ws_get(c, WS_RUNS, (size_t)n * 4 + 64);
+                    if (!runs_s) return set_err(c, CAPSSA_ENOMEM, "run lengths");
+                    run_ends_kernel<<<grid_for(n, 256), 256, 0, c.stream>>>(a.text, a.sym_bytes,
+                                                                            n, runs_s);
+                    CAPSSA_LAUNCHED(c);
+                    s = scan_u32(c, runs_s, runs_s, n, /*max_op=*/true, /*inclusive=*/true);
+                    if (s != CAPSSA_OK) return s;
+                }
+                R.runs_s = runs_s;
+                R.rbits = rbits;
+            }
+            const int ord_shift = R.runs_s ? k2bits + 1 + rbits : k2bits;
             gather_big_kernel<<<grid_for(big_total, 256), 256, 0, c.stream>>>(
                 G.big[cur], nb, big_total, sa, rank, a.lim, h, lf,
-                                                        empty_lf, k2bits, keys_a, spare_vals);
+                                                        empty_lf, k2bits, R, keys_a, spare_vals);
             CAPSSA_LAUNCHED(c);
             bool tb = false;
             uint32_t *tv_b = (uint32_t *)key2;  // free once sort_small has run
             s = radix::sort_pairs(c, keys_a, spare_vals, keys_b, tv_b, big_total, 0,
-                                  k2bits + ord_bits, false, 0, &tb);
+                                  ord_shift + ord_bits, false, 0, &tb);
             if (s != CAPSSA_OK) return s;
             const uint64_t *tk = tb ? keys_b : keys_a;
             const uint32_t *tv = tb ? tv_b : spare_vals;
             split_big_kernel<<<grid_for(big_total, 256), 256, 0, c.stream>>>(
-                tk, tv, big_total, G.big[cur], nb, k2bits, sa, hd, rank, lf, empty, 2 * h, G,
-                nxt);
+                tk, tv, big_total, G.big[cur], nb, k2bits, ord_shift, R, sa, hd, rank, lf, empty,
+                h, G, nxt);
             CAPSSA_LAUNCHED(c);
             kt.mark(c.stream, "big");
         }

@@ -19,92 +19,109 @@ __device__ __forceinline__ uint32_t op(uint32_t a, uint32_t b) {
     return MAX ? (a > b ? a : b) : a + b;
 }
 
+// Decoupled look-back by one whole warp: publishes the tile's aggregate,
+// then reads 32 predecessors' status words per round trip, combines those
+// up to the nearest inclusive prefix (waiting while any of them is not yet
+// published, bounded), and publishes this tile's inclusive prefix.  Returns
+// the tile's exclusive prefix on every lane.  (A single thread walking the
+// predecessors one at a time waited one L2 round trip per predecessor.)
+template <bool MAX>
+__device__ __forceinline__ uint32_t warp_lookback(unsigned long long *status, uint64_t tile,
+                                                  uint32_t tile_total, int *err) {
+    const int lane = threadIdx.x & 31;
+    if (lane == 0)
+        *(volatile unsigned long long *)(status + tile) = (tile == 0 ? kP : kA) | tile_total;
+    if (tile == 0) return 0u;
+    uint32_t acc = 0u;
+    int64_t top = (int64_t)tile - 1;  // lane l reads tile top - l
+    uint32_t spins = 0;
+    const unsigned long long before_first = kP;  // before tile 0: inclusive, 0
+    for (;;) {
+        const int64_t t = top - lane;
+        unsigned long long sv = before_first;
+        if (t >= 0) sv = *(volatile unsigned long long *)(status + t);
+        const unsigned long long fl = sv & ~kMask;
+        const unsigned pm = __ballot_sync(0xffffffffu, fl == kP);
+        const unsigned bad = __ballot_sync(0xffffffffu, fl == 0);
+        const int first_p = pm ? __ffs((int)pm) - 1 : 31;  // lanes 0..first_p count
+        const unsigned need = first_p == 31 ? 0xffffffffu : (2u << first_p) - 1u;
+        if (bad & need) {
+            if (++spins > kSpinLimit) {
+                if (lane == 0) atomicCAS(err, DEV_OK, DEV_LOOKBACK_TIMEOUT);
+                break;
+            }
+            __nanosleep(32);
+            continue;
+        }
+        uint32_t v = lane <= first_p ? (uint32_t)(sv & kMask) : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = op<MAX>(v, __shfl_xor_sync(0xffffffffu, v, o));
+        acc = op<MAX>(acc, v);
+        if (pm) break;
+        top -= 32;
+    }
+    if (lane == 0) *(volatile unsigned long long *)(status + tile) = kP | op<MAX>(acc, tile_total);
+    return acc;
+}
+
 template <bool MAX, bool INCLUSIVE>
 __global__ void __launch_bounds__(kScanThreads)
     scan_kernel(const uint32_t *__restrict__ in, uint32_t *__restrict__ out, uint64_t n,
                 unsigned long long *__restrict__ status, uint32_t *__restrict__ counter,
                 int *__restrict__ err) {
+    constexpr int kWarps = kScanThreads / 32;
+    static_assert(kScanItems * kWarps == 64, "two (step, warp) totals per lane of warp 0");
     __shared__ uint32_t s_tile;
-    __shared__ uint32_t s_warp[kScanThreads / 32];
+    // each (step, warp)'s total; then the exclusive prefix in entry order
+    __shared__ uint32_t s_tot[kScanItems * kWarps];
     __shared__ uint32_t s_prefix;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) s_tile = atomicAdd(counter, 1u);
     __syncthreads();
     const uint64_t tile = s_tile;
-    const uint64_t base = tile * kScanTile + (uint64_t)tid * kScanItems;
-    uint32_t v[kScanItems];
-    uint32_t agg = 0u;
+    const uint64_t base = tile * kScanTile;
+    // step j covers entries base + j * 256 .. + 255, one per thread: a warp
+    // reads and writes 32 consecutive words; x[j] = its inclusive warp prefix
+    uint32_t v[kScanItems], x[kScanItems];
 #pragma unroll
     for (int j = 0; j < kScanItems; j++) {
-        uint64_t i = base + j;
-        v[j] = i < n ? in[i] : 0u;
-        agg = op<MAX>(agg, v[j]);
-    }
-    // block inclusive scan of per-thread aggregates
-    uint32_t x = agg;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x = op<MAX>(x, y);
-    }
-    if (lane == 31) s_warp[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t w = lane < kScanThreads / 32 ? s_warp[lane] : 0u;
+        const uint64_t i = base + (uint64_t)j * kScanThreads + tid;
+        v[j] = i < n ? __ldg(in + i) : 0u;
+        uint32_t y = v[j];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w = op<MAX>(w, y);
+            const uint32_t z = __shfl_up_sync(0xffffffffu, y, o);
+            if (lane >= o) y = op<MAX>(y, z);
         }
-        if (lane < kScanThreads / 32) s_warp[lane] = w;
+        x[j] = y;
+        if (lane == 31) s_tot[j * kWarps + warp] = y;
     }
     __syncthreads();
-    // exclusive prefix of this thread's items inside the tile
-    uint32_t within_excl;
-    {
-        uint32_t prev_in_warp = __shfl_up_sync(0xffffffffu, x, 1);
-        if (lane == 0) prev_in_warp = 0;
-        within_excl = op<MAX>(warp > 0 ? s_warp[warp - 1] : 0u, prev_in_warp);
-    }
-    const uint32_t tile_total = s_warp[kScanThreads / 32 - 1];
-    if (tid == 0) {
-        uint64_t excl = 0;
-        unsigned long long *st = status + tile;
-        if (tile == 0) {
-            *(volatile unsigned long long *)st = kP | tile_total;
-        } else {
-            *(volatile unsigned long long *)st = kA | tile_total;
-            int64_t t = (int64_t)tile - 1;
-            uint32_t spins = 0;
-            uint32_t acc = 0;
-            while (t >= 0) {
-                unsigned long long s = *(volatile unsigned long long *)(status + t);
-                unsigned long long f = s & ~kMask;
-                if (f == 0) {
-                    if (++spins > kSpinLimit) {
-                        atomicCAS(err, DEV_OK, DEV_LOOKBACK_TIMEOUT);
-                        break;
-                    }
-                    __nanosleep(64);
-                    continue;
-                }
-                acc = op<MAX>(acc, (uint32_t)(s & kMask));
-                if (f == kP) break;
-                t--;
-            }
-            excl = acc;
-            *(volatile unsigned long long *)st = kP | op<MAX>((uint32_t)excl, tile_total);
+    if (warp == 0) {
+        const uint32_t c0 = s_tot[2 * lane], c1 = s_tot[2 * lane + 1];
+        uint32_t w = op<MAX>(c0, c1);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t z = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w = op<MAX>(w, z);
         }
-        s_prefix = (uint32_t)excl;
+        const uint32_t tile_total = __shfl_sync(0xffffffffu, w, 31);
+        uint32_t ex = __shfl_up_sync(0xffffffffu, w, 1);  // before this lane's pair
+        if (lane == 0) ex = 0u;
+        s_tot[2 * lane] = ex;
+        s_tot[2 * lane + 1] = op<MAX>(ex, c0);
+        const uint32_t acc = warp_lookback<MAX>(status, tile, tile_total, err);
+        if (lane == 0) s_prefix = acc;
     }
     __syncthreads();
-    uint32_t run = op<MAX>(s_prefix, within_excl);
 #pragma unroll
     for (int j = 0; j < kScanItems; j++) {
-        uint64_t i = base + j;
-        uint32_t nx = op<MAX>(run, v[j]);
-        if (i < n) out[i] = INCLUSIVE ? nx : run;
-        run = nx;
+        const uint64_t i = base + (uint64_t)j * kScanThreads + tid;
+        const uint32_t pre = op<MAX>(s_prefix, s_tot[j * kWarps + warp]);
+        uint32_t incl = op<MAX>(pre, x[j]);
+        uint32_t excl = __shfl_up_sync(0xffffffffu, incl, 1);
+        if (lane == 0) excl = pre;
+        if (i < n) out[i] = INCLUSIVE ? incl : excl;
     }
 }
 
@@ -117,77 +134,51 @@ __global__ void __launch_bounds__(kScanThreads)
     select_kernel(const uint32_t *__restrict__ sa, uint64_t n, const uint32_t *__restrict__ bits,
                   uint64_t off, OT *__restrict__ out, unsigned long long *__restrict__ status,
                   uint32_t *__restrict__ counter, int *__restrict__ err) {
+    constexpr int kWarps = kScanThreads / 32;
+    static_assert(kScanItems * kWarps == 64, "two (step, warp) counts per lane of warp 0");
     __shared__ uint32_t s_tile;
-    __shared__ uint32_t s_warp[kScanThreads / 32];
+    // kept entries per (step, warp); then their exclusive prefix in entry order
+    __shared__ uint32_t s_cnt[kScanItems * kWarps];
     __shared__ uint32_t s_prefix;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) s_tile = atomicAdd(counter, 1u);
     __syncthreads();
     const uint64_t tile = s_tile;
-    const uint64_t base = tile * kScanTile + (uint64_t)tid * kScanItems;
-    uint32_t v[kScanItems];
-    uint32_t keep = 0u, agg = 0u;  // keep: bit j set when item j is selected
+    const uint64_t base = tile * kScanTile;
+    // step j covers entries base + j * 256 .. + 255, one per thread: loads and
+    // stores of a warp are contiguous
+    uint32_t v[kScanItems], ball[kScanItems];
 #pragma unroll
     for (int j = 0; j < kScanItems; j++) {
-        const uint64_t i = base + j;
-        v[j] = i < n ? sa[i] : 0u;
-        const uint32_t f = i < n ? (__ldg(bits + (v[j] >> 5)) >> (v[j] & 31)) & 1u : 0u;
-        keep |= f << j;
-        agg += f;
+        const uint64_t i = base + (uint64_t)j * kScanThreads + tid;
+        v[j] = i < n ? __ldg(sa + i) : 0u;
+        const bool f = i < n && ((__ldg(bits + (v[j] >> 5)) >> (v[j] & 31)) & 1u);
+        ball[j] = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) s_cnt[j * kWarps + warp] = __popc(ball[j]);
     }
-    uint32_t x = agg;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) s_warp[warp] = x;
     __syncthreads();
     if (warp == 0) {
-        uint32_t w = lane < kScanThreads / 32 ? s_warp[lane] : 0u;
+        const uint32_t c0 = s_cnt[2 * lane], c1 = s_cnt[2 * lane + 1];
+        uint32_t x = c0 + c1;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += y;
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
         }
-        if (lane < kScanThreads / 32) s_warp[lane] = w;
+        const uint32_t tile_total = __shfl_sync(0xffffffffu, x, 31);
+        const uint32_t ex = x - c0 - c1;
+        s_cnt[2 * lane] = ex;
+        s_cnt[2 * lane + 1] = ex + c0;
+        const uint32_t acc = warp_lookback<false>(status, tile, tile_total, err);
+        if (lane == 0) s_prefix = acc;
     }
     __syncthreads();
-    const uint32_t within_excl = (warp > 0 ? s_warp[warp - 1] : 0u) + x - agg;
-    const uint32_t tile_total = s_warp[kScanThreads / 32 - 1];
-    if (tid == 0) {
-        uint64_t excl = 0;
-        unsigned long long *st = status + tile;
-        if (tile == 0) {
-            *(volatile unsigned long long *)st = kP | tile_total;
-        } else {
-            *(volatile unsigned long long *)st = kA | tile_total;
-            int64_t t = (int64_t)tile - 1;
-            uint32_t spins = 0;
-            while (t >= 0) {
-                unsigned long long s = *(volatile unsigned long long *)(status + t);
-                unsigned long long f = s & ~kMask;
-                if (f == 0) {
-                    if (++spins > kSpinLimit) {
-                        atomicCAS(err, DEV_OK, DEV_LOOKBACK_TIMEOUT);
-                        break;
-                    }
-                    __nanosleep(64);
-                    continue;
-                }
-                excl += s & kMask;
-                if (f == kP) break;
-                t--;
-            }
-            *(volatile unsigned long long *)st = kP | (excl + tile_total);
-        }
-        s_prefix = (uint32_t)excl;
-    }
-    __syncthreads();
-    uint64_t o = off + (uint64_t)s_prefix + within_excl;
+    const uint64_t o0 = off + (uint64_t)s_prefix;
+    const uint32_t lt = (1u << lane) - 1u;
 #pragma unroll
     for (int j = 0; j < kScanItems; j++)
-        if ((keep >> j) & 1u) out[o++] = (OT)v[j];
+        if ((ball[j] >> lane) & 1u)
+            out[o0 + s_cnt[j * kWarps + warp] + __popc(ball[j] & lt)] = (OT)v[j];
 }
 
 

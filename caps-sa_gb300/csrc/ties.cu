@@ -190,7 +190,7 @@ __global__ void split_info_kernel(Classes K, uint32_t *__restrict__ slo, uint32_
 // split nodes on its input's path (pred = slot + 1, the largest wins).
 __global__ void __launch_bounds__(256)
     walk_kernel(Classes K, const uint32_t *__restrict__ idxf, uint32_t *__restrict__ pred,
-                uint32_t *__restrict__ cstate) {
+                uint32_t *__restrict__ cstate, uint32_t *__restrict__ n_budget) {
     __shared__ uint32_t s_found;
     for (uint32_t c = blockIdx.x; c < K.C; c += gridDim.x) {
         const uint32_t s = K.cstart[c], mb = K.moff[c], k = K.size(c);
@@ -234,7 +234,10 @@ __global__ void __launch_bounds__(256)
             __syncthreads();
             if (done) break;
         }
-        if (threadIdx.x == 0) cstate[c] = state;
+        if (threadIdx.x == 0) {
+            cstate[c] = state;
+            if (state == kWalkBudget) atomicAdd(n_budget, 1u);
+        }
         __syncthreads();
     }
 }
@@ -505,10 +508,12 @@ capssa_status reference_tie_order(Ctx &c, const TieArgs &t) {
         CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
         ascending = h[0] == 0;
     }
+    // the slot of every input index (slot_of) is needed only if a walk runs
+    // out of budget; for a whole text or ascending positions it is scattered
+    // from idxf then, the other positions need it from the sorts below
+    bool have_slots = false;
     if (!t.positions) {  // a whole text: the input index is the position
         idxf = pos32;
-        s = scatter_u32(c, pos32, nullptr, m, slot_of, m, ka, (uint32_t *)kb);
-        if (s != CAPSSA_OK) return s;
     } else if (ascending) {
         const uint64_t nw = (t.lim.n + 1) / 32 + 1;  // position n included
         uint32_t *bits = (uint32_t *)ws_get(c, WS_KEEP, nw * 4 + 64);
@@ -528,8 +533,6 @@ capssa_status reference_tie_order(Ctx &c, const TieArgs &t) {
         if (s != CAPSSA_OK) return s;
         pos_rank_kernel<<<g, 256, 0, c.stream>>>(pos32, mm, bits, wc, idxf);
         CAPSSA_LAUNCHED(c);
-        s = scatter_u32(c, idxf, nullptr, m, slot_of, m, ka, (uint32_t *)kb);
-        if (s != CAPSSA_OK) return s;
     } else {
         // inputs and slots, each sorted by position (stably): the j-th of
         // both name the same suffix (repeated positions pair up in order)
@@ -565,6 +568,7 @@ capssa_status reference_tie_order(Ctx &c, const TieArgs &t) {
         if (s != CAPSSA_OK) return s;
         s = scatter_u32(c, inp, sl, m, slot_of, m, ka, (uint32_t *)kb);
         if (s != CAPSSA_OK) return s;
+        have_slots = true;
         // pos32 still holds the slots' positions; `inp` and `sl` are dead
     }
     kt.mark(c.stream, "maps");
@@ -593,13 +597,25 @@ capssa_status reference_tie_order(Ctx &c, const TieArgs &t) {
     CAPSSA_LAUNCHED(c);
     kt.mark(c.stream, "members");
     // 4. predecessors: walk, then scan what the walk left
+    uint32_t *n_budget = (uint32_t *)(c.d_flags + 2);  // a scratch device word
+    CAPSSA_CUDA(c, cudaMemsetAsync(n_budget, 0, 4, c.stream));
     walk_kernel<<<std::min<uint32_t>(C, (uint32_t)c.sm_count * 16), 256, 0, c.stream>>>(
-        K, idxf, pred, cstate);
+        K, idxf, pred, cstate, n_budget);
     CAPSSA_LAUNCHED(c);
     kt.mark(c.stream, "walk");
-    brute_kernel<<<grid_for((uint64_t)S * 32, 256, (unsigned)c.sm_count * 32), 256, 0,
-                   c.stream>>>(K, S, slo, shi, scls, cstate, slot_of, pred);
-    CAPSSA_LAUNCHED(c);
+    CAPSSA_CUDA(c, cudaMemcpyAsync(h, n_budget, 4, cudaMemcpyDeviceToHost, c.stream));
+    CAPSSA_CUDA(c, cudaStreamSynchronize(c.stream));
+    if (h[0]) {
+        if (!have_slots) {  // pairs and counts in the sort buffers the members left free
+            uint64_t *kfree = mkey == ka ? kb : ka;
+            uint32_t *vfree = melem == va ? vb : va;
+            s = scatter_u32(c, idxf, nullptr, m, slot_of, m, kfree, vfree);
+            if (s != CAPSSA_OK) return s;
+        }
+        brute_kernel<<<grid_for((uint64_t)S * 32, 256, (unsigned)c.sm_count * 32), 256, 0,
+                       c.stream>>>(K, S, slo, shi, scls, cstate, slot_of, pred);
+        CAPSSA_LAUNCHED(c);
+    }
     kt.mark(c.stream, "scan");
     // 5. first halves, links, places
     const unsigned gS = grid_for(S, 256);

@@ -472,6 +472,38 @@ def test_rank_build_by_window_2p25(ctx):
     assert np.array_equal(got, orc.build_in_memory(t, None, lo))
 
 
+def _runs_of_each_symbol(n, seed):
+    """Random DNA with dozens of long runs of every symbol, some reaching a
+    segment end, so that deep tied groups consist of run suffixes whose runs
+    end in a smaller symbol, a larger one, or the end of the suffix."""
+    rng = np.random.default_rng(seed)
+    t = rng.integers(0, 4, n).astype(np.uint8)
+    ends = np.unique(np.concatenate([rng.integers(1, n, 300), [n]]))
+    for c in range(4):
+        for _ in range(40):
+            L = int(rng.integers(300, 3000))
+            if rng.random() < 0.3:  # up to a segment end
+                e = int(ends[rng.integers(0, len(ends))])
+                a = max(0, e - L)
+            else:
+                a = int(rng.integers(0, n - L))
+            t[a:a + L] = c
+    return t, ends
+
+
+def test_runs_of_one_symbol_deep_groups(ctx):
+    """Groups of thousands of run suffixes tied far past the key: ordered by
+    their run lengths and what ends each run.  PlainText and SegmentedText,
+    bit-exact (the segmented case in the reference's tie order)."""
+    t, ends = _runs_of_each_symbol(1 << 20, seed=21)
+    got = ctx.build_in_memory(t)
+    assert ctx.stats()["refine_rounds"] >= 3
+    assert np.array_equal(got, orc.build_in_memory(t))
+    lp, lo = limits_pair(len(t), ends)
+    got = ctx.build_in_memory(t, lp, capssa.Opts(tie_order=capssa.TieOrder.REFERENCE))
+    assert np.array_equal(got, orc.build_in_memory(t, None, lo))
+
+
 def test_large_text_star_segments(ctx):
     t = _runs_text((1 << 22) + 777, seed=12).astype(np.uint8)
     rng = np.random.default_rng(5)
