@@ -10,13 +10,43 @@ namespace capssa {
 namespace {
 
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 8;
+constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr unsigned long long kA = 1ull << 62, kP = 2ull << 62, kMask = (1ull << 62) - 1;
 
 template <bool MAX>
 __device__ __forceinline__ uint32_t op(uint32_t a, uint32_t b) {
     return MAX ? (a > b ? a : b) : a + b;
+}
+
+// Exclusive prefix (in place) of the kScanItems * 8 (step, warp) totals of
+// a tile, run by warp 0, each lane owning kPer consecutive entries; returns
+// the tile total on every lane.
+template <bool MAX>
+__device__ __forceinline__ uint32_t tile_prefix(uint32_t *tot) {
+    constexpr int kPer = kScanItems * (kScanThreads / 32) / 32;
+    const int lane = threadIdx.x & 31;
+    uint32_t c[kPer], sum = 0u;
+#pragma unroll
+    for (int q = 0; q < kPer; q++) {
+        c[q] = tot[kPer * lane + q];
+        sum = op<MAX>(sum, c[q]);
+    }
+    uint32_t w = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t z = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w = op<MAX>(w, z);
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, w, 31);
+    uint32_t run = __shfl_up_sync(0xffffffffu, w, 1);  // before this lane's entries
+    if (lane == 0) run = 0u;
+#pragma unroll
+    for (int q = 0; q < kPer; q++) {
+        tot[kPer * lane + q] = run;
+        run = op<MAX>(run, c[q]);
+    }
+    return total;
 }
 
 // Decoupled look-back by one whole warp: publishes the tile's aggregate,
@@ -70,7 +100,7 @@ __global__ void __launch_bounds__(kScanThreads)
                 unsigned long long *__restrict__ status, uint32_t *__restrict__ counter,
                 int *__restrict__ err) {
     constexpr int kWarps = kScanThreads / 32;
-    static_assert(kScanItems * kWarps == 64, "two (step, warp) totals per lane of warp 0");
+    static_assert(kScanItems * kWarps % 32 == 0, "whole (step, warp) totals per lane of warp 0");
     __shared__ uint32_t s_tile;
     // each (step, warp)'s total; then the exclusive prefix in entry order
     __shared__ uint32_t s_tot[kScanItems * kWarps];
@@ -98,18 +128,7 @@ __global__ void __launch_bounds__(kScanThreads)
     }
     __syncthreads();
     if (warp == 0) {
-        const uint32_t c0 = s_tot[2 * lane], c1 = s_tot[2 * lane + 1];
-        uint32_t w = op<MAX>(c0, c1);
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t z = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w = op<MAX>(w, z);
-        }
-        const uint32_t tile_total = __shfl_sync(0xffffffffu, w, 31);
-        uint32_t ex = __shfl_up_sync(0xffffffffu, w, 1);  // before this lane's pair
-        if (lane == 0) ex = 0u;
-        s_tot[2 * lane] = ex;
-        s_tot[2 * lane + 1] = op<MAX>(ex, c0);
+        const uint32_t tile_total = tile_prefix<MAX>(s_tot);
         const uint32_t acc = warp_lookback<MAX>(status, tile, tile_total, err);
         if (lane == 0) s_prefix = acc;
     }
@@ -135,7 +154,7 @@ __global__ void __launch_bounds__(kScanThreads)
                   uint64_t off, OT *__restrict__ out, unsigned long long *__restrict__ status,
                   uint32_t *__restrict__ counter, int *__restrict__ err) {
     constexpr int kWarps = kScanThreads / 32;
-    static_assert(kScanItems * kWarps == 64, "two (step, warp) counts per lane of warp 0");
+    static_assert(kScanItems * kWarps % 32 == 0, "whole (step, warp) counts per lane of warp 0");
     __shared__ uint32_t s_tile;
     // kept entries per (step, warp); then their exclusive prefix in entry order
     __shared__ uint32_t s_cnt[kScanItems * kWarps];
@@ -158,17 +177,7 @@ __global__ void __launch_bounds__(kScanThreads)
     }
     __syncthreads();
     if (warp == 0) {
-        const uint32_t c0 = s_cnt[2 * lane], c1 = s_cnt[2 * lane + 1];
-        uint32_t x = c0 + c1;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        const uint32_t tile_total = __shfl_sync(0xffffffffu, x, 31);
-        const uint32_t ex = x - c0 - c1;
-        s_cnt[2 * lane] = ex;
-        s_cnt[2 * lane + 1] = ex + c0;
+        const uint32_t tile_total = tile_prefix<false>(s_cnt);
         const uint32_t acc = warp_lookback<false>(status, tile, tile_total, err);
         if (lane == 0) s_prefix = acc;
     }

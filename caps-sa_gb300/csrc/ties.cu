@@ -409,14 +409,24 @@ __global__ void popc_words_kernel(const uint32_t *__restrict__ bits, uint64_t nw
         wc[w] = __popc(bits[w]);
 }
 
+// (prefix count, bits) of every bitmap word side by side: a rank lookup is
+// one 8-byte load.
+__global__ void rank_words_kernel(const uint32_t *__restrict__ bits,
+                                  const uint32_t *__restrict__ wc, uint64_t nw,
+                                  uint2 *__restrict__ rw) {
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nw;
+         w += (uint64_t)gridDim.x * blockDim.x)
+        rw[w] = make_uint2(wc[w], bits[w]);
+}
+
 // Input index of each slot for ascending positions: the rank of its position
-// among them (words' prefix counts + the bits below it in its word).
+// among them (its word's prefix count + the bits below it in the word).
 __global__ void pos_rank_kernel(const uint32_t *__restrict__ pos32, uint32_t m,
-                                const uint32_t *__restrict__ bits,
-                                const uint32_t *__restrict__ wc, uint32_t *__restrict__ idxf) {
+                                const uint2 *__restrict__ rw, uint32_t *__restrict__ idxf) {
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
         const uint32_t p = pos32[r];
-        idxf[r] = wc[p >> 5] + __popc(bits[p >> 5] & ((1u << (p & 31)) - 1u));
+        const uint2 e = __ldg(rw + (p >> 5));
+        idxf[r] = e.x + __popc(e.y & ((1u << (p & 31)) - 1u));
     }
 }
 
@@ -517,8 +527,9 @@ capssa_status reference_tie_order(Ctx &c, const TieArgs &t) {
     } else if (ascending) {
         const uint64_t nw = (t.lim.n + 1) / 32 + 1;  // position n included
         uint32_t *bits = (uint32_t *)ws_get(c, WS_KEEP, nw * 4 + 64);
-        uint32_t *wc = (uint32_t *)ws_get(c, WS_RANK, nw * 4 + 64);
-        if (!bits || !wc) return set_err(c, CAPSSA_ENOMEM, "tie order workspace");
+        uint2 *rw = (uint2 *)ws_get(c, WS_RANK, nw * 12 + 128);  // rw, then the counts
+        if (!bits || !rw) return set_err(c, CAPSSA_ENOMEM, "tie order workspace");
+        uint32_t *wc = (uint32_t *)(rw + nw);
         CAPSSA_CUDA(c, cudaMemsetAsync(bits, 0, nw * 4, c.stream));
         if (t.pos_bytes == 8)
             pos_bits_kernel<uint64_t><<<g, 256, 0, c.stream>>>((const uint64_t *)t.positions, mm,
@@ -531,7 +542,9 @@ capssa_status reference_tie_order(Ctx &c, const TieArgs &t) {
         CAPSSA_LAUNCHED(c);
         s = scan_u32(c, wc, wc, nw, false, false);
         if (s != CAPSSA_OK) return s;
-        pos_rank_kernel<<<g, 256, 0, c.stream>>>(pos32, mm, bits, wc, idxf);
+        rank_words_kernel<<<grid_for(nw, 256), 256, 0, c.stream>>>(bits, wc, nw, rw);
+        CAPSSA_LAUNCHED(c);
+        pos_rank_kernel<<<g, 256, 0, c.stream>>>(pos32, mm, rw, idxf);
         CAPSSA_LAUNCHED(c);
     } else {
         // inputs and slots, each sorted by position (stably): the j-th of
