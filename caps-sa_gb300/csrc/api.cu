@@ -732,6 +732,14 @@ capssa_status capssa_ctx_create(capssa_ctx **out, int device) {
                 if (cudaEventCreate(&e) != cudaSuccess) return true;
             for (auto &e : c->tune_ev)
                 if (cudaEventCreate(&e) != cudaSuccess) return true;
+            for (auto &st : c->side)
+                if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+                    return true;
+            if (cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess)
+                return true;
+            for (auto &e : c->join_ev)
+                if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+                    return true;
             return false;
         }()) {
         cudaGetLastError();
@@ -772,6 +780,11 @@ void capssa_ctx_destroy(capssa_ctx *ctx) {
     for (auto &e : c->kev)
         if (e) cudaEventDestroy(e);
     for (auto &e : c->tune_ev)
+        if (e) cudaEventDestroy(e);
+    for (auto &st : c->side)
+        if (st) cudaStreamDestroy(st);
+    if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+    for (auto &e : c->join_ev)
         if (e) cudaEventDestroy(e);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;

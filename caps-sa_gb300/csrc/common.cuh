@@ -148,6 +148,12 @@ struct Ctx {
     bool seg_major_done = false;
     uint64_t *h_emit = nullptr;     // pinned double buffer of the emit stream
     uint64_t launches = 0;
+    // side streams: the independent kernels of one refinement round run
+    // concurrently, forked from and joined back to `stream` by events
+    static constexpr int kSide = 4;
+    cudaStream_t side[kSide] = {};
+    cudaEvent_t fork_ev = nullptr;
+    cudaEvent_t join_ev[kSide] = {};
 };
 
 // Returns a device buffer of at least `bytes` for `slot` (nullptr on OOM).

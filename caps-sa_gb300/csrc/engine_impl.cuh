@@ -2922,38 +2922,50 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
         for (int l = 0; l < kLists; l++)
             CAPSSA_CUDA(c, cudaMemsetAsync(&G.ctr->n[l][nxt], 0, 4, c.stream));
         CAPSSA_CUDA(c, cudaMemsetAsync(&G.ctr->big_packed[nxt], 0, 8, c.stream));
+        // the direct kernels work on disjoint groups and only append to the
+        // next round's lists: the four small-group kinds run on side streams
+        // next to the medium kernel on the main one (each alone is latency-
+        // bound and leaves the SMs half idle), joined before rank doubling
+        CAPSSA_CUDA(c, cudaEventRecord(c.fork_ev, c.stream));
+        int forked = 0;
+        auto side = [&]() -> cudaStream_t {
+            cudaStream_t st = c.side[forked];
+            cudaStreamWaitEvent(st, c.fork_ev, 0);
+            forked++;
+            return st;
+        };
         if (cnt[L_PAIR]) {
-            direct_pair_kernel<<<grid_for(cnt[L_PAIR], 256), 256, 0, c.stream>>>(
+            direct_pair_kernel<<<grid_for(cnt[L_PAIR], 256), 256, 0, side()>>>(
                 G.list[L_PAIR][cur], cnt[L_PAIR], sa, hd, rk, a.lim, P, lf, G, nxt);
             CAPSSA_LAUNCHED(c);
-            kt.mark(c.stream, "pair");
         }
         if (cnt[L_TINY]) {
-            direct_tiny_kernel<kTiny4><<<grid_for(cnt[L_TINY], 128), 128, 0, c.stream>>>(
+            direct_tiny_kernel<kTiny4><<<grid_for(cnt[L_TINY], 128), 128, 0, side()>>>(
                 G.list[L_TINY][cur], cnt[L_TINY], sa, hd, rk, a.lim, P, lf, G, nxt);
             CAPSSA_LAUNCHED(c);
-            kt.mark(c.stream, "tiny3-4");
         }
         if (cnt[L_TINY8]) {
             direct_tiny_seg_kernel<kTinyMax>
-                <<<grid_for((uint64_t)cnt[L_TINY8] * kTinyMax, 128), 128, 0, c.stream>>>(
+                <<<grid_for((uint64_t)cnt[L_TINY8] * kTinyMax, 128), 128, 0, side()>>>(
                     G.list[L_TINY8][cur], cnt[L_TINY8], sa, hd, rk, a.lim, P, lf, G, nxt);
             CAPSSA_LAUNCHED(c);
-            kt.mark(c.stream, "tiny5-8");
         }
         if (cnt[L_SMALL]) {
-            direct_warp_kernel<<<grid_for((uint64_t)cnt[L_SMALL] * 32, 128), 128, 0, c.stream>>>(
+            direct_warp_kernel<<<grid_for((uint64_t)cnt[L_SMALL] * 32, 128), 128, 0, side()>>>(
                 G.list[L_SMALL][cur], cnt[L_SMALL], sa, hd, rk, a.lim, P, lf, G, nxt);
             CAPSSA_LAUNCHED(c);
-            kt.mark(c.stream, "small");
         }
         if (cnt[L_MEDIUM]) {
             direct_medium_kernel<<<std::min<unsigned>(cnt[L_MEDIUM], c.sm_count * 8), kMedThreads,
                                    0, c.stream>>>(G.list[L_MEDIUM][cur], cnt[L_MEDIUM], sa, hd,
                                                   rk, a.lim, P, lf, G, nxt);
             CAPSSA_LAUNCHED(c);
-            kt.mark(c.stream, "medium");
         }
+        for (int i = 0; i < forked; i++) {
+            CAPSSA_CUDA(c, cudaEventRecord(c.join_ev[i], c.side[i]));
+            CAPSSA_CUDA(c, cudaStreamWaitEvent(c.stream, c.join_ev[i], 0));
+        }
+        kt.mark(c.stream, "direct");
         // rank doubling last: the direct kernels above rewrote the ranks of
         // every group they resolved, which only refines them (equal ranks
         // still agree through h symbols) and settles the depth-0 groups of
