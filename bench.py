@@ -226,7 +226,12 @@ def run_reference(args):
     oracle.build_in_memory(probe)
     rate = len(probe) / (time.perf_counter() - t0)
     lg = min(22, log2n)
-    while lg < log2n and (1 << (lg + 1)) * 1.25 / rate * args.steps <= REF_BUDGET_S:
+    lg0 = lg
+
+    def est(lg_):  # seconds for all steps: n log n from the probe, with margin
+        return (1 << lg_) * lg_ / (rate * lg0) * 1.3 * args.steps
+
+    while lg < log2n and est(lg + 1) <= REF_BUDGET_S:
         lg += 1
     sample = np.ascontiguousarray(text[: 1 << lg])
     times = []

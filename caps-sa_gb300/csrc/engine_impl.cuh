@@ -615,15 +615,37 @@ __global__ void __launch_bounds__(256)
     __shared__ int s_prev[kInitTile / 32];
     __shared__ uint32_t s_carry;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // pass 1: the heads bitmap; singletons (the bulk) are finished here, and
+    // the records in groups are marked for pass 2 (bit j of m_grp: record j;
+    // m_head / m_last: it heads / ends its group)
+    uint32_t m_grp = 0, m_head = 0, m_last = 0;
     auto heads = [&](auto fast_c) {
         constexpr bool FAST = decltype(fast_c)::value;
 #pragma unroll 4
         for (int j = 0; j < kInitPer; j++) {
             const uint32_t l = j * 256 + threadIdx.x;
-            const bool hb = FAST ? sk[l] != sk[l + 1]
-                                 : l < valid && (base + l == 0 || sk[l] != sk[l + 1]);
-            const uint32_t word = __ballot_sync(0xffffffffu, hb);
+            const bool in = FAST || l < valid;
+            const uint32_t i = base + l;
+            bool head = false, last = false;
+            if (in) {
+                const uint64_t key = sk[l + 1];
+                head = (!FAST && i == 0) || sk[l] != key;
+                last = (!FAST && i == n - 1) || sk[l + 2] != key;
+            }
+            const uint32_t word = __ballot_sync(0xffffffffu, in && head);
             if (lane == 0) s_hb[j * 8 + warp] = word;
+            if (in) {
+                if (head && last) {
+                    // an insertion point only ever falls on a group head, so
+                    // a group moves by one shift
+                    const uint32_t sh = FAST ? sh_lo : shift_of(i);
+                    hd[i + sh] = i + sh;
+                } else {
+                    m_grp |= 1u << j;
+                    m_head |= (head ? 1u : 0u) << j;
+                    m_last |= (last ? 1u : 0u) << j;
+                }
+            }
         }
     };
     if (fast)
@@ -684,25 +706,16 @@ __global__ void __launch_bounds__(256)
     uint32_t ends = 0;                 // bit j: key j ends a group that needs refining
     // only LongerFirst with a length field separates complete ties by position
     const bool lf_field = lf && !flag_len;
-    // pass 1: heads, and the groups this thread ends (singletons, the bulk,
-    // take the shortest path)
+    // pass 2: the group members' heads, and the groups this thread ends
     auto pass1 = [&](auto fast_c) {
         constexpr bool FAST = decltype(fast_c)::value;
-#pragma unroll 4
-        for (int j = 0; j < kInitPer; j++) {
+        for (uint32_t mg = m_grp; mg; mg &= mg - 1) {
+            const int j = __ffs((int)mg) - 1;
             const uint32_t l = j * 256 + threadIdx.x;
-            if (!FAST && l >= valid) break;
             const uint32_t i = base + l;
             const uint64_t key = sk[l + 1];
-            const bool head = (!FAST && i == 0) || sk[l] != key;
-            const bool last = (!FAST && i == n - 1) || sk[l + 2] != key;
-            // an insertion point only ever falls on a group head, so a group
-            // moves by one shift
+            const bool head = (m_head >> j) & 1u, last = (m_last >> j) & 1u;
             const uint32_t sh = FAST ? sh_lo : shift_of(i);
-            if (head && last) {
-                hd[i + sh] = i + sh;
-                continue;
-            }
             const uint32_t g = head ? i : head_of(l);
             bool complete = false;
             uint64_t depth = (uint64_t)k;
@@ -736,7 +749,7 @@ __global__ void __launch_bounds__(256)
         if (total) s_base[li] = atomicAdd(&G.ctr->n[li][0], total);
     }
     __syncthreads();
-    // pass 2: write the entries of the groups found in pass 1
+    // pass 3: write the entries of the groups found in pass 2
     for (; ends; ends &= ends - 1) {
         const int j = __ffs((int)ends) - 1;
         const uint32_t l = j * 256 + threadIdx.x;
