@@ -74,7 +74,7 @@ capssa_status check_dev_flags(Ctx &c) {
 // packed below it when key and position fit 64 bits.  Otherwise the widest
 // key holds kmax symbols (kmax*b + bits(kmax) <= 64) and a length field.
 KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits, int top_bits, uint64_t n_k,
-                 bool allow_flagless) {
+                 bool allow_flagless, bool seg_flag) {
     KeyGeom g{};
     g.b = b < 1 ? 1 : b;
     if (n_k == 0 || n_k > n) n_k = n;
@@ -121,6 +121,31 @@ KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits, int top_bits, uint
         g.total = k * g.b + 1;
         g.vbits = vbits;
         return g;
+    }
+    // segment-major ShorterFirst (many texts in one sort): suffixes from
+    // different texts never tie, so the few that end inside the key need only
+    // an early-end flag (their groups are refined from depth 0), not a length
+    // field; with the flag, one symbol less than kmin when that saves a pass
+    if (seg_flag && top_bits) {
+        int k = kmin;
+        int passes = (top_bits + k * g.b + 1 + 7) / 8;
+        const int passes2 = (top_bits + (k - 1) * g.b + 1 + 7) / 8;
+        if (k - 1 >= 2 && passes2 < passes && top_bits + (k - 1) * g.b + 1 + vbits <= 64) {
+            k--;
+            passes = passes2;
+        }
+        if (top_bits + k * g.b + 1 + vbits <= 64) {
+            while (top_bits + (k + 1) * g.b + 1 <= 8 * passes &&
+                   top_bits + (k + 1) * g.b + 1 + vbits <= 64)
+                k++;
+            g.k = k;
+            g.lbits = 1;
+            g.flag_len = 1;
+            g.total = k * g.b + 1;
+            g.vbits = vbits;
+            g.local_pos = 1;
+            return g;
+        }
     }
     auto lbits_of = [](int k) {
         int lb = 0;

@@ -94,9 +94,11 @@ struct KeyGeom {
 // hbits: entropy of the symbols in bits (<= b).
 // top_bits: bits the caller keeps above the key (a segment index), n_k: the
 // longest run of symbols a key has to tell apart (n when 0), allow_flagless:
-// a ShorterFirst plain text may drop the early-end flag (see KeyGeom).
+// a ShorterFirst plain text may drop the early-end flag (see KeyGeom);
+// seg_flag: a segment-major ShorterFirst sort may mark the suffixes that end
+// inside the key with one flag bit instead of a length field.
 KeyGeom key_geom(int b, uint64_t n, bool plain, double hbits, int top_bits = 0,
-                 uint64_t n_k = 0, bool allow_flagless = false);
+                 uint64_t n_k = 0, bool allow_flagless = false, bool seg_flag = false);
 
 // Key geometry of a partition-first sort: a bucket index of bucket_bits
 // above a window of k symbols taken after the bucket's common prefix, a

@@ -2725,7 +2725,8 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
         }
     } else {
         geo = key_geom(b, n, !a.lim.segmented, hbits, seg_bits,
-                       seg_bits ? a.seg_max_len : (sp ? sp->m : 0), allow_flagless);
+                       seg_bits ? a.seg_max_len : (sp ? sp->m : 0), allow_flagless,
+                       a.seg_major && !lf);
     }
     // records the radix sort orders: every suffix, or the full ones only
     const uint64_t n_short = geo.flagless ? (uint64_t)geo.k - 1 : 0;
