@@ -281,7 +281,8 @@ FORMS = ("sample_sort", "batched", "segmented_filtered")
 def run_forms(ctx, t_dev, n, only=FORMS):
     """The secondary forms of the metric, each on its own workload:
     sample sort of the bench text with p = 4096 partitions found by splitter
-    binary search vs the learned CDF model (65,536 training samples); 8,192
+    search (indexed by the pivots' leading key bits, or a plain bisection over
+    all pivots) vs the learned CDF model (16,384 training samples); 8,192
     independent texts sorted in one batched call vs a per-text loop; the
     segmented, filtered subset build (n = 2^29, u64 index).  `only` picks
     some of them (bench.py --form)."""
@@ -303,6 +304,7 @@ def form_sample_sort(ctx, t_dev, n):
     # chunk order comes from a full sort first
     ss = {}
     for name, part, smp in (("splitters", capssa.Partition.SPLITTERS, capssa.Sampling.AUTO),
+                            ("bisection", capssa.Partition.BISECT, capssa.Sampling.AUTO),
                             ("learned", capssa.Partition.LEARNED, capssa.Sampling.AUTO),
                             ("reference_rule_sort_first", capssa.Partition.SPLITTERS,
                              capssa.Sampling.REFERENCE)):

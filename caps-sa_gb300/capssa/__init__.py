@@ -80,6 +80,7 @@ class Partition(enum.IntEnum):
     AUTO = 0
     SPLITTERS = 1
     LEARNED = 2
+    BISECT = 3
 
 
 class Sampling(enum.IntEnum):

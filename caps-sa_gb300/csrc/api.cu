@@ -447,6 +447,14 @@ capssa_status build_common(Ctx &c, const ST *text, uint64_t n, const void *posit
     return CAPSSA_OK;
 }
 
+// The partition a sample-sort call asked for (AUTO: splitter search).
+int part_mode(const capssa_opts *opts) {
+    if (opts && (opts->partition == CAPSSA_PARTITION_LEARNED ||
+                 opts->partition == CAPSSA_PARTITION_BISECT))
+        return opts->partition;
+    return CAPSSA_PARTITION_SPLITTERS;
+}
+
 // effective_subproblem_count (src/ext_mem.rs:1159-1178)
 uint64_t effective_p(uint64_t n, uint64_t requested, int threads) {
     if (n == 0) return 0;
@@ -510,8 +518,7 @@ capssa_status sample_sort_common(Ctx &c, const ST *text, uint64_t n, const uint6
     if (!d_sa) return set_err(c, CAPSSA_ENOMEM, "output buffer");
     PartRequest pr{(uint32_t)effective_p(count, opts ? opts->subproblem_count : 0,
                                          opts ? opts->host_threads : 0),
-                   opts && opts->partition == CAPSSA_PARTITION_LEARNED ? CAPSSA_PARTITION_LEARNED
-                                                                       : CAPSSA_PARTITION_SPLITTERS,
+                   part_mode(opts),
                    nullptr, nullptr};
     capssa_status s =
         build_common<ST>(c, text, n, positions, 8, m, lp, opts, d_sa, 8, nullptr, &pr);
@@ -1098,8 +1105,7 @@ capssa_status plan_common(Ctx &c, const ST *text, uint64_t n, const uint64_t *po
     uint64_t *d_sa = (uint64_t *)ws_get(c, WS_OUT, count * 8 + 64);
     if (!d_sa) return set_err(c, CAPSSA_ENOMEM, "output buffer");
     PartRequest pr{(uint32_t)p,
-                   opts && opts->partition == CAPSSA_PARTITION_LEARNED ? CAPSSA_PARTITION_LEARNED
-                                                                       : CAPSSA_PARTITION_SPLITTERS,
+                   part_mode(opts),
                    pivots, sizes};
     return build_common<ST>(c, text, n, positions, 8, m, lp, opts, d_sa, 8, nullptr, &pr);
 }

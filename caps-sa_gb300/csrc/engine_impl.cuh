@@ -2168,7 +2168,7 @@ __global__ void __launch_bounds__(kKeyThreads)
                   int lf, int n_passes, int bucket_shift, const uint64_t *__restrict__ pkey,
                   const uint32_t *__restrict__ ppos, const uint64_t *__restrict__ plim,
                   const uint16_t *__restrict__ ell, const uint16_t *__restrict__ tbl, uint32_t p,
-                  const __nv_bfloat16 *__restrict__ w,
+                  const __nv_bfloat16 *__restrict__ w, int bisect,
                   uint64_t *__restrict__ keys, uint32_t *__restrict__ counts,
                   unsigned long long *__restrict__ sizes, unsigned long long *__restrict__ stats,
                   int *__restrict__ fallback) {
@@ -2288,9 +2288,10 @@ __global__ void __launch_bounds__(kKeyThreads)
                 bk[e] = lo;
                 mis += lo != guess ? 1u : 0u;
             } else {
-                // binary search between the pivots that share the key's top bits
+                // binary search between the pivots that share the key's top
+                // bits (or over all of them: bisect)
                 const uint32_t top = (uint32_t)(K[e] >> (64 - kPfTableBits));
-                uint32_t lo = stbl[top], hi = stbl[top + 1];
+                uint32_t lo = bisect ? 0u : stbl[top], hi = bisect ? n_piv : stbl[top + 1];
                 while (lo < hi) {
                     const uint32_t mid = (lo + hi) >> 1;
                     if (greater(mid))
@@ -2451,6 +2452,7 @@ struct SparseRun {
 struct PfRun {
     uint32_t p = 0;
     bool learned = false;
+    bool bisect = false;  // splitter search over all pivots, without the top-bits index
     bool fell_back = false;                  // out: a comparison ran too deep; nothing sorted
     const uint32_t *d_pivots = nullptr;      // out: device, p - 1 pivot positions
     const unsigned long long *d_sizes = nullptr;  // out: device, p bucket sizes + 2 stats
@@ -2586,7 +2588,8 @@ capssa_status pf_keys(Ctx &c, const EngineArgs &a, const eng::Packed &P, const K
                              (int)smem);                                                          \
         pf_key_kernel<PL, LE><<<grid, kKeyThreads, smem, c.stream>>>(                             \
             P, n, a.lim, geo.k, geo.lbits, geo.flag_len, geo.vbits, lf, key_passes, geo.total,    \
-            pkey, ppos, plim, ell, tbl, p, wbf, keys, counts, sizes, sizes + p, fb);               \
+            pkey, ppos, plim, ell, tbl, p, wbf, pf->bisect ? 1 : 0, keys, counts, sizes, sizes + p, \
+            fb);                                                                                   \
     } while (0)
     cudaEventRecord(q0, c.stream);
     if (plain && pf->learned)
@@ -3468,6 +3471,7 @@ capssa_status engine_build_t(Ctx &c, const EngineArgs &a) {
         PfRun pf;
         pf.p = a.part_p;
         pf.learned = a.part_mode == CAPSSA_PARTITION_LEARNED;
+        pf.bisect = a.part_mode == CAPSSA_PARTITION_BISECT;
         capssa_status s = core_sort<S>(c, a, &sa, &P, &pf);
         if (s != CAPSSA_OK) return s;
         if (!pf.fell_back) {

@@ -75,7 +75,11 @@ typedef enum {
     /* as SPLITTERS, but a small MLP trained on the splitter sample
      * predicts the bucket; every prediction is checked against its two
      * neighbouring splitters and corrected */
-    CAPSSA_PARTITION_LEARNED = 2
+    CAPSSA_PARTITION_LEARNED = 2,
+    /* as SPLITTERS, but a plain binary search over all the splitters (the
+     * reference's upper_bound_by_pivot, src/ext_mem.rs:1705-1734), without
+     * the index of the splitters' leading key bits */
+    CAPSSA_PARTITION_BISECT = 3
 } capssa_partition;
 
 /* Where the sample sort's splitter sample comes from. */

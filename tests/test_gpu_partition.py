@@ -254,6 +254,16 @@ def test_partition_first_plain_bit_exact(ctx, p):
     assert st["partitions"] == p and st["partition_probes"] > 0
 
 
+def test_partition_first_bisection(ctx):
+    """The plain binary search over all pivots (no index of their leading
+    key bits) finds the same buckets with log2(p) probes per suffix."""
+    t = _dna(1 << 20, seed=41)
+    st = check_pf(ctx, t, 1024, partition=capssa.Partition.BISECT)
+    assert st["partition_probes"] >= 9 * len(t)
+    st2 = check_pf(ctx, t, 1024)
+    assert st2["partition_probes"] < st["partition_probes"] / 4
+
+
 def test_partition_first_learned(ctx):
     t = _dna(1 << 20, seed=40)
     st = check_learned_pf(ctx, t, 1024)
