@@ -1032,6 +1032,24 @@ __device__ __forceinline__ int direct_cmp(const Packed &P, uint64_t a, uint64_t 
             A[q] = q < nwa ? __ldg(wa + q) : 0ull;
             B[q] = q < nwb ? __ldg(wb + q) : 0ull;
         }
+        if (wbits == 64) {
+            // whole-word windows (b divides 64, e.g. DNA): window s starts in
+            // word s of both bursts, no runtime word selection
+#pragma unroll
+            for (int s = 0; s < kBurst; s++) {
+                if (t >= end) break;
+                const uint64_t va = sha ? (A[s] << sha) | (A[s + 1] >> (64 - sha)) : A[s];
+                const uint64_t vb = shb ? (B[s] << shb) | (B[s + 1] >> (64 - shb)) : B[s];
+                const uint64_t x = va ^ vb;
+                if (x) {
+                    const uint64_t d = (uint64_t)__clzll((long long)x) / (uint64_t)P.b;
+                    if (t + d < end) return va < vb ? -1 : 1;
+                    t = end;
+                    break;
+                }
+                t += (uint64_t)P.spw;
+            }
+        } else {
         uint32_t bit_a = sha, bit_b = shb;
 #pragma unroll
         for (int s = 0; s < kBurst; s++) {
@@ -1052,6 +1070,7 @@ __device__ __forceinline__ int direct_cmp(const Packed &P, uint64_t a, uint64_t 
             bit_a += (uint32_t)(P.spw * P.b);
             bit_b += (uint32_t)(P.spw * P.b);
             t += (uint64_t)P.spw;
+        }
         }
     }
     if (t < end) {
