@@ -237,6 +237,73 @@ __global__ void __launch_bounds__(kKeyThreads)
         if (hist[i]) atomicAdd(&counts[i], hist[i]);
 }
 
+// key_kernel for a plain text in the flagless geometry when a radix digit
+// holds whole symbols (b divides 8) and the key whole digits.  Every record
+// is a full window (p <= n - k), so there is no limit, flag or segment
+// logic; a thread's kKeyPer windows lie in the two packed words at its
+// first position (its bit offset is a multiple of 8b, so offset + 7b < 64).
+// Only pass 0's digit histogram is counted: key_hist_shift_kernel derives
+// the other passes' from it.
+__global__ void __launch_bounds__(kKeyThreads)
+    key_flagless_kernel(Packed P, uint64_t n_rec, int kbits, int vbits,
+                        uint64_t *__restrict__ keys, uint32_t *__restrict__ counts) {
+    static_assert(kKeyThreads == 256 && kKeyPer == 8, "one thread per digit; 8 windows per word pair");
+    __shared__ uint32_t hist[256];
+    hist[threadIdx.x] = 0;
+    __syncthreads();
+    const int b = P.b;
+    for (uint64_t t0 = (uint64_t)blockIdx.x * kKeyTile; t0 < n_rec;
+         t0 += (uint64_t)gridDim.x * kKeyTile) {
+        const uint64_t p0 = t0 + (uint64_t)threadIdx.x * kKeyPer;
+        if (p0 >= n_rec) continue;
+        const uint64_t bit0 = p0 * (uint64_t)b;
+        const uint64_t w0 = __ldg(P.w + (bit0 >> 6)), w1 = __ldg(P.w + (bit0 >> 6) + 1);
+        const uint32_t sh0 = (uint32_t)(bit0 & 63);
+        uint64_t out[kKeyPer];
+#pragma unroll
+        for (int e = 0; e < kKeyPer; e++) {
+            const uint32_t sh = sh0 + (uint32_t)(e * b);
+            const uint64_t content = ((w0 << sh) | ((w1 >> 1) >> (63 - sh))) >> (64 - kbits);
+            if (p0 + e < n_rec) atomicAdd(&hist[(uint32_t)content & 255u], 1u);
+            out[e] = (content << vbits) | (p0 + e);
+        }
+        if (p0 + kKeyPer <= n_rec) {
+            uint4 *dst = reinterpret_cast<uint4 *>(keys + p0);
+#pragma unroll
+            for (int e = 0; e < kKeyPer; e += 2)
+                dst[e / 2] = make_uint4((uint32_t)out[e], (uint32_t)(out[e] >> 32),
+                                        (uint32_t)out[e + 1], (uint32_t)(out[e + 1] >> 32));
+        } else {
+            for (int e = 0; e < kKeyPer; e++)
+                if (p0 + e < n_rec) keys[p0 + e] = out[e];
+        }
+    }
+    __syncthreads();
+    if (hist[threadIdx.x]) atomicAdd(&counts[threadIdx.x], hist[threadIdx.x]);
+}
+
+// Digit histograms of radix passes 1.. from pass 0's (key_flagless_kernel).
+// Digit j of record p is the s8 = 8 / b symbols at p + k - (j + 1) s8, which
+// is digit 0 of record p - j s8.  So pass j counts pass 0's records except
+// the last j s8, plus digit j of the first j s8 records (needs n_rec >= j s8).
+// One block of 256 threads, one per digit value.
+__global__ void key_hist_shift_kernel(Packed P, uint64_t n_rec, int kbits, int n_passes,
+                                      uint32_t *__restrict__ counts) {
+    const uint32_t x = threadIdx.x;
+    const uint32_t h0 = counts[x];
+    const uint64_t s8 = 8 / (uint64_t)P.b;
+    for (int j = 1; j < n_passes; j++) {
+        uint32_t h = h0;
+        for (uint64_t q = 0; q < (uint64_t)j * s8; q++) {
+            const uint64_t tail = window_at(P, n_rec - 1 - q) >> (64 - kbits);
+            const uint64_t head = window_at(P, q) >> (64 - kbits);
+            h -= ((uint32_t)tail & 255u) == x ? 1u : 0u;
+            h += ((uint32_t)(head >> (8 * j)) & 255u) == x ? 1u : 0u;
+        }
+        counts[j * 256 + x] = h;
+    }
+}
+
 // Composite key of each of m chosen positions (a subset sorted on its own):
 // the same record as key_kernel's, read at pos[i] (distinct, ascending,
 // < n), with the digit histograms of every radix pass.
@@ -2815,6 +2882,13 @@ capssa_status core_sort(Ctx &c, const EngineArgs &a, uint32_t **sa_out, eng::Pac
         if (!vbits)  // the record's value is its position
             CAPSSA_CUDA(c, cudaMemcpyAsync(vals_a, sp->pos, (size_t)N * 4, cudaMemcpyDeviceToDevice,
                                            c.stream));
+    } else if (!a.lim.segmented && !seg_bits && geo.flagless && vbits && 8 % geo.b == 0 &&
+               geo.total % 8 == 0 && key_passes == geo.total / 8 && n_rec >= 64) {
+        key_flagless_kernel<<<kgrid, kKeyThreads, 0, c.stream>>>(P, n_rec, geo.total, vbits,
+                                                                 keys_a, counts);
+        CAPSSA_LAUNCHED(c);
+        key_hist_shift_kernel<<<1, 256, 0, c.stream>>>(P, n_rec, geo.total, key_passes, counts);
+        CAPSSA_LAUNCHED(c);
     } else if (!a.lim.segmented && !seg_bits) {
         key_kernel<true><<<kgrid, kKeyThreads, 0, c.stream>>>(
             P, n, n_rec, a.lim, geo.k, geo.lbits, geo.flag_len, vbits, lf, key_passes, 0, 0,
