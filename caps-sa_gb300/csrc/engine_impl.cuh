@@ -1527,11 +1527,16 @@ __global__ void __launch_bounds__(128)
     }
 }
 
-// Tied groups of 9..32 members: one warp per group, one lane per member.
-// Every lane compares its member with all others (direct comparisons past
-// the shared depth, ties by position), so its rank in the group is a count
-// and the relation to its sorted predecessor is already known.  Groups
-// deeper than kDirectMaxH are left to rank doubling.
+// Tied groups of 9..32 members: one warp per group, one lane per member, in
+// rounds of four windows like direct_tiny_seg_kernel: every lane whose
+// member is still undecided loads its next four windows (one round trip
+// for the group) and compares them with every other member's through
+// shuffles, settling the relations that differ in them (relations settle
+// in both lanes at once, so a settled member's windows are not needed
+// again).  Near a member's end or the horizon the rest is settled by
+// direct_cmp (ties by position).  A member's place is the count of members
+// before it, so the relation to its sorted predecessor is already known.
+// Groups deeper than kDirectMaxH are left to rank doubling.
 __global__ void direct_warp_kernel(const uint4 *__restrict__ groups, uint32_t count,
                                    uint32_t *__restrict__ sa, uint32_t *__restrict__ hd,
                                    uint32_t *__restrict__ rank, DevLimits L, Packed P, int lf,
@@ -1539,49 +1544,77 @@ __global__ void direct_warp_kernel(const uint4 *__restrict__ groups, uint32_t co
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t span = 4 * (uint64_t)P.spw;
     for (uint64_t gi = warp; gi < count; gi += nwarps) {
         const uint4 g = groups[gi];
         const uint32_t len = g.y;
         const uint64_t o = g.z;
         const uint64_t cap = o > kDirectCap ? o : kDirectCap;
+        const uint64_t horizon = o + cap;
         const bool mine = lane < len;
         const uint32_t my_p = mine ? sa[g.x + lane] : 0u;
-        const uint64_t my_l = mine ? dev_lim_at(L, my_p) : 0ull;
-        uint32_t before = 0;
-        uint64_t rel = 0;  // 2 bits per other member j: code of cmp(j, mine)
-        for (uint32_t j = 0; j < len; j++) {
-            uint32_t pj = __shfl_sync(0xffffffffu, my_p, j);
-            uint64_t lj = __shfl_sync(0xffffffffu, my_l, j);
-            if (mine && j != lane) {
-                int r = direct_cmp(P, pj, lj, my_p, my_l, o, cap, lf);
-                bool j_first = r == -1 || ((r == 0 || r == 2) && pj < my_p);
-                before += j_first ? 1u : 0u;
-                rel |= (uint64_t)(r == -1 ? 0 : r == 1 ? 1 : r == 0 ? 2 : 3) << (2 * j);
-            }
-        }
-        // my sorted predecessor and whether I start a subgroup
-        bool start = true;
-        int my_rel = -1;
-        for (uint32_t j = 0; j < len; j++) {
-            uint32_t bj = __shfl_sync(0xffffffffu, before, j);
-            if (mine && before > 0 && bj + 1 == before) {
-                uint32_t code = (uint32_t)(rel >> (2 * j)) & 3u;
-                if (code >= 2) {
-                    start = false;
-                    my_rel = code == 2 ? 0 : 2;
+        const uint32_t my_l = mine ? (uint32_t)dev_lim_at(L, my_p) : 0xFFFFFFFFu;
+        const uint32_t lmin = __reduce_min_sync(0xffffffffu, my_l);
+        const uint64_t minend = lmin < horizon ? lmin : horizon;
+        const uint32_t members = len >= 32 ? 0xFFFFFFFFu : (1u << len) - 1u;
+        uint32_t und = mine ? members & ~(1u << lane) : 0u;  // bit u: not settled with u
+        uint32_t before = 0, tie = 0, undc = 0;  // tie / undc: bit u, relation with u
+        uint64_t base = o;
+        while (__any_sync(0xffffffffu, und != 0)) {
+            if (base + span <= minend) {
+                uint64_t w[4] = {0, 0, 0, 0};
+                if (und) windows4_at(P, (uint64_t)my_p + base, w);
+                for (uint32_t u = 0; u < len; u++) {
+                    int r = 0;
+#pragma unroll
+                    for (int q = 3; q >= 0; q--) {
+                        const uint64_t wu = __shfl_sync(0xffffffffu, w[q], u);
+                        r = w[q] != wu ? (w[q] < wu ? -1 : 1) : r;
+                    }
+                    if (((und >> u) & 1u) && r) {
+                        before += r > 0 ? 1u : 0u;
+                        und &= ~(1u << u);
+                    }
                 }
+                base += span;
+            } else {
+                for (uint32_t u = 0; u < len; u++) {
+                    const uint32_t b = __shfl_sync(0xffffffffu, my_p, u);
+                    const uint32_t lb = __shfl_sync(0xffffffffu, my_l, u);
+                    if ((und >> u) & 1u) {
+                        const int r = direct_cmp(P, my_p, my_l, b, lb, base, horizon - base, lf);
+                        const bool me_first = r == -1 || ((r == 0 || r == 2) && my_p < b);
+                        before += me_first ? 0u : 1u;
+                        if (r == 0) tie |= 1u << u;
+                        if (r == 2) undc |= 1u << u;
+                    }
+                }
+                und = 0;
             }
         }
-        unsigned starts = __reduce_or_sync(0xffffffffu, (mine && start) ? (1u << before) : 0u);
+        // sorted slot, relation to the slot before, tie-run heads
+        const uint32_t slot = before;
+        bool ptie = false, popen = false;
+        for (uint32_t u = 0; u < len; u++) {
+            const uint32_t su = __shfl_sync(0xffffffffu, slot, u);
+            if (mine && u != lane && su + 1 == slot) {
+                ptie = (tie >> u) & 1u;
+                popen = (undc >> u) & 1u;
+            }
+        }
+        const uint32_t starts = __reduce_or_sync(
+            0xffffffffu, (mine && (slot == 0 || (!ptie && !popen))) ? (1u << slot) : 0u);
+        const uint32_t undec =
+            __reduce_or_sync(0xffffffffu, (mine && slot > 0 && popen) ? (1u << slot) : 0u);
         if (mine) {
-            uint32_t head = 31u - (uint32_t)__clz((int)(starts & (before == 31 ? 0xffffffffu
-                                                                     : ((2u << before) - 1u))));
-            sa[g.x + before] = my_p;
-            hd[g.x + before] = g.x + head;
+            const uint32_t head = 31u - (uint32_t)__clz((int)(starts & ((2u << slot) - 1u)));
+            sa[g.x + slot] = my_p;
+            hd[g.x + slot] = g.x + head;
             if (rank) rank[my_p] = g.x + head;
-            bool last = before + 1 == len || ((starts >> (before + 1)) & 1u);
-            if (last && before > head && my_rel == 2)
-                append_group(G, nxt, g.x + head, before - head + 1, o + cap);
+            // slot == 31 only when len == 32, so the shift below stays < 32
+            const bool run_end = slot + 1 == len || ((starts >> (slot + 1)) & 1u);
+            if (run_end && head < slot && ((undec >> slot) & 1u))
+                append_group(G, nxt, g.x + head, slot - head + 1, o + cap);
         }
     }
 }
