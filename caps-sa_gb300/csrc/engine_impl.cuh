@@ -1433,8 +1433,9 @@ __global__ void __launch_bounds__(128)
 // the next four windows of its member (one round trip for the group),
 // exchanges them with its group by shuffles and settles its undecided
 // relations that differ in them.  Near a member's end or the horizon the
-// rest is settled by direct_cmp.  A member's place is the count of members
-// before it.
+// rest is settled by direct_cmp, the other member's position and limit
+// taken by shuffles in a loop every lane runs (no per-member arrays).  A
+// member's place is the count of members before it.
 template <int S>
 __global__ void __launch_bounds__(128)
     direct_tiny_seg_kernel(const uint4 *__restrict__ groups, uint32_t count,
@@ -1451,17 +1452,13 @@ __global__ void __launch_bounds__(128)
     const uint64_t cap = o > kDirectCap ? o : kDirectCap;
     const uint64_t horizon = o + cap;
     const uint32_t my_p = mine ? sa[g.x + sl] : 0u;
-    const uint32_t my_lim = mine ? (uint32_t)dev_lim_at(L, my_p) : 0u;
-    uint32_t op[S], ol[S];
-    uint32_t und = 0;  // bit u: relation with member u not settled yet
-    uint64_t minend = horizon;
+    const uint32_t my_lim = mine ? (uint32_t)dev_lim_at(L, my_p) : 0xFFFFFFFFu;
+    uint32_t lmin = my_lim;
 #pragma unroll
-    for (int u = 0; u < S; u++) {
-        op[u] = __shfl_sync(0xffffffffu, my_p, sb + u);
-        ol[u] = __shfl_sync(0xffffffffu, my_lim, sb + u);
-        if (u < len) minend = ol[u] < minend ? ol[u] : minend;
-        if (mine && u != (int)sl && u < len) und |= 1u << u;
-    }
+    for (int x = 1; x < S; x <<= 1) lmin = min(lmin, __shfl_xor_sync(0xffffffffu, lmin, x));
+    const uint64_t minend = lmin < horizon ? lmin : horizon;
+    // bit u: relation with member u not settled yet
+    uint32_t und = mine ? ((1u << len) - 1u) & ~(1u << sl) : 0u;
     uint32_t before = 0, tie = 0, undc = 0;  // tie / undc: bit u, relation with u
     const uint64_t span = 4 * (uint64_t)P.spw;
     uint64_t base = o;
@@ -1483,20 +1480,24 @@ __global__ void __launch_bounds__(128)
                 und &= ~(1u << u);
             }
         }
-        if (fast) {
-            base += span;
-        } else {
-            for (uint32_t m = und; m; m &= m - 1) {
-                const int u = __ffs((int)m) - 1;
-                const uint32_t b = pick32(op, u), lb = pick32(ol, u);
-                const int r = direct_cmp(P, my_p, my_lim, b, lb, base, horizon - base, lf);
-                const bool me_first = r == -1 || ((r == 0 || r == 2) && my_p < b);
-                before += me_first ? 0u : 1u;
-                if (r == 0) tie |= 1u << u;
-                if (r == 2) undc |= 1u << u;
+        if (__any_sync(0xffffffffu, !fast && und != 0)) {
+#pragma unroll 1
+            for (int u = 0; u < S; u++) {
+                const uint32_t b = __shfl_sync(0xffffffffu, my_p, sb + u);
+                const uint32_t lb = __shfl_sync(0xffffffffu, my_lim, sb + u);
+                if (!fast && ((und >> u) & 1u)) {
+                    const int r = direct_cmp(P, my_p, my_lim, b, lb, base, horizon - base, lf);
+                    const bool me_first = r == -1 || ((r == 0 || r == 2) && my_p < b);
+                    before += me_first ? 0u : 1u;
+                    if (r == 0) tie |= 1u << u;
+                    if (r == 2) undc |= 1u << u;
+                }
             }
-            und = 0;
         }
+        if (fast)
+            base += span;
+        else
+            und = 0;
     }
     // sorted slot, relation to the slot before, tie-run heads
     const uint32_t slot = before;

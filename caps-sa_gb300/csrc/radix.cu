@@ -340,10 +340,6 @@ capssa_status sort_impl(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *ke
         }
         CAPSSA_CUDA(c, cudaMemcpyAsync(offsets, h_off + p * kRadix, kRadix * 4,
                                        cudaMemcpyHostToDevice, c.stream));
-        CAPSSA_CUDA(c, cudaMemsetAsync(status, 0, (size_t)n_tiles * kRadix * 8, c.stream));
-        CAPSSA_CUDA(c, cudaMemsetAsync(tile_counter, 0, 4, c.stream));
-        const bool timed = passes_run && (*passes_run) < 16;
-        if (timed) cudaEventRecord(c.kev[2 * (*passes_run)], c.stream);
         const uint64_t *ki = in_b ? keys_b : keys_a;
         const uint32_t *vi = in_b ? vals_b : vals_a;
         uint64_t *ko = in_b ? keys_a : keys_b;
@@ -379,10 +375,16 @@ capssa_status sort_impl(Ctx &c, uint64_t *keys_a, uint32_t *vals_a, uint64_t *ke
                         shape = cand[q];
                     }
                 }
-                CAPSSA_CUDA(c, cudaMemsetAsync(status, 0, (size_t)n_tiles * kRadix * 8, c.stream));
-                CAPSSA_CUDA(c, cudaMemsetAsync(tile_counter, 0, 4, c.stream));
             }
         }
+        // status words of this shape's tiles only (the buffer is sized for the
+        // smallest tile any shape uses)
+        const uint64_t tile_recs = (uint64_t)kThreads * (uint64_t)shape;
+        const uint64_t pass_tiles = ((uint64_t)n + tile_recs - 1) / tile_recs;
+        CAPSSA_CUDA(c, cudaMemsetAsync(status, 0, (size_t)pass_tiles * kRadix * 8, c.stream));
+        CAPSSA_CUDA(c, cudaMemsetAsync(tile_counter, 0, 4, c.stream));
+        const bool timed = passes_run && (*passes_run) < 16;
+        if (timed) cudaEventRecord(c.kev[2 * (*passes_run)], c.stream);
         c.stats.radix_items = (uint32_t)shape;
         launch_pass(c, mode, shape, ki, vi, ko, vo, n, begin_bit + 8 * p, offsets, status,
                     tile_counter, val_base);
