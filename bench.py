@@ -60,11 +60,17 @@ def workload(log2n, seed=2):
 
 
 def config(log2n, n):
+    # working set: two 8-byte record buffers per suffix, plus the text
+    ws_bytes = 16 * n + n
+    l2 = ("no flush: inputs (%d MiB text, ~%.1f GiB working set) exceed the 129 MB L2"
+          % (n >> 20, ws_bytes / 2**30) if ws_bytes > 129e6 else
+          "no flush; a small case whose working set (%.1f MiB) fits the 129 MB L2"
+          % (ws_bytes / 2**20))
     return {"workload": "dna-repeats: n=2^%d u8 over {0,1,2,3}, 30%% planted repeats "
                         "(log-uniform 100..10000, 1%% substitutions), build_in_memory "
                         "PlainText, u32 index" % log2n,
             "n": n, "symbol": "u8", "index": "u32", "limits": "PlainText",
-            "l2": "no flush: inputs (256 MiB text, ~4 GiB working set) exceed the 129 MB L2",
+            "l2": l2,
             "parallelism": "replicas (one independent text per GPU)"}
 
 
