@@ -125,6 +125,25 @@ def test_random_plain(ctx, dtype, sigma):
         check_against_oracle(ctx, t)
 
 
+@pytest.mark.parametrize("sigma,geometry", [(2, (24, 1, 8)), (16, (8, 4, 8)), (200, (6, 8, 12))])
+def test_flagless_keys_other_symbol_widths(ctx, sigma, geometry):
+    """Plain texts of 2^21 + 37 symbols over 2, 16 and 200 symbols.  Codes of
+    1 and 4 bits take the flagless geometry with whole radix digits (24 and 8
+    symbols, 8-byte records), so the key kernel that counts one digit
+    histogram and shifts it for the other passes runs for widths other than
+    DNA's; 8-bit codes take 6 symbols and a length field (12-byte records).
+    A long run and a periodic stretch give deep groups.  Bit-exact with the
+    oracle."""
+    rng = np.random.default_rng(0xF1A6 + sigma)
+    t = rng.integers(0, sigma, (1 << 21) + 37).astype(np.uint8)
+    t[5000:25000] = 1
+    t[100000:130000] = np.tile(np.array([0, sigma - 1], dtype=np.uint8), 15000)
+    got = ctx.build_in_memory(t)
+    st = ctx.stats()
+    assert (st["key_symbols"], st["key_bits_per_symbol"], st["sort_item_bytes"]) == geometry
+    assert np.array_equal(got, orc.build_in_memory(t))
+
+
 def test_long_runs_and_periodic(ctx):
     check_against_oracle(ctx, np.full(20000, 7, dtype=np.uint8))
     check_against_oracle(ctx, (np.arange(30000) % 3).astype(np.uint8))
