@@ -1233,7 +1233,7 @@ __global__ void __launch_bounds__(256)
 // the SA slice and heads (and ranks once they exist), and passes a pair
 // still undecided after max(g.z, kDirectCap) more symbols to the next
 // round with that larger depth.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 5)
     direct_pair_kernel(const uint4 *__restrict__ groups, uint32_t count, uint32_t *__restrict__ sa,
                        uint32_t *__restrict__ hd, uint32_t *__restrict__ rank, DevLimits L,
                        Packed P, int lf, GroupLists G, int nxt) {
